@@ -1,0 +1,188 @@
+/*
+ * pysit_gb300.h -- C ABI of libpysit_gb300.so, the GB300 (sm_103a) engine for
+ * PySIT's time-domain constant-density acoustic solver with PML and its
+ * adjoint-state FWI gradient.
+ *
+ * Conventions for every entry point:
+ *   - plain pointers and sizes only; array pointers marked "dev" are device
+ *     pointers (e.g. torch.Tensor.data_ptr()), "host" are host pointers;
+ *   - all wavefield arrays are C-contiguous with z the fastest axis, exactly the
+ *     reference layout (idx = i*nz + k in 2D, (i*ny + j)*nz + k in 3D);
+ *   - dtype is PYSIT_F32 or PYSIT_F64 and applies to every array argument of a
+ *     kernel call (the reference's SWIG typemaps also demand one dtype,
+ *     constant_density_acoustic_time_scalar.i:16-42);
+ *   - `stream` is a cudaStream_t (0 = legacy default stream);
+ *   - the return value is PYSIT_OK (0) or a negative PYSIT_E* code, and
+ *     pysit_cuda_last_error() returns a message for the calling thread;
+ *   - no C++ exception crosses the ABI; the library holds no host threads.
+ */
+#ifndef PYSIT_GB300_H
+#define PYSIT_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PYSIT_OK          0
+#define PYSIT_EINVAL     -1  /* bad argument (shape, order, dtype, alignment, size) */
+#define PYSIT_ECUDA      -2  /* CUDA runtime error */
+#define PYSIT_ENONFINITE -3  /* NaN/Inf found in a wavefield (unstable CFL) */
+#define PYSIT_ESTATE     -4  /* call out of order (e.g. no workspace bound) */
+
+#define PYSIT_F32 0
+#define PYSIT_F64 1
+
+/* Message describing the last error on the calling thread ("" if none). */
+const char* pysit_cuda_last_error(void);
+/* Library ABI version (major*1000 + minor). */
+int pysit_cuda_version(void);
+
+/* ------------------------------------------------------------------------
+ * Per-step kernels: one leapfrog step over the whole padded grid.
+ * Same argument order and meaning as the reference templates, minus SWIG's
+ * (rows, cols) pairs:
+ *   pysit_cda_step_1d  <- cda_time_scalar_1D  (pysit/solvers/constant_density_acoustic/
+ *                         time/scalar/constant_density_acoustic_time_scalar_1D.h:44-56)
+ *   pysit_cda_step_2d  <- cda_time_scalar_2D  (..._2D.h:43-61)
+ *   pysit_cda_step_3d  <- cda_time_scalar_3D  (..._3D.h:46-72)
+ * bound through SWIG at constant_density_acoustic_time_scalar.i:57-84 and
+ * called from ConstantDensityAcousticTimeScalar_{1,2,3}D_cpp.time_step
+ * (..._1D.py:138-158, _2D.py:166-190, _3D.py:194-227).
+ * The sigma arrays are the per-side PML profiles (length n_*l / n_*r, may be 0
+ * for a Dirichlet side).  Outputs must not alias inputs.
+ * ------------------------------------------------------------------------ */
+int pysit_cda_step_1d(int dtype, int order,
+                      const void* km1_u, const void* k_phiz, const void* k_u,
+                      const void* C, const void* rhs,
+                      const void* zlpml, int n_zlpml, const void* zrpml, int n_zrpml,
+                      double dt, double dz, int nz,
+                      void* kp1_phiz, void* kp1_u, void* stream);
+
+int pysit_cda_step_2d(int dtype, int order,
+                      const void* km1_u, const void* k_phix, const void* k_phiz,
+                      const void* k_u, const void* C, const void* rhs,
+                      const void* xlpml, int n_xlpml, const void* xrpml, int n_xrpml,
+                      const void* zlpml, int n_zlpml, const void* zrpml, int n_zrpml,
+                      double dt, double dx, double dz, int nx, int nz,
+                      void* kp1_phix, void* kp1_phiz, void* kp1_u, void* stream);
+
+int pysit_cda_step_3d(int dtype, int order,
+                      const void* km1_u, const void* k_phix, const void* k_phiy,
+                      const void* k_phiz, const void* k_psi, const void* k_u,
+                      const void* C, const void* rhs,
+                      const void* xlpml, int n_xlpml, const void* xrpml, int n_xrpml,
+                      const void* ylpml, int n_ylpml, const void* yrpml, int n_yrpml,
+                      const void* zlpml, int n_zlpml, const void* zrpml, int n_zrpml,
+                      double dt, double dx, double dy, double dz, int nx, int ny, int nz,
+                      void* kp1_phix, void* kp1_phiy, void* kp1_phiz, void* kp1_psi,
+                      void* kp1_u, void* stream);
+
+/* Imaging-condition operand of one step (the reference's dWaveOp,
+ * ConstantDensityAcousticBase._compute_dWaveOp_time,
+ * pysit/solvers/constant_density_acoustic/constant_density_acoustic_base.py:24-40):
+ *   out = (u_kp1 - 2 u_k + u_km1)/dt^2 + S1 (u_kp1 - u_km1)/(2 dt) + S2 u_k [+ S3 psi_k]
+ * with S1 = sum of the mesh sigma maps, S2 = sum of their pairwise products and
+ * S3 = their triple product (3D).  sig_x/sig_y/sig_z are the full-length
+ * per-axis sigma maps (length nx/ny/nz; pass NULL for an absent axis) of the
+ * mesh (StructuredPML.eval_on_mesh, pysit/core/mesh.py:784-831).  psi_k may be
+ * NULL in 1D/2D.  All arrays have nx*ny*nz entries. */
+int pysit_cda_dwaveop(int dtype, int dim, const void* km1_u, const void* k_u,
+                      const void* kp1_u, const void* psi_k,
+                      const void* sig_x, const void* sig_y, const void* sig_z,
+                      int nx, int ny, int nz, double dt, void* out, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Batched, checkpointed forward / gradient pipeline ("plan").
+ * Replaces the per-shot Python loops of TemporalModeling.forward_model
+ * (pysit/modeling/temporal_modeling.py:60-169), adjoint_model (:228-387),
+ * migrate_shot (:171-214) and TemporalLeastSquares._gradient_helper /
+ * compute_gradient / evaluate (pysit/objective_functions/
+ * temporal_least_squares.py:27-198) by one call per gradient for a whole
+ * batch of shots.  The library allocates no device memory: the caller asks
+ * for the workspace size and binds a buffer it owns.
+ * ------------------------------------------------------------------------ */
+typedef struct pysit_plan pysit_plan;
+
+typedef struct {
+    int dim;               /* 1, 2 or 3 */
+    int order;             /* spatial accuracy order 2, 4, 6, 8 */
+    int dtype;             /* PYSIT_F32 or PYSIT_F64 */
+    int n[3];              /* padded grid sizes (x, y, z); unused axes = 1, 1D uses n[2] */
+    double delta[3];       /* grid spacings (x, y, z) */
+    int pad_lo[3];         /* padding cells on the low / high side of each axis, used */
+    int pad_hi[3];         /*   to fold the PML strips of the gradient (add_padding)   */
+    double dt;             /* time step */
+    int nsteps;            /* number of time steps */
+    int imaging_period;    /* image every p-th step (TemporalLeastSquares.imaging_period) */
+    int checkpoint_every;  /* segment length S of the checkpoint / recompute schedule */
+    int shots_per_launch;  /* shots advanced together by one kernel launch (<= nshots) */
+    int nshots;            /* shots in the batch */
+    /* PML profiles in the step kernels' convention (host, FP64): per axis the left
+     * and right arrays that time_step passes to the reference kernel. */
+    const double* sig_l[3]; int nsig_l[3];
+    const double* sig_r[3]; int nsig_r[3];
+    /* Full-length per-axis sigma maps of the mesh (host, FP64, length n[a]), the
+     * convention of the imaging operand dWaveOp; NULL for an axis without PML. */
+    const double* sigmap[3];
+    /* Sources: per shot a list of taps (padded flat cell, source point, weight);
+     * rhs_k(cell) = sum_taps weight * src_amp[shot][k][point]. */
+    int nsrc;                      /* source points per shot */
+    const int64_t* src_tap_ptr;    /* host [nshots+1] offsets into the tap arrays */
+    const int64_t* src_tap_cell;   /* host */
+    const int32_t* src_tap_point;  /* host */
+    const double* src_tap_w;       /* host */
+    const double* src_amp;         /* host [nshots][nsteps][nsrc] */
+    /* Receivers: per shot a list of taps (padded flat cell, receiver, sampling
+     * weight, injection weight).  trace[k][r] = sum w_sample * u_k(cell);
+     * adjoint rhs_k(cell) = sum w_inject * resid[k][r]. */
+    int nrec;                      /* receivers per shot */
+    const int64_t* rec_tap_ptr;    /* host [nshots+1] */
+    const int64_t* rec_tap_cell;   /* host */
+    const int32_t* rec_tap_point;  /* host */
+    const double* rec_tap_wsample; /* host */
+    const double* rec_tap_winject; /* host */
+    int use_graph;                 /* capture the time loops in CUDA graphs (1) or launch eagerly (0) */
+} pysit_plan_desc;
+
+int pysit_plan_create(const pysit_plan_desc* desc, pysit_plan** out);
+int pysit_plan_destroy(pysit_plan* plan);
+/* Device workspace the plan needs, in bytes (256-byte aligned buffer). */
+int pysit_plan_workspace_bytes(const pysit_plan* plan, uint64_t* bytes);
+/* Binds (and initialises) the caller-owned workspace; uploads acquisition data. */
+int pysit_plan_bind_workspace(pysit_plan* plan, void* workspace_dev, uint64_t bytes,
+                              void* stream);
+/* Sets the padded wave speed C (dev, FP64, n[0]*n[1]*n[2] cells, z fastest). */
+int pysit_plan_set_model(pysit_plan* plan, const double* C_padded_dev, void* stream);
+/* Forward modelling of every shot: traces_dev (plan dtype) receives
+ * [nshots][nsteps][nrec] samples u_k at the receivers, k = 0..nsteps-1
+ * (TemporalModeling.forward_model 'simdata', temporal_modeling.py:123-125). */
+int pysit_plan_forward(pysit_plan* plan, void* traces_dev, void* stream);
+/* Misfit and gradient of the batch.  dobs_dev (plan dtype, [nshots][nsteps][nrec])
+ * holds the observed data already resampled to this plan's time axis
+ * (ReceiverSet.interpolate_data).  Outputs (dev, FP64):
+ *   grad_dev    [prod(n - pad_lo - pad_hi)] unpadded gradient with respect to
+ *               m = C^-2, PML strips folded onto the boundary (= the reference's
+ *               compute_gradient result);
+ *   rnorm2_dev  [1] sum over shots of ||dobs - dsim||^2 (objective = 0.5*dt*rnorm2);
+ *   traces_dev  optional (may be NULL) simulated traces as in pysit_plan_forward. */
+int pysit_plan_gradient(pysit_plan* plan, const void* dobs_dev, double* grad_dev,
+                        double* rnorm2_dev, void* traces_dev, void* stream);
+/* Migration F* of a data-space operand (TemporalModeling.migrate_shot,
+ * temporal_modeling.py:171-214, for every shot of the batch, summed):
+ * operand_dev (plan dtype, [nshots][nsteps][nrec]) drives the adjoint directly;
+ * image_dev (FP64, unpadded) = sum over shots of -dt*p*sum_k q_k*dWaveOp_k with
+ * the strips folded; norm2_dev [1] = ||operand||^2. */
+int pysit_plan_migrate(pysit_plan* plan, const void* operand_dev, double* image_dev,
+                       double* norm2_dev, void* stream);
+/* Misfit only (TemporalLeastSquares.evaluate without the 0.5*dt factor). */
+int pysit_plan_misfit(pysit_plan* plan, const void* dobs_dev, double* rnorm2_dev,
+                      void* traces_dev, void* stream);
+/* Number of kernel launches the last forward/gradient/misfit call issued. */
+int pysit_plan_last_launch_count(const pysit_plan* plan, int64_t* launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PYSIT_GB300_H */

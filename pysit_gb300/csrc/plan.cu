@@ -1,0 +1,893 @@
+// Batched forward / gradient pipeline ("plan") behind pysit_plan_* of the C ABI.
+//
+// Schedule of one gradient for a group of shots (all shots of a group advance
+// together in every launch):
+//   forward sweep   k = 0..n-1: record traces of u_k, step to u_{k+1}; every S
+//                   steps save the step inputs (u_{k-1}, u_k, PML state) as a
+//                   checkpoint            (TemporalModeling.forward_model,
+//                   pysit/modeling/temporal_modeling.py:115-161, without the
+//                   per-step dWaveOp list of :146-148)
+//   residual        r = dobs - dsim and ||r||^2 in FP64
+//                   (TemporalLeastSquares._residual / evaluate,
+//                   pysit/objective_functions/temporal_least_squares.py:27-82)
+//   backward sweep  segments from last to first: restore the checkpoint,
+//                   recompute the segment writing dWaveOp_k into a replay
+//                   buffer, then run the adjoint steps k = k1..k0 with
+//                   ic += q_k * dWaveOp_k  (adjoint_model, :312-365)
+//   reduction       grad += dt * p * sum_shots ic_shot (FP64)   (:367-369 and
+//                   compute_gradient's grad -= g, temporal_least_squares.py:167)
+//   fold            PML strips summed onto the boundary rows/columns
+//                   (ModelPerturbationBase.add_padding,
+//                   pysit/solvers/model_parameter.py:537-594).
+// The whole schedule of a call is captured once in a CUDA graph and replayed.
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <vector>
+
+#include "wave.cuh"
+
+namespace pgb {
+namespace {
+
+// ---------------------------------------------------------------------------
+// small kernels
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ long long ioff(int i, int j, int k, int hx, int hy, int rows_y,
+                                          int ldz) {
+    return ((long long)(i + hx) * rows_y + (j + hy)) * ldz + kOZ + k;
+}
+
+template <typename T>
+__global__ void set_c2_kernel(const double* __restrict__ C, int nx, int ny, int nz, int hx,
+                              int hy, int rows_y, int ldz, T* __restrict__ c2) {
+    long long n = (long long)nx * ny * nz;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
+         c += (long long)gridDim.x * blockDim.x) {
+        int k = (int)(c % nz);
+        long long r = c / nz;
+        int j = (int)(r % ny), i = (int)(r / ny);
+        T v = T(C[c]);
+        c2[ioff(i, j, k, hx, hy, rows_y, ldz)] = v * v;
+    }
+}
+
+constexpr int kRedBlocks = 1024;
+constexpr int kRedThreads = 256;
+
+// resid = dobs - dsim (in place over the trace buffer); per-block FP64 partial
+// sums of resid^2 in a fixed order (deterministic).
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads) residual_kernel(const T* __restrict__ dobs,
+                                                               T* __restrict__ tr, long long n,
+                                                               double* __restrict__ partial,
+                                                               int operand) {
+    double acc = 0.0;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
+         c += (long long)gridDim.x * blockDim.x) {
+        T r = operand ? dobs[c] : dobs[c] - tr[c];
+        tr[c] = r;
+        acc += (double)r * (double)r;
+    }
+    __shared__ double s[kRedThreads];
+    s[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = kRedThreads / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) s[threadIdx.x] += s[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = s[0];
+}
+
+// out[0] (+)= sum of partial[0..n) in a fixed order, one block.
+__global__ void __launch_bounds__(kRedThreads) sum_partials_kernel(const double* __restrict__ partial,
+                                                                   int n, double* __restrict__ out,
+                                                                   int accumulate) {
+    __shared__ double s[kRedThreads];
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) acc += partial[i];
+    s[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = kRedThreads / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) s[threadIdx.x] += s[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[0] = (accumulate ? out[0] : 0.0) + s[0];
+}
+
+// grad_pad[c] += scale * sum_s ic[s](c) in FP64, shots summed in order.
+template <typename T>
+__global__ void reduce_ic_kernel(const T* __restrict__ ic, long long fstride, int nshot, int nx,
+                                 int ny, int nz, int hx, int hy, int rows_y, int ldz, double scale,
+                                 double* __restrict__ gpad) {
+    long long n = (long long)nx * ny * nz;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
+         c += (long long)gridDim.x * blockDim.x) {
+        int k = (int)(c % nz);
+        long long r = c / nz;
+        int j = (int)(r % ny), i = (int)(r / ny);
+        long long o = ioff(i, j, k, hx, hy, rows_y, ldz);
+        double acc = 0.0;
+        for (int s = 0; s < nshot; ++s) acc += (double)ic[s * fstride + o];
+        gpad[c] += scale * acc;
+    }
+}
+
+// Unpadded gradient: each physical cell collects the padded cells that
+// add_padding folds onto it (strips beyond a boundary row/column fold onto it).
+__global__ void fold_kernel(const double* __restrict__ gpad, int nx, int ny, int nz, int lx,
+                            int hxp, int ly, int hyp, int lz, int hzp, double* __restrict__ out) {
+    const int px = nx - lx - hxp, py = ny - ly - hyp, pz = nz - lz - hzp;
+    long long n = (long long)px * py * pz;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
+         c += (long long)gridDim.x * blockDim.x) {
+        int k = (int)(c % pz);
+        long long r = c / pz;
+        int j = (int)(r % py), i = (int)(r / py);
+        int i0 = lx + i, i1 = lx + i, j0 = ly + j, j1 = ly + j, k0 = lz + k, k1 = lz + k;
+        if (i == 0) i0 = 0;
+        if (i == px - 1) i1 = nx - 1;
+        if (j == 0) j0 = 0;
+        if (j == py - 1) j1 = ny - 1;
+        if (k == 0) k0 = 0;
+        if (k == pz - 1) k1 = nz - 1;
+        double acc = 0.0;
+        for (int a = i0; a <= i1; ++a)
+            for (int b = j0; b <= j1; ++b)
+                for (int d = k0; d <= k1; ++d) acc += gpad[((long long)a * ny + b) * nz + d];
+        out[c] = acc;
+    }
+}
+
+int grid_for(long long n, int threads) {
+    long long b = (n + threads - 1) / threads;
+    return (int)std::max<long long>(1, std::min<long long>(b, 152LL * 16));
+}
+
+// ---------------------------------------------------------------------------
+// host-side plan
+// ---------------------------------------------------------------------------
+struct CSRBox {  // injection operator of one shot: box + CSR over box cells
+    int box[6];
+    std::vector<int> rowptr;  // relative entry indices
+    std::vector<int> pt;
+    std::vector<double> w;
+};
+
+}  // namespace
+}  // namespace pgb
+
+struct pysit_plan {
+    virtual ~pysit_plan() = default;
+    virtual int workspace_bytes(uint64_t* b) const = 0;
+    virtual int bind(void* ws, uint64_t bytes, cudaStream_t s) = 0;
+    virtual int set_model(const double* C, cudaStream_t s) = 0;
+    virtual int forward(void* traces, cudaStream_t s) = 0;
+    virtual int gradient(const void* dobs, double* grad, double* rnorm2, void* traces,
+                         cudaStream_t s, bool with_grad, bool migrate) = 0;
+    int64_t last_launches = 0;
+};
+
+namespace pgb {
+namespace {
+
+template <typename T>
+struct PlanT final : public pysit_plan {
+    // ---- description -------------------------------------------------------
+    int dim, order, R, nx, ny, nz, nsteps, p_img, S, G, nshots, nsrc, nrec, use_graph;
+    double dx, dy, dz, dt;
+    int pad_lo[3], pad_hi[3];
+    int pl[3], pr[3];  // PML-state widths (kernel profile lengths)
+    std::vector<double> sg[3], mg[3];
+    // ---- layout --------------------------------------------------------------
+    int hx, hy, rows_y, ldz;
+    long long fstride;  // elements per field per shot (256-byte multiple)
+    int bz, tx, ntz, ntx;
+    int nseg;
+    // ---- acquisition (host) ----------------------------------------------------
+    std::vector<CSRBox> src_inj, rec_inj;
+    std::vector<int> rec_rows;        // [nshots*nrec+1]
+    std::vector<long long> rec_off;   // internal offsets
+    std::vector<double> rec_ws;       // sampling weights
+    std::vector<double> src_amp;      // [nshots][nsteps][nsrc]
+    // ---- workspace -------------------------------------------------------------
+    char* ws = nullptr;
+    uint64_t ws_need = 0;
+    struct Off {
+        size_t c2, sgx, sgy, sgz, mgx, mgy, mgz;
+        size_t U[2], PX[2], PY[2], PZ[2], PS[2];   // forward state
+        size_t A[2], AX[2], AY[2], AZ[2], AS[2];   // adjoint state
+        size_t ic, replay, ckpt, traces, srcamp;
+        size_t sbox, srpb, srow, spt, sw;          // source injection
+        size_t rbox, rrpb, rrow, rpt, rw;          // receiver injection
+        size_t recrow, recoff, recw;               // recording
+        size_t gpad, partial, rnorm;
+    } off{};
+    size_t field_bytes = 0;      // one field for G shots
+    int ckpt_fields = 0;         // fields per checkpoint
+    bool model_set = false;
+    // ---- graphs ----------------------------------------------------------------
+    cudaStream_t cap = nullptr;
+    struct GraphKey {
+        int kind;
+        const void *a, *b, *c, *d;
+        bool operator<(const GraphKey& o) const {
+            if (kind != o.kind) return kind < o.kind;
+            if (a != o.a) return a < o.a;
+            if (b != o.b) return b < o.b;
+            if (c != o.c) return c < o.c;
+            return d < o.d;
+        }
+    };
+    struct GraphRec {
+        cudaGraphExec_t exec = nullptr;
+        int64_t launches = 0;
+    };
+    std::map<GraphKey, GraphRec> graphs;
+    int64_t launches = 0;
+
+    ~PlanT() override {
+        for (auto& kv : graphs)
+            if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+        if (cap) cudaStreamDestroy(cap);
+    }
+
+    template <typename U>
+    U* at(size_t o) const { return reinterpret_cast<U*>(ws + o); }
+    T* fld(size_t o, int shot = 0) const { return at<T>(o) + (long long)shot * fstride; }
+
+    // ---- creation --------------------------------------------------------------
+    int init(const pysit_plan_desc& d) {
+        dim = d.dim; order = d.order; R = order / 2;
+        nx = d.n[0]; ny = d.n[1]; nz = d.n[2];
+        if (dim == 1) { nx = 1; ny = 1; }
+        if (dim == 2) ny = 1;
+        dx = d.delta[0]; dy = d.delta[1]; dz = d.delta[2];
+        dt = d.dt; nsteps = d.nsteps; p_img = d.imaging_period; S = d.checkpoint_every;
+        nshots = d.nshots; G = std::min(d.shots_per_launch, d.nshots); nsrc = d.nsrc; nrec = d.nrec;
+        use_graph = d.use_graph;
+        for (int a = 0; a < 3; ++a) { pad_lo[a] = d.pad_lo[a]; pad_hi[a] = d.pad_hi[a]; }
+        const int na[3] = {nx, ny, nz};
+        for (int a = 0; a < 3; ++a) {
+            pl[a] = d.sig_l[a] ? d.nsig_l[a] : 0;
+            pr[a] = d.sig_r[a] ? d.nsig_r[a] : 0;
+            PGB_REQUIRE(pl[a] >= 0 && pr[a] >= 0 && pl[a] <= na[a] && pr[a] <= na[a],
+                        "bad PML profile length on axis %d", a);
+            sg[a].assign(na[a], 0.0);
+            mg[a].assign(na[a], 0.0);
+            for (int i = 0; i < na[a]; ++i) {
+                // profile lookup of the step kernels (_2D.h:137-157)
+                if (pl[a] > 0 && i < pl[a]) sg[a][i] = d.sig_l[a][i];
+                else if (pr[a] > 0 && i >= na[a] - pr[a] && i <= na[a] - 2)
+                    sg[a][i] = d.sig_r[a][pr[a] - ((na[a] - 1) - i)];
+                if (d.sigmap[a]) mg[a][i] = d.sigmap[a][i];
+            }
+        }
+        // layout
+        hx = dim >= 2 ? kHalo : 0;
+        hy = dim == 3 ? kHalo : 0;
+        rows_y = ny + 2 * hy;
+        ldz = ((kOZ + nz + kHalo) + 31) / 32 * 32;
+        fstride = (long long)(nx + 2 * hx) * rows_y * ldz;
+        fstride = (fstride + 63) / 64 * 64;
+        field_bytes = (size_t)fstride * G * sizeof(T);
+        nseg = (nsteps + S - 1) / S;
+        ckpt_fields = dim == 1 ? 3 : dim == 2 ? 4 : 6;
+        choose_tiling();
+        // acquisition
+        int rc = build_injection(d.src_tap_ptr, d.src_tap_cell, d.src_tap_point, d.src_tap_w, nsrc,
+                                 src_inj, "source");
+        if (rc) return rc;
+        rc = build_injection(d.rec_tap_ptr, d.rec_tap_cell, d.rec_tap_point, d.rec_tap_winject, nrec,
+                             rec_inj, "receiver");
+        if (rc) return rc;
+        rc = build_recording(d);
+        if (rc) return rc;
+        src_amp.assign(d.src_amp, d.src_amp + (size_t)nshots * nsteps * nsrc);
+        carve();
+        return PYSIT_OK;
+    }
+
+    void choose_tiling() {
+        constexpr int V = V16<T>::N;
+        const char* e = getenv("PYSIT_CUDA_TILE");  // "bz,tx" override (tuning)
+        int ebz = 0, etx = 0;
+        if (e && sscanf(e, "%d,%d", &ebz, &etx) == 2 && ebz >= 32 && ebz <= 256 && ebz % 32 == 0 &&
+            etx >= 1) {
+            bz = ebz; tx = etx;
+        } else {
+            // fewest loaded elements (tile + halo) per useful cell, bz >= 64
+            double best = 1e30;
+            for (int b : {64, 128, 256}) {
+                int tiles = (nz + b * V - 1) / (b * V);
+                double cost = (double)tiles * (b * V + 2 * kHalo) / nz;
+                if (cost < best - 1e-9) { best = cost; bz = b; }
+            }
+            tx = 32;
+        }
+        ntz = (nz + bz * V - 1) / (bz * V);
+        ntx = (nx + tx - 1) / tx;
+    }
+
+    long long internal_offset(long long cell) const {
+        int k = (int)(cell % nz);
+        long long r = cell / nz;
+        int j = (int)(r % ny), i = (int)(r / ny);
+        return ((long long)(i + hx) * rows_y + (j + hy)) * ldz + kOZ + k;
+    }
+
+    int build_injection(const int64_t* ptr, const int64_t* cell, const int32_t* pt, const double* w,
+                        int npts, std::vector<CSRBox>& out, const char* what) {
+        out.assign(nshots, CSRBox{});
+        const long long ncell = (long long)nx * ny * nz;
+        for (int s = 0; s < nshots; ++s) {
+            CSRBox& b = out[s];
+            long long e0 = ptr ? ptr[s] : 0, e1 = ptr ? ptr[s + 1] : 0;
+            PGB_REQUIRE(e1 >= e0, "%s tap pointers must be non-decreasing", what);
+            int lo[3] = {nx, ny, nz}, hi[3] = {0, 0, 0};
+            for (long long e = e0; e < e1; ++e) {
+                PGB_REQUIRE(cell[e] >= 0 && cell[e] < ncell, "%s tap cell %lld out of the grid", what,
+                            (long long)cell[e]);
+                PGB_REQUIRE(pt[e] >= 0 && pt[e] < npts, "%s tap point %d out of range", what, pt[e]);
+                int k = (int)(cell[e] % nz);
+                long long r = cell[e] / nz;
+                int j = (int)(r % ny), i = (int)(r / ny);
+                lo[0] = std::min(lo[0], i); hi[0] = std::max(hi[0], i + 1);
+                lo[1] = std::min(lo[1], j); hi[1] = std::max(hi[1], j + 1);
+                lo[2] = std::min(lo[2], k); hi[2] = std::max(hi[2], k + 1);
+            }
+            if (e1 == e0) { for (int a = 0; a < 3; ++a) { lo[a] = 0; hi[a] = 0; } }
+            b.box[0] = lo[0]; b.box[1] = hi[0]; b.box[2] = lo[1]; b.box[3] = hi[1];
+            b.box[4] = lo[2]; b.box[5] = hi[2];
+            long long bw = (long long)(hi[0] - lo[0]) * (hi[1] - lo[1]) * (hi[2] - lo[2]);
+            if (bw < 0) bw = 0;
+            PGB_REQUIRE(bw < (1LL << 30), "%s footprint too large", what);
+            std::vector<int> cnt(bw + 1, 0);
+            auto boxcell = [&](long long c) {
+                int k = (int)(c % nz);
+                long long r = c / nz;
+                int j = (int)(r % ny), i = (int)(r / ny);
+                return ((long long)(i - lo[0]) * (hi[1] - lo[1]) + (j - lo[1])) * (hi[2] - lo[2]) +
+                       (k - lo[2]);
+            };
+            for (long long e = e0; e < e1; ++e) cnt[boxcell(cell[e]) + 1]++;
+            b.rowptr.assign(bw + 1, 0);
+            for (long long c = 0; c < bw; ++c) b.rowptr[c + 1] = b.rowptr[c] + cnt[c + 1];
+            b.pt.assign(e1 - e0, 0);
+            b.w.assign(e1 - e0, 0.0);
+            std::vector<int> fill(b.rowptr.begin(), b.rowptr.begin() + bw);
+            for (long long e = e0; e < e1; ++e) {  // stable: taps keep their order per cell
+                long long c = boxcell(cell[e]);
+                int pos = fill[c]++;
+                b.pt[pos] = pt[e];
+                b.w[pos] = w[e];
+            }
+        }
+        return PYSIT_OK;
+    }
+
+    int build_recording(const pysit_plan_desc& d) {
+        const long long ncell = (long long)nx * ny * nz;
+        rec_rows.assign((size_t)nshots * nrec + 1, 0);
+        std::vector<long long> cnt((size_t)nshots * nrec + 1, 0);
+        long long total = d.rec_tap_ptr ? d.rec_tap_ptr[nshots] - d.rec_tap_ptr[0] : 0;
+        PGB_REQUIRE(total < (1LL << 31), "too many receiver taps");
+        for (int s = 0; s < nshots && d.rec_tap_ptr; ++s)
+            for (long long e = d.rec_tap_ptr[s]; e < d.rec_tap_ptr[s + 1]; ++e) {
+                PGB_REQUIRE(d.rec_tap_point[e] >= 0 && d.rec_tap_point[e] < nrec, "receiver index out of range");
+                PGB_REQUIRE(d.rec_tap_cell[e] >= 0 && d.rec_tap_cell[e] < ncell, "receiver tap out of grid");
+                cnt[(size_t)s * nrec + d.rec_tap_point[e] + 1]++;
+            }
+        for (size_t r = 0; r < (size_t)nshots * nrec; ++r) rec_rows[r + 1] = (int)(rec_rows[r] + cnt[r + 1]);
+        rec_off.assign(total, 0);
+        rec_ws.assign(total, 0.0);
+        std::vector<int> fill(rec_rows.begin(), rec_rows.end() - 1);
+        for (int s = 0; s < nshots && d.rec_tap_ptr; ++s)
+            for (long long e = d.rec_tap_ptr[s]; e < d.rec_tap_ptr[s + 1]; ++e) {
+                int pos = fill[(size_t)s * nrec + d.rec_tap_point[e]]++;
+                rec_off[pos] = internal_offset(d.rec_tap_cell[e]);
+                rec_ws[pos] = d.rec_tap_wsample[e];
+            }
+        return PYSIT_OK;
+    }
+
+    void carve() {
+        size_t tot = 0;
+        auto take = [&](size_t bytes) { size_t o = tot; tot += (bytes + 255) / 256 * 256; return o; };
+        const size_t one = (size_t)fstride * sizeof(T);  // one field, one shot
+        off.c2 = take(one);
+        off.sgx = take(nx * sizeof(T)); off.sgy = take(ny * sizeof(T)); off.sgz = take(nz * sizeof(T));
+        off.mgx = take(nx * sizeof(T)); off.mgy = take(ny * sizeof(T)); off.mgz = take(nz * sizeof(T));
+        for (int b = 0; b < 2; ++b) {
+            off.U[b] = take(field_bytes); off.A[b] = take(field_bytes);
+            off.PZ[b] = take(field_bytes); off.AZ[b] = take(field_bytes);
+            off.PX[b] = dim >= 2 ? take(field_bytes) : off.PZ[b];
+            off.AX[b] = dim >= 2 ? take(field_bytes) : off.AZ[b];
+            off.PY[b] = dim == 3 ? take(field_bytes) : off.PZ[b];
+            off.AY[b] = dim == 3 ? take(field_bytes) : off.AZ[b];
+            off.PS[b] = dim == 3 ? take(field_bytes) : off.PZ[b];
+            off.AS[b] = dim == 3 ? take(field_bytes) : off.AZ[b];
+        }
+        off.ic = take(field_bytes);
+        off.replay = take(field_bytes * (size_t)S);
+        off.ckpt = take(field_bytes * (size_t)ckpt_fields * nseg);
+        off.traces = take((size_t)G * nsteps * nrec * sizeof(T));
+        off.srcamp = take((size_t)nshots * nsteps * nsrc * sizeof(T));
+        auto take_inj = [&](std::vector<CSRBox>& v, size_t& box, size_t& rpb, size_t& row, size_t& pt,
+                            size_t& w) {
+            size_t nrow = 0, nent = 0;
+            for (auto& b : v) { nrow += b.rowptr.size(); nent += b.pt.size(); }
+            box = take(v.size() * 6 * sizeof(int));
+            rpb = take(v.size() * sizeof(long long));
+            row = take(std::max<size_t>(nrow, 1) * sizeof(int));
+            pt = take(std::max<size_t>(nent, 1) * sizeof(int));
+            w = take(std::max<size_t>(nent, 1) * sizeof(T));
+        };
+        take_inj(src_inj, off.sbox, off.srpb, off.srow, off.spt, off.sw);
+        take_inj(rec_inj, off.rbox, off.rrpb, off.rrow, off.rpt, off.rw);
+        off.recrow = take(rec_rows.size() * sizeof(int));
+        off.recoff = take(std::max<size_t>(rec_off.size(), 1) * sizeof(long long));
+        off.recw = take(std::max<size_t>(rec_ws.size(), 1) * sizeof(T));
+        off.gpad = take((size_t)nx * ny * nz * sizeof(double));
+        off.partial = take(kRedBlocks * sizeof(double));
+        off.rnorm = take(sizeof(double));
+        ws_need = tot;
+    }
+
+    int workspace_bytes(uint64_t* b) const override { *b = ws_need; return PYSIT_OK; }
+
+    template <typename U>
+    int upload(size_t o, const std::vector<U>& v, cudaStream_t s) {
+        if (v.empty()) return PYSIT_OK;
+        PGB_CHECK_CUDA(cudaMemcpyAsync(ws + o, v.data(), v.size() * sizeof(U), cudaMemcpyHostToDevice, s));
+        return PYSIT_OK;
+    }
+    std::vector<T> toT(const std::vector<double>& v) { return std::vector<T>(v.begin(), v.end()); }
+
+    int upload_inj(std::vector<CSRBox>& v, size_t box, size_t rpb, size_t row, size_t pt, size_t w,
+                   cudaStream_t s) {
+        std::vector<int> boxes, rows, pts;
+        std::vector<long long> bases;
+        std::vector<double> ws_;
+        for (auto& b : v) {
+            boxes.insert(boxes.end(), b.box, b.box + 6);
+            bases.push_back((long long)rows.size());
+            int base = (int)pts.size();
+            for (int r : b.rowptr) rows.push_back(r + base);
+            pts.insert(pts.end(), b.pt.begin(), b.pt.end());
+            ws_.insert(ws_.end(), b.w.begin(), b.w.end());
+        }
+        int rc;
+        if ((rc = upload(box, boxes, s)) || (rc = upload(rpb, bases, s)) || (rc = upload(row, rows, s)) ||
+            (rc = upload(pt, pts, s)))
+            return rc;
+        std::vector<T> wt = toT(ws_);
+        rc = upload(w, wt, s);
+        if (rc) return rc;
+        return cudaStreamSynchronize(s) == cudaSuccess ? PYSIT_OK : cuda_status(cudaGetLastError(), "upload");
+    }
+
+    int bind(void* w, uint64_t bytes, cudaStream_t s) override {
+        PGB_REQUIRE(w != nullptr, "NULL workspace");
+        PGB_REQUIRE(aligned(w, 256), "workspace must be 256-byte aligned");
+        PGB_REQUIRE(bytes >= ws_need, "workspace too small: %llu < %llu bytes",
+                    (unsigned long long)bytes, (unsigned long long)ws_need);
+        for (auto& kv : graphs)
+            if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+        graphs.clear();
+        ws = static_cast<char*>(w);
+        PGB_CHECK_CUDA(cudaMemsetAsync(ws, 0, ws_need, s));
+        int rc;
+        std::vector<T> tmp;
+        if ((rc = upload(off.sgx, tmp = toT(sg[0]), s)) || (rc = upload(off.sgy, tmp = toT(sg[1]), s)) ||
+            (rc = upload(off.sgz, tmp = toT(sg[2]), s)) || (rc = upload(off.mgx, tmp = toT(mg[0]), s)) ||
+            (rc = upload(off.mgy, tmp = toT(mg[1]), s)) || (rc = upload(off.mgz, tmp = toT(mg[2]), s)))
+            return rc;
+        PGB_CHECK_CUDA(cudaStreamSynchronize(s));
+        if ((rc = upload(off.srcamp, tmp = toT(src_amp), s))) return rc;
+        PGB_CHECK_CUDA(cudaStreamSynchronize(s));
+        if ((rc = upload_inj(src_inj, off.sbox, off.srpb, off.srow, off.spt, off.sw, s))) return rc;
+        if ((rc = upload_inj(rec_inj, off.rbox, off.rrpb, off.rrow, off.rpt, off.rw, s))) return rc;
+        if ((rc = upload(off.recrow, rec_rows, s)) || (rc = upload(off.recoff, rec_off, s))) return rc;
+        if ((rc = upload(off.recw, tmp = toT(rec_ws), s))) return rc;
+        PGB_CHECK_CUDA(cudaStreamSynchronize(s));
+        if (!cap) PGB_CHECK_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+        model_set = false;
+        return PYSIT_OK;
+    }
+
+    int set_model(const double* C, cudaStream_t s) override {
+        PGB_REQUIRE(ws, "no workspace bound");
+        PGB_REQUIRE(C, "NULL model");
+        long long n = (long long)nx * ny * nz;
+        set_c2_kernel<T><<<grid_for(n, 256), 256, 0, s>>>(C, nx, ny, nz, hx, hy, rows_y, ldz, at<T>(off.c2));
+        PGB_CHECK_CUDA(cudaGetLastError());
+        model_set = true;
+        return PYSIT_OK;
+    }
+
+    // ---- step launch -------------------------------------------------------------
+    struct State {  // role-tracking pointers of one wavefield state (ping-pong)
+        T *prev, *cur, *phx[2], *phy[2], *phz[2], *psi[2];
+        int pb = 0;  // which PML buffer is the input
+    };
+
+    WaveParams<T> base_params(int g0, int gn) const {
+        WaveParams<T> p{};
+        p.nx = nx; p.ny = ny; p.nz = nz; p.ldz = ldz; p.rows_y = rows_y; p.fstride = fstride;
+        p.hx = hx; p.hy = hy; p.tx = tx; p.ty = 1; p.ntz = ntz; p.nty = 1; p.ntx = ntx; p.nshot = gn;
+        p.c2 = at<T>(off.c2);
+        p.sgx = at<T>(off.sgx); p.sgy = at<T>(off.sgy); p.sgz = at<T>(off.sgz);
+        p.mgx = at<T>(off.mgx); p.mgy = at<T>(off.mgy); p.mgz = at<T>(off.mgz);
+        p.pxl = pl[0]; p.pxr = pr[0]; p.pyl = pl[1]; p.pyr = pr[1]; p.pzl = pl[2]; p.pzr = pr[2];
+        p.dt = T(dt); p.dt2 = T(dt * dt); p.idt2 = T(1.0 / (dt * dt)); p.i2dt = T(1.0 / (2.0 * dt));
+        p.idx = T(1.0 / dx); p.idx2 = T(1.0 / (T(dx) * T(dx)));
+        p.idy = T(1.0 / dy); p.idy2 = T(1.0 / (T(dy) * T(dy)));
+        p.idz = T(1.0 / dz); p.idz2 = T(1.0 / (T(dz) * T(dz)));
+        (void)g0;
+        return p;
+    }
+
+    void set_inject(WaveParams<T>& p, bool src, int g0, int k, const T* resid) const {
+        Inject<T>& j = p.inj;
+        if (src) {
+            j.box = at<int>(off.sbox) + g0 * 6;
+            j.rpbase = at<long long>(off.srpb) + g0;
+            j.rowptr = at<int>(off.srow);
+            j.pt = at<int>(off.spt);
+            j.w = at<T>(off.sw);
+            j.amp_sstride = (long long)nsteps * nsrc;
+            j.amp = at<T>(off.srcamp) + (long long)g0 * j.amp_sstride + (long long)k * nsrc;
+            j.on = nsrc > 0;
+        } else {
+            j.box = at<int>(off.rbox) + g0 * 6;
+            j.rpbase = at<long long>(off.rrpb) + g0;
+            j.rowptr = at<int>(off.rrow);
+            j.pt = at<int>(off.rpt);
+            j.w = at<T>(off.rw);
+            j.amp_sstride = (long long)nsteps * nrec;
+            j.amp = resid + (long long)k * nrec;
+            j.on = nrec > 0;
+        }
+    }
+
+    void launch(const WaveParams<T>& p, int mode, cudaStream_t s) {
+        ++launches;
+#define PGB_L(RR)                                                              \
+    do {                                                                       \
+        if (dim == 2) {                                                        \
+            if (mode == kFwd) launch_wave2d<T, RR, kFwd>(p, bz, s);            \
+            else if (mode == kRecomp) launch_wave2d<T, RR, kRecomp>(p, bz, s); \
+            else launch_wave2d<T, RR, kAdj>(p, bz, s);                         \
+        } else if (dim == 3) {                                                 \
+            if (mode == kFwd) launch_wave3d<T, RR, kFwd>(p, bz, s);            \
+            else if (mode == kRecomp) launch_wave3d<T, RR, kRecomp>(p, bz, s); \
+            else launch_wave3d<T, RR, kAdj>(p, bz, s);                         \
+        } else {                                                               \
+            if (mode == kFwd) launch_wave1d<T, RR, kFwd>(p, bz, s);            \
+            else if (mode == kRecomp) launch_wave1d<T, RR, kRecomp>(p, bz, s); \
+            else launch_wave1d<T, RR, kAdj>(p, bz, s);                         \
+        }                                                                      \
+    } while (0)
+        switch (R) {
+            case 1: PGB_L(1); break;
+            case 2: PGB_L(2); break;
+            case 3: PGB_L(3); break;
+            default: PGB_L(4); break;
+        }
+#undef PGB_L
+    }
+
+    // fill the state pointers of a sweep from buffer sets
+    State make_state(const size_t* U, const size_t* PX, const size_t* PY, const size_t* PZ,
+                     const size_t* PS) const {
+        State st{};
+        st.prev = at<T>(U[0]); st.cur = at<T>(U[1]);
+        for (int b = 0; b < 2; ++b) {
+            st.phx[b] = at<T>(PX[b]); st.phy[b] = at<T>(PY[b]);
+            st.phz[b] = at<T>(PZ[b]); st.psi[b] = at<T>(PS[b]);
+        }
+        st.pb = 0;
+        return st;
+    }
+
+    void bind_state(WaveParams<T>& p, const State& st) const {
+        p.u_prev = st.prev; p.u_cur = st.cur;
+        p.phx_in = st.phx[st.pb]; p.phx_out = st.phx[st.pb ^ 1];
+        p.phy_in = st.phy[st.pb]; p.phy_out = st.phy[st.pb ^ 1];
+        p.phz_in = st.phz[st.pb]; p.phz_out = st.phz[st.pb ^ 1];
+        p.psi_in = st.psi[st.pb]; p.psi_out = st.psi[st.pb ^ 1];
+    }
+    static void advance(State& st) { std::swap(st.prev, st.cur); st.pb ^= 1; }
+
+    void zero_state(const size_t* U, const size_t* PX, const size_t* PY, const size_t* PZ,
+                    const size_t* PS, cudaStream_t s) const {
+        for (int b = 0; b < 2; ++b) {
+            cudaMemsetAsync(ws + U[b], 0, field_bytes, s);
+            cudaMemsetAsync(ws + PZ[b], 0, field_bytes, s);
+            if (dim >= 2) cudaMemsetAsync(ws + PX[b], 0, field_bytes, s);
+            if (dim == 3) {
+                cudaMemsetAsync(ws + PY[b], 0, field_bytes, s);
+                cudaMemsetAsync(ws + PS[b], 0, field_bytes, s);
+            }
+        }
+    }
+
+    // the arrays a checkpoint holds: prev, cur and the input PML state
+    void ckpt_ptrs(const State& st, T** v) const {
+        int n = 0;
+        v[n++] = st.prev; v[n++] = st.cur; v[n++] = st.phz[st.pb];
+        if (dim >= 2) v[n++] = st.phx[st.pb];
+        if (dim == 3) { v[n++] = st.phy[st.pb]; v[n++] = st.psi[st.pb]; }
+    }
+
+    void copy_fields(T* const* dst, T* const* src, cudaStream_t s) const {
+        for (int f = 0; f < ckpt_fields; ++f)
+            if (dst[f] && src[f]) cudaMemcpyAsync(dst[f], src[f], field_bytes, cudaMemcpyDeviceToDevice, s);
+    }
+
+    T* ckpt_slot(int seg, int f) const {
+        return reinterpret_cast<T*>(ws + off.ckpt + ((size_t)seg * ckpt_fields + f) * field_bytes);
+    }
+
+    // forward sweep of one group; optional checkpoints
+    void forward_sweep(int g0, int gn, bool checkpoints, cudaStream_t s) {
+        zero_state(off.U, off.PX, off.PY, off.PZ, off.PS, s);
+        State st = make_state(off.U, off.PX, off.PY, off.PZ, off.PS);
+        WaveParams<T> p = base_params(g0, gn);
+        T* tr = at<T>(off.traces);
+        for (int k = 0; k < nsteps; ++k) {
+            if (checkpoints && k % S == 0) {
+                T* src[6]; T* dst[6];
+                ckpt_ptrs(st, src);
+                for (int f = 0; f < ckpt_fields; ++f) dst[f] = ckpt_slot(k / S, f);
+                copy_fields(dst, src, s);
+            }
+            bind_state(p, st);
+            set_inject(p, true, g0, k, nullptr);
+            p.rec.rowptr = at<int>(off.recrow) + (size_t)g0 * nrec;
+            p.rec.off = at<long long>(off.recoff);
+            p.rec.w = at<T>(off.recw);
+            p.rec.traces = tr + (long long)k * nrec;
+            p.rec.tr_sstride = (long long)nsteps * nrec;
+            p.rec.nrec = nrec;
+            p.rec.blocks = nrec > 0 ? ceil_div((long long)gn * nrec, bz) : 0;
+            launch(p, kFwd, s);
+            advance(st);
+        }
+    }
+
+    void backward_sweep(int g0, int gn, cudaStream_t s) {
+        zero_state(off.A, off.AX, off.AY, off.AZ, off.AS, s);
+        cudaMemsetAsync(ws + off.ic, 0, field_bytes, s);
+        State adj = make_state(off.A, off.AX, off.AY, off.AZ, off.AS);
+        const T* resid = at<T>(off.traces);
+        for (int seg = nseg - 1; seg >= 0; --seg) {
+            const int k0 = seg * S, k1 = std::min(k0 + S, nsteps) - 1;
+            // restore the forward state at k0 into buffer set 0
+            State fw = make_state(off.U, off.PX, off.PY, off.PZ, off.PS);
+            {
+                T* dst[6]; T* src[6];
+                ckpt_ptrs(fw, dst);
+                for (int f = 0; f < ckpt_fields; ++f) src[f] = ckpt_slot(seg, f);
+                copy_fields(dst, src, s);
+            }
+            WaveParams<T> p = base_params(g0, gn);
+            for (int k = k0; k <= k1; ++k) {
+                bind_state(p, fw);
+                set_inject(p, true, g0, k, nullptr);
+                p.dw_out = (k % p_img == 0) ? fld(off.replay) + (size_t)(k - k0) * fstride * G : nullptr;
+                launch(p, kRecomp, s);
+                advance(fw);
+            }
+            WaveParams<T> q = base_params(g0, gn);
+            for (int k = k1; k >= k0; --k) {
+                bind_state(q, adj);
+                set_inject(q, false, g0, k, resid);
+                q.image = (k % p_img == 0);
+                q.dw_in = fld(off.replay) + (size_t)(k - k0) * fstride * G;
+                q.ic = fld(off.ic);
+                launch(q, kAdj, s);
+                advance(adj);
+            }
+        }
+    }
+
+    void enqueue_forward(void* traces_out, cudaStream_t s) {
+        const size_t tr_group = (size_t)nsteps * nrec * sizeof(T);
+        for (int g0 = 0; g0 < nshots; g0 += G) {
+            int gn = std::min(G, nshots - g0);
+            forward_sweep(g0, gn, false, s);
+            if (traces_out && nrec > 0)
+                cudaMemcpyAsync(static_cast<char*>(traces_out) + (size_t)g0 * tr_group, ws + off.traces,
+                                tr_group * gn, cudaMemcpyDeviceToDevice, s);
+        }
+    }
+
+    void enqueue_gradient(const void* dobs, double* grad, double* rnorm2, void* traces_out, bool with_grad,
+                          bool migrate, cudaStream_t s) {
+        const size_t tr_group = (size_t)nsteps * nrec * sizeof(T);
+        if (with_grad) cudaMemsetAsync(ws + off.gpad, 0, (size_t)nx * ny * nz * sizeof(double), s);
+        cudaMemsetAsync(ws + off.rnorm, 0, sizeof(double), s);
+        for (int g0 = 0; g0 < nshots; g0 += G) {
+            int gn = std::min(G, nshots - g0);
+            forward_sweep(g0, gn, with_grad, s);
+            if (traces_out && nrec > 0)
+                cudaMemcpyAsync(static_cast<char*>(traces_out) + (size_t)g0 * tr_group, ws + off.traces,
+                                tr_group * gn, cudaMemcpyDeviceToDevice, s);
+            long long n = (long long)gn * nsteps * nrec;
+            if (n > 0) {
+                residual_kernel<T><<<kRedBlocks, kRedThreads, 0, s>>>(
+                    static_cast<const T*>(dobs) + (size_t)g0 * nsteps * nrec, at<T>(off.traces), n,
+                    at<double>(off.partial), migrate ? 1 : 0);
+                sum_partials_kernel<<<1, kRedThreads, 0, s>>>(at<double>(off.partial), kRedBlocks,
+                                                              at<double>(off.rnorm), 1);
+                launches += 2;
+            }
+            if (with_grad) {
+                backward_sweep(g0, gn, s);
+                long long nc = (long long)nx * ny * nz;
+                // migration returns F* r = -dt p sum q dWaveOp (adjoint_model, :367-371);
+                // the gradient is its negative (compute_gradient, :167)
+                reduce_ic_kernel<T><<<grid_for(nc, 256), 256, 0, s>>>(
+                    fld(off.ic), fstride, gn, nx, ny, nz, hx, hy, rows_y, ldz,
+                    migrate ? -dt * p_img : dt * p_img, at<double>(off.gpad));
+                ++launches;
+            }
+        }
+        if (with_grad) {
+            const int px = nx - pad_lo[0] - pad_hi[0], py = ny - pad_lo[1] - pad_hi[1],
+                      pz = nz - pad_lo[2] - pad_hi[2];
+            fold_kernel<<<grid_for((long long)px * py * pz, 256), 256, 0, s>>>(
+                at<double>(off.gpad), nx, ny, nz, pad_lo[0], pad_hi[0], pad_lo[1], pad_hi[1], pad_lo[2],
+                pad_hi[2], grad);
+            ++launches;
+        }
+        cudaMemcpyAsync(rnorm2, ws + off.rnorm, sizeof(double), cudaMemcpyDeviceToDevice, s);
+    }
+
+    // run `enqueue` eagerly or through a cached CUDA graph keyed by the I/O pointers
+    template <typename F>
+    int run(int kind, const void* a, const void* b, const void* c, const void* d, cudaStream_t s, F enqueue) {
+        if (!use_graph) {
+            launches = 0;
+            enqueue(s);
+            PGB_CHECK_CUDA(cudaGetLastError());
+            last_launches = launches;
+            return PYSIT_OK;
+        }
+        GraphKey key{kind, a, b, c, d};
+        auto it = graphs.find(key);
+        if (it == graphs.end()) {
+            launches = 0;
+            cudaGraph_t graph = nullptr;
+            PGB_CHECK_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+            enqueue(cap);
+            cudaError_t e = cudaStreamEndCapture(cap, &graph);
+            if (e != cudaSuccess) return cuda_status(e, "cudaStreamEndCapture");
+            GraphRec rec;
+            e = cudaGraphInstantiate(&rec.exec, graph, 0);
+            cudaGraphDestroy(graph);
+            if (e != cudaSuccess) return cuda_status(e, "cudaGraphInstantiate");
+            rec.launches = launches;
+            it = graphs.emplace(key, rec).first;
+        }
+        PGB_CHECK_CUDA(cudaGraphLaunch(it->second.exec, s));
+        last_launches = it->second.launches;
+        return PYSIT_OK;
+    }
+
+    int forward(void* traces, cudaStream_t s) override {
+        PGB_REQUIRE(ws, "no workspace bound");
+        PGB_REQUIRE(model_set, "pysit_plan_set_model must be called first");
+        return run(0, traces, nullptr, nullptr, nullptr, s,
+                   [&](cudaStream_t st) { enqueue_forward(traces, st); });
+    }
+
+    int gradient(const void* dobs, double* grad, double* rnorm2, void* traces, cudaStream_t s,
+                 bool with_grad, bool migrate) override {
+        PGB_REQUIRE(ws, "no workspace bound");
+        PGB_REQUIRE(model_set, "pysit_plan_set_model must be called first");
+        PGB_REQUIRE(dobs || nrec == 0, "NULL observed data");
+        PGB_REQUIRE(rnorm2, "NULL misfit output");
+        PGB_REQUIRE(!with_grad || grad, "NULL gradient output");
+        return run(migrate ? 3 : with_grad ? 1 : 2, dobs, grad, rnorm2, traces, s, [&](cudaStream_t st) {
+            enqueue_gradient(dobs, grad, rnorm2, traces, with_grad, migrate, st);
+        });
+    }
+};
+
+}  // namespace
+}  // namespace pgb
+
+using namespace pgb;
+
+extern "C" int pysit_plan_create(const pysit_plan_desc* d, pysit_plan** out) {
+    PGB_REQUIRE(d && out, "NULL argument");
+    *out = nullptr;
+    PGB_REQUIRE(d->dim >= 1 && d->dim <= 3, "dim must be 1, 2 or 3");
+    PGB_REQUIRE(d->order == 2 || d->order == 4 || d->order == 6 || d->order == 8, "order must be 2/4/6/8");
+    PGB_REQUIRE(d->dtype == PYSIT_F32 || d->dtype == PYSIT_F64, "bad dtype");
+    PGB_REQUIRE(d->nsteps >= 1, "nsteps must be >= 1");
+    PGB_REQUIRE(d->dt > 0, "dt must be positive");
+    PGB_REQUIRE(d->nshots >= 1 && d->shots_per_launch >= 1, "need at least one shot");
+    PGB_REQUIRE(d->imaging_period >= 1 && d->checkpoint_every >= 1, "imaging_period / checkpoint_every must be >= 1");
+    PGB_REQUIRE(d->nsrc >= 0 && d->nrec >= 0, "negative point counts");
+    PGB_REQUIRE(d->nsrc == 0 || (d->src_tap_ptr && d->src_amp), "source taps / amplitudes missing");
+    PGB_REQUIRE(d->nrec == 0 || d->rec_tap_ptr, "receiver taps missing");
+    for (int a = 0; a < 3; ++a) {
+        bool used = (d->dim == 1 && a == 2) || (d->dim == 2 && a != 1) || d->dim == 3;
+        if (!used) continue;
+        PGB_REQUIRE(d->n[a] >= 3, "grid axis %d must have >= 3 cells", a);
+        PGB_REQUIRE(d->delta[a] > 0, "grid spacing on axis %d must be positive", a);
+        PGB_REQUIRE(d->pad_lo[a] >= 0 && d->pad_hi[a] >= 0 && d->pad_lo[a] + d->pad_hi[a] < d->n[a],
+                    "bad padding on axis %d", a);
+    }
+    if (d->dim == 3) PGB_REQUIRE(d->n[1] >= 3, "3D needs ny >= 3");
+    std::unique_ptr<pysit_plan> p;
+    int rc;
+    if (d->dtype == PYSIT_F64) {
+        auto q = std::make_unique<PlanT<double>>();
+        rc = q->init(*d);
+        p = std::move(q);
+    } else {
+        auto q = std::make_unique<PlanT<float>>();
+        rc = q->init(*d);
+        p = std::move(q);
+    }
+    if (rc) return rc;
+    *out = p.release();
+    return PYSIT_OK;
+}
+
+extern "C" int pysit_plan_destroy(pysit_plan* p) {
+    delete p;
+    return PYSIT_OK;
+}
+
+extern "C" int pysit_plan_workspace_bytes(const pysit_plan* p, uint64_t* bytes) {
+    PGB_REQUIRE(p && bytes, "NULL argument");
+    return p->workspace_bytes(bytes);
+}
+
+extern "C" int pysit_plan_bind_workspace(pysit_plan* p, void* ws, uint64_t bytes, void* stream) {
+    PGB_REQUIRE(p, "NULL plan");
+    return p->bind(ws, bytes, (cudaStream_t)stream);
+}
+
+extern "C" int pysit_plan_set_model(pysit_plan* p, const double* C, void* stream) {
+    PGB_REQUIRE(p, "NULL plan");
+    return p->set_model(C, (cudaStream_t)stream);
+}
+
+extern "C" int pysit_plan_forward(pysit_plan* p, void* traces, void* stream) {
+    PGB_REQUIRE(p, "NULL plan");
+    return p->forward(traces, (cudaStream_t)stream);
+}
+
+extern "C" int pysit_plan_gradient(pysit_plan* p, const void* dobs, double* grad, double* rnorm2,
+                                   void* traces, void* stream) {
+    PGB_REQUIRE(p, "NULL plan");
+    return p->gradient(dobs, grad, rnorm2, traces, (cudaStream_t)stream, true, false);
+}
+
+extern "C" int pysit_plan_migrate(pysit_plan* p, const void* operand, double* image, double* norm2,
+                                  void* stream) {
+    PGB_REQUIRE(p, "NULL plan");
+    return p->gradient(operand, image, norm2, nullptr, (cudaStream_t)stream, true, true);
+}
+
+extern "C" int pysit_plan_misfit(pysit_plan* p, const void* dobs, double* rnorm2, void* traces,
+                                 void* stream) {
+    PGB_REQUIRE(p, "NULL plan");
+    return p->gradient(dobs, nullptr, rnorm2, traces, (cudaStream_t)stream, false, false);
+}
+
+extern "C" int pysit_plan_last_launch_count(const pysit_plan* p, int64_t* n) {
+    PGB_REQUIRE(p && n, "NULL argument");
+    *n = p->last_launches;
+    return PYSIT_OK;
+}

@@ -1,0 +1,143 @@
+// Device-side data layout and kernel parameters of the batched wave pipeline.
+//
+// Internal field layout (per shot, per field): a zero halo of HX = 4 rows on
+// both x sides (2D/3D), HY = 4 rows on both y sides (3D), and along z a row
+// pitch `ldz` (multiple of 32 elements) with the grid starting at z offset
+// OZ = 4.  Cell (i, j, k) of the padded PySIT grid lives at
+//     ((i + HX) * (ny + 2*HY) + (j + HY)) * ldz + OZ + k.
+// The halos are never written with non-zero values, so the stencils read the
+// reference's zero extension without bounds tests, rows start 128-byte
+// aligned and z-vectors of 16 bytes are aligned.
+#pragma once
+
+#include "common.cuh"
+
+namespace pgb {
+
+constexpr int kHalo = 4;  // x/y halo rows and smem z halo (max stencil radius)
+constexpr int kOZ = 4;    // z offset of cell k = 0 inside a row
+
+template <typename T> struct V16;
+template <> struct V16<float> { using type = float4; static constexpr int N = 4; };
+template <> struct V16<double> { using type = double2; static constexpr int N = 2; };
+
+template <typename T>
+struct alignas(16) VReg {
+    T v[V16<T>::N];
+};
+
+template <typename T>
+__device__ __forceinline__ VReg<T> vzero() {
+    VReg<T> r;
+#pragma unroll
+    for (int i = 0; i < V16<T>::N; ++i) r.v[i] = T(0);
+    return r;
+}
+template <typename T>
+__device__ __forceinline__ VReg<T> vld_ro(const T* p) {  // read-only path
+    VReg<T> r;
+    *reinterpret_cast<typename V16<T>::type*>(r.v) =
+        __ldg(reinterpret_cast<const typename V16<T>::type*>(p));
+    return r;
+}
+template <typename T>
+__device__ __forceinline__ VReg<T> vld(const T* p) {
+    VReg<T> r;
+    *reinterpret_cast<typename V16<T>::type*>(r.v) =
+        *reinterpret_cast<const typename V16<T>::type*>(p);
+    return r;
+}
+template <typename T>
+__device__ __forceinline__ VReg<T> vld_stream(const T* p) {  // read once: evict-first
+    VReg<T> r;
+    *reinterpret_cast<typename V16<T>::type*>(r.v) =
+        __ldcs(reinterpret_cast<const typename V16<T>::type*>(p));
+    return r;
+}
+template <typename T>
+__device__ __forceinline__ void vst(T* p, const VReg<T>& r) {
+    *reinterpret_cast<typename V16<T>::type*>(p) = *reinterpret_cast<const typename V16<T>::type*>(r.v);
+}
+template <typename T>
+__device__ __forceinline__ void vst_stream(T* p, const VReg<T>& r) {
+    __stcs(reinterpret_cast<typename V16<T>::type*>(p), *reinterpret_cast<const typename V16<T>::type*>(r.v));
+}
+
+// Kernel modes of the batched step.
+enum StepMode : int {
+    kFwd = 0,     // forward step; records traces of u_k
+    kRecomp = 1,  // forward recompute; writes the imaging operand dWaveOp_k
+    kAdj = 2,     // adjoint step driven by the residual; accumulates ic += q_k * dWaveOp_k
+};
+
+// Injection operator of one step: per shot a box of cells [x0,x1) x [y0,y1) x [z0,z1)
+// with CSR rows over the box cells (x-major, z fastest); entries (point, weight).
+// rhs(cell) = sum_e w[e] * amp[shot * amp_sstride + pt[e]].
+template <typename T>
+struct Inject {
+    const int* box;          // [nshot][6]: x0, x1, y0, y1, z0, z1 (grid coords)
+    const long long* rpbase; // [nshot] offset of the shot's first row pointer
+    const int* rowptr;       // CSR row pointers (absolute entry indices)
+    const int* pt;           // entry point index
+    const T* w;              // entry weight
+    const T* amp;            // amplitudes of this step for shot 0
+    long long amp_sstride;   // amplitude stride between shots
+    int on;                  // 0: no injection this step
+};
+
+// Trace recording of u_k: per (shot, receiver) a CSR row of taps.
+template <typename T>
+struct Record {
+    const int* rowptr;       // [nshot*nrec + 1] absolute tap index (shot-major)
+    const long long* off;    // tap offset inside a field (internal layout)
+    const T* w;              // tap weight (sampling operator)
+    T* traces;               // trace sample k of shot 0 receiver 0
+    long long tr_sstride;    // stride between shots in the trace array
+    int nrec;
+    int blocks;              // number of recorder blocks appended to the grid
+};
+
+template <typename T>
+struct WaveParams {
+    // geometry
+    int nx, ny, nz;          // padded grid (ny = 1 in 2D)
+    int ldz;                 // row pitch (elements)
+    int rows_y;              // ny + 2*HY
+    long long fstride;       // elements between consecutive shots of one field
+    int hx, hy;              // halos (4 / 0 in 2D)
+    // tiling
+    int tx;                  // rows swept per block along x
+    int ty;                  // 3D: y rows per block (blockDim.y)
+    int ntz, nty, ntx;       // tiles per shot along z, y, x
+    int nshot;               // shots in this launch
+    // wavefields (shot 0 base)
+    T* u_prev;               // in: u_{k-1}; out: u_{k+1} (same cell, in place)
+    const T* u_cur;          // u_k
+    const T* phx_in; T* phx_out;
+    const T* phy_in; T* phy_out;
+    const T* phz_in; T* phz_out;
+    const T* psi_in; T* psi_out;
+    const T* c2;             // C^2, shared by all shots (internal layout)
+    // PML (kernel convention) and mesh sigma maps, full length per axis
+    const T *sgx, *sgy, *sgz;
+    const T *mgx, *mgy, *mgz;
+    int pxl, pxr, pyl, pyr, pzl, pzr;  // padding widths holding PML state
+    // scalars
+    T dt, dt2, idt2, i2dt, idx, idx2, idy, idy2, idz, idz2;
+    // injection / recording / imaging
+    Inject<T> inj;
+    Record<T> rec;
+    T* dw_out;               // kRecomp: imaging operand of this step (shot 0 base)
+    const T* dw_in;          // kAdj: imaging operand of this step
+    T* ic;                   // kAdj: imaging accumulator (shot 0 base)
+    int image;               // kAdj: accumulate this step
+};
+
+template <typename T, int R, int MODE>
+void launch_wave2d(const WaveParams<T>& p, int bz, cudaStream_t s);
+template <typename T, int R, int MODE>
+void launch_wave3d(const WaveParams<T>& p, int bz, cudaStream_t s);
+template <typename T, int R, int MODE>
+void launch_wave1d(const WaveParams<T>& p, int bz, cudaStream_t s);
+
+}  // namespace pgb

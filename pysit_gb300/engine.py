@@ -1,0 +1,242 @@
+"""Batched checkpointed pipeline over the C ABI (pysit_plan_*).
+
+A ``WavePlan`` binds one solver configuration (grid, order, precision, dt,
+nsteps) and one list of shots to a device workspace owned by torch.  It runs
+the forward modelling of all shots (``forward``), their misfit (``misfit``) or
+misfit plus gradient (``gradient``) with one library call each, the time loops
+captured in CUDA graphs.  It replaces, for the batch, the per-shot loops of
+TemporalModeling.forward_model / adjoint_model and TemporalLeastSquares
+(pysit/modeling/temporal_modeling.py:60-387,
+pysit/objective_functions/temporal_least_squares.py:27-198).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import _native
+from .solvers.cda_time import axis_sigma_map
+
+__all__ = ["WavePlan", "padded_cells", "default_checkpoint_every"]
+
+_DESC_AXIS = {1: [2], 2: [0, 2], 3: [0, 1, 2]}  # mesh axis -> (x, y, z) slot of the descriptor
+
+
+def padded_cells(mesh, cells):
+    """Map flat indices of the unpadded grid to flat indices of the padded grid."""
+    cells = np.asarray(cells, dtype=np.int64)
+    idx = np.unravel_index(cells, tuple(mesh.shape(include_bc=False, as_grid=True)))
+    idx = [i + mesh.parameters[a].lbc.n for a, i in enumerate(idx)]
+    return np.ravel_multi_index(idx, tuple(mesh.shape(include_bc=True, as_grid=True))).astype(np.int64)
+
+
+def default_checkpoint_every(nsteps, dim):
+    """Segment length minimising replay + checkpoint storage: sqrt(fields_per_checkpoint * nsteps)."""
+    fields = {1: 3, 2: 4, 3: 6}[dim]
+    return int(max(1, min(nsteps, round(math.sqrt(fields * nsteps)))))
+
+
+def _dptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class WavePlan:
+    """Device plan of one (solver configuration, shot list)."""
+
+    def __init__(self, solver, shots, imaging_period=1, checkpoint_every=None, shots_per_launch=None,
+                 use_graph=None):
+        torch = _native.require_cuda()
+        lib = _native.load()
+        self.solver = solver
+        self.shots = list(shots)
+        mesh = solver.mesh
+        self.mesh = mesh
+        self.dim = mesh.dim
+        self.nsteps = solver.nsteps
+        self.dt = solver.dt
+        self.imaging_period = int(imaging_period)
+        self.nshots = len(self.shots)
+        self.tdtype = torch.float64 if solver.dtype == np.double else torch.float32
+        if checkpoint_every is None:
+            checkpoint_every = solver.checkpoint_every or default_checkpoint_every(self.nsteps, self.dim)
+        self.checkpoint_every = int(min(max(1, checkpoint_every), self.nsteps))
+        if shots_per_launch is None:
+            shots_per_launch = solver.shots_per_launch or self.nshots
+        self.shots_per_launch = int(max(1, min(shots_per_launch, self.nshots)))
+        use_graph = solver.use_graph if use_graph is None else use_graph
+
+        d = _native.PlanDesc()
+        d.dim = self.dim
+        d.order = solver.spatial_accuracy_order
+        d.dtype = _native.PYSIT_F64 if solver.dtype == np.double else _native.PYSIT_F32
+        full = mesh.shape(include_bc=True, as_grid=True)
+        keep = []  # numpy buffers referenced by the descriptor during plan creation
+        for slot in range(3):
+            d.n[slot] = 1
+            d.delta[slot] = 1.0
+        for a, slot in enumerate(_DESC_AXIS[self.dim]):
+            p = mesh.parameters[a]
+            d.n[slot] = full[a]
+            d.delta[slot] = p.delta
+            d.pad_lo[slot] = p.lbc.n
+            d.pad_hi[slot] = p.rbc.n
+            lp, rp = solver._profiles(a)
+            lp, rp = np.ascontiguousarray(lp), np.ascontiguousarray(rp)
+            mp = np.ascontiguousarray(axis_sigma_map(mesh, a))
+            keep += [lp, rp, mp]
+            d.sig_l[slot] = _dptr(lp)
+            d.nsig_l[slot] = len(lp)
+            d.sig_r[slot] = _dptr(rp)
+            d.nsig_r[slot] = len(rp)
+            d.sigmap[slot] = _dptr(mp)
+        d.dt = self.dt
+        d.nsteps = self.nsteps
+        d.imaging_period = self.imaging_period
+        d.checkpoint_every = self.checkpoint_every
+        d.shots_per_launch = self.shots_per_launch
+        d.nshots = self.nshots
+        d.use_graph = 1 if use_graph else 0
+
+        ts = np.arange(self.nsteps) * self.dt
+        # sources
+        s_ptr, s_cell, s_pt, s_w, amps = [0], [], [], [], []
+        nsrc = max(getattr(s.sources, "source_count", 1) for s in self.shots)
+        for s in self.shots:
+            cells, pts, w = s.sources.taps()
+            s_cell.append(padded_cells(mesh, cells)); s_pt.append(np.asarray(pts, np.int32))
+            s_w.append(np.asarray(w, float)); s_ptr.append(s_ptr[-1] + len(cells))
+            a = np.zeros((self.nsteps, nsrc))
+            aa = s.sources.amplitudes(ts)
+            a[:, :aa.shape[1]] = aa
+            amps.append(a)
+        # receivers
+        r_ptr, r_cell, r_pt, r_ws, r_wi = [0], [], [], [], []
+        self.nrec_shot = [s.receivers.receiver_count for s in self.shots]
+        nrec = max(self.nrec_shot)
+        for s in self.shots:
+            cells, recs, ws, wi = s.receivers.taps()
+            r_cell.append(padded_cells(mesh, cells)); r_pt.append(np.asarray(recs, np.int32))
+            r_ws.append(np.asarray(ws, float)); r_wi.append(np.asarray(wi, float))
+            r_ptr.append(r_ptr[-1] + len(cells))
+        self.nrec = nrec
+        self.nsrc = nsrc
+        arrs = dict(
+            src_tap_ptr=np.asarray(s_ptr, np.int64), src_tap_cell=np.concatenate(s_cell),
+            src_tap_point=np.concatenate(s_pt), src_tap_w=np.concatenate(s_w),
+            src_amp=np.ascontiguousarray(np.stack(amps)),
+            rec_tap_ptr=np.asarray(r_ptr, np.int64), rec_tap_cell=np.concatenate(r_cell),
+            rec_tap_point=np.concatenate(r_pt), rec_tap_wsample=np.concatenate(r_ws),
+            rec_tap_winject=np.concatenate(r_wi))
+        ctype = {np.int64: C.c_int64, np.int32: C.c_int32, np.float64: C.c_double}
+        for k, v in arrs.items():
+            v = np.ascontiguousarray(v)
+            keep.append(v)
+            setattr(d, k, v.ctypes.data_as(C.POINTER(ctype[v.dtype.type])))
+        d.nsrc = nsrc
+        d.nrec = nrec
+
+        h = C.c_void_p()
+        _native.check(lib.pysit_plan_create(C.byref(d), C.byref(h)))
+        self._h = h
+        nbytes = C.c_uint64()
+        _native.check(lib.pysit_plan_workspace_bytes(h, C.byref(nbytes)))
+        self.workspace_bytes = int(nbytes.value)
+        self.workspace = torch.empty(self.workspace_bytes + 256, dtype=torch.uint8, device="cuda")
+        base = self.workspace.data_ptr()
+        self._ws_ptr = (base + 255) // 256 * 256
+        _native.check(lib.pysit_plan_bind_workspace(h, C.c_void_p(self._ws_ptr), C.c_uint64(self.workspace_bytes),
+                                                    C.c_void_p(_native.stream_handle())))
+        self._model_version = None
+        # reusable outputs (stable pointers keep the captured graphs valid)
+        self.traces = torch.zeros((self.nshots, self.nsteps, nrec), dtype=self.tdtype, device="cuda")
+        self.dobs = torch.zeros_like(self.traces)
+        dof_phys = mesh.dof(include_bc=False)
+        self.grad = torch.zeros(dof_phys, dtype=torch.float64, device="cuda")
+        self.rnorm2 = torch.zeros(1, dtype=torch.float64, device="cuda")
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                _native.load().pysit_plan_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    # ---------------------------------------------------------------------------
+    def set_model(self):
+        """Upload the solver's current padded model (once per model change)."""
+        ver = (self.solver._model_change_count, id(self.solver._mp))
+        if ver != self._model_version:
+            C_dev = self.solver.device_model()
+            _native.check(_native.load().pysit_plan_set_model(self._h, C.c_void_p(C_dev.data_ptr()),
+                                                              C.c_void_p(_native.stream_handle())))
+            self._model_version = ver
+
+    def launches(self):
+        n = C.c_int64()
+        _native.check(_native.load().pysit_plan_last_launch_count(self._h, C.byref(n)))
+        return int(n.value)
+
+    def forward(self):
+        """Simulated traces of all shots, [nshots, nsteps, nrec] (device)."""
+        self.set_model()
+        _native.check(_native.load().pysit_plan_forward(self._h, C.c_void_p(self.traces.data_ptr()),
+                                                        C.c_void_p(_native.stream_handle())))
+        return self.traces
+
+    def load_observed(self, dobs=None):
+        """Copy observed data (resampled to this plan's time axis) into the device buffer.
+
+        ``dobs`` is a [nshots, nsteps, nrec] array/tensor; by default the shots'
+        recorded data are interpolated onto ``solver.ts()`` (ReceiverSet.interpolate_data)."""
+        torch = _native.require_cuda()
+        if dobs is None:
+            ts = self.solver.ts()
+            host = np.zeros((self.nshots, self.nsteps, self.nrec))
+            for i, s in enumerate(self.shots):
+                host[i, :, :self.nrec_shot[i]] = s.receivers.interpolate_data(ts)
+            dobs = host
+        if isinstance(dobs, np.ndarray):
+            src = torch.from_numpy(np.ascontiguousarray(dobs, dtype=np.float64 if self.tdtype == torch.float64
+                                                        else np.float32))
+            self.dobs.copy_(src.pin_memory() if src.numel() > (1 << 20) else src, non_blocking=True)
+        else:
+            self.dobs.copy_(dobs)
+        return self.dobs
+
+    def gradient(self, with_traces=False):
+        """Run misfit + gradient on the loaded observed data.
+
+        Returns (grad [dof_phys] FP64 device, rnorm2 [1] FP64 device); grad is with
+        respect to m = C**-2 with the PML strips folded (compute_gradient semantics)."""
+        self.set_model()
+        _native.check(_native.load().pysit_plan_gradient(
+            self._h, C.c_void_p(self.dobs.data_ptr()), C.c_void_p(self.grad.data_ptr()),
+            C.c_void_p(self.rnorm2.data_ptr()), C.c_void_p(self.traces.data_ptr() if with_traces else None),
+            C.c_void_p(_native.stream_handle())))
+        return self.grad, self.rnorm2
+
+    def misfit(self, with_traces=False):
+        self.set_model()
+        _native.check(_native.load().pysit_plan_misfit(
+            self._h, C.c_void_p(self.dobs.data_ptr()), C.c_void_p(self.rnorm2.data_ptr()),
+            C.c_void_p(self.traces.data_ptr() if with_traces else None), C.c_void_p(_native.stream_handle())))
+        return self.rnorm2
+
+
+def plan_for(solver, shots, imaging_period=1, **kw):
+    """Cached WavePlan of a solver for a shot list (rebuilt when dt/nsteps change)."""
+    key = (tuple(id(s) for s in shots), solver.dt, solver.nsteps, solver.precision,
+           solver.spatial_accuracy_order, int(imaging_period), tuple(sorted(kw.items())))
+    cache = solver._plans
+    p = cache.get(key)
+    if p is None:
+        # keep at most a few plans alive (each owns a workspace)
+        while len(cache) >= 2:
+            cache.pop(next(iter(cache)))
+        p = WavePlan(solver, shots, imaging_period=imaging_period, **kw)
+        cache[key] = p
+    return p

@@ -1,0 +1,3 @@
+"""Modelling (mirror of pysit.modeling for the time-domain CDA path)."""
+from .temporal_modeling import TemporalModeling  # noqa: F401
+from .data_modeling import generate_seismic_data, generate_shot_data_time  # noqa: F401

@@ -1,0 +1,77 @@
+"""Generate the golden fixtures of tests/golden/ by running the unmodified reference.
+
+Run in a container that has the reference tree (default /root/reference) after
+``make -C oracle`` built its SWIG module into oracle/_ref:
+
+    python tests/golden/make_golden.py            # all problems of tests/problems.py
+
+For every problem it stores (compressed .npz): the traces of every shot
+modelled on the true model by the reference's own ``generate_seismic_data``
+with ``kernel_implementation='cpp'`` (FP64), the gradient and objective of
+``TemporalLeastSquares.compute_gradient`` at the starting model, dt/nsteps of
+both models, and snapshots of host-side operators (source / receiver
+smearing weights, PML profiles, resampled observed data) that the product's
+host code must reproduce.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+import pysit_live  # noqa: E402
+import problems  # noqa: E402
+
+
+def _sparse_nz(op):
+    import scipy.sparse as spsp
+    op = op.tocsr() if hasattr(op, "tocsr") else spsp.csr_matrix(np.asarray(op))
+    coo = op.tocoo()
+    order = np.lexsort((coo.col, coo.row))
+    return np.asarray(coo.row)[order], np.asarray(coo.col)[order], np.asarray(coo.data)[order]
+
+
+def run(name):
+    pysit = pysit_live.import_pysit()
+    m, shots, solver, C, C0 = problems.build(pysit, name, kernel="cpp")
+    truth = solver.ModelParameters(m, {"C": C})
+    pysit.generate_seismic_data(shots, solver, truth)
+    dt_true, nsteps_true = solver.dt, solver.nsteps
+    traces = np.stack([s.receivers.data.copy() for s in shots])
+    obj = pysit.TemporalLeastSquares(solver)
+    start = solver.ModelParameters(m, {"C": C0})
+    aux = {"objective_value": (True, None), "residual_norm": (True, None)}
+    grad = obj.compute_gradient(shots, start, aux)
+    dt0, nsteps0 = solver.dt, solver.nsteps
+    dobs0 = np.stack([s.receivers.interpolate_data(solver.ts()) for s in shots])
+    out = dict(traces=traces, dt_true=dt_true, nsteps_true=nsteps_true, grad=grad.data.reshape(-1),
+               objective=aux["objective_value"][1], residual_norm=aux["residual_norm"][1],
+               dt0=dt0, nsteps0=nsteps0, dobs0=dobs0)
+    s0 = shots[0]
+    r, c, v = _sparse_nz(s0.sources.adjoint_sampling_operator)
+    out.update(src_rows=r, src_vals=v)
+    r, c, v = _sparse_nz(s0.receivers.sampling_operator)
+    out.update(rec_rows=r, rec_cols=c, rec_vals=v)
+    for a in range(m.dim):
+        p = m.parameters[a]
+        for side, bc in (("l", p.lbc), ("r", p.rbc)):
+            if bc.type == "pml":
+                out[f"sigma_{a}{side}"] = np.asarray(bc.sigma)
+        axis = {1: "z", 2: "xz", 3: "xyz"}[m.dim][a]
+        out[f"sigmap_{a}"] = np.asarray(solver.operator_components["s" + axis])
+    out["ricker"] = np.array([pysit.RickerWavelet(problems.SPECS[name]["f"])(t) for t in (0.0, 0.01, 0.05, 0.1)])
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
+    print(f"{name}: shots={len(shots)} nsteps_true={nsteps_true} nsteps0={nsteps0} "
+          f"|grad|={np.linalg.norm(out['grad']):.6e} objective={out['objective']:.6e}")
+
+
+if __name__ == "__main__":
+    names = sys.argv[1:] or list(problems.SPECS)
+    for n in names:
+        run(n)

@@ -1,0 +1,163 @@
+"""GPU parity of the modelling / gradient pipeline against the reference.
+
+Reference outputs come from tests/golden/ (the unmodified reference run with
+kernel_implementation='cpp', FP64) and from the CPU oracle (pinned to the same
+reference).  Tolerances (relative L2):
+  FP64  traces <= 1e-11, gradient <= 1e-9, objective <= 1e-10
+  FP32  traces <= 1e-4,  gradient <= 1e-3 (against the FP64 reference)
+"""
+import numpy as np
+import pytest
+
+import pipeline
+import problems
+import pysit_gb300 as api
+
+pytestmark = pytest.mark.gpu
+
+NAMES_2D = ["cfg1", "o2", "o6", "o8", "dirichlet"]
+NAMES_ALL = NAMES_2D + ["1d", "3d", "3d_o8"]
+
+
+def _rel(a, b):
+    a, b = np.ravel(np.asarray(a, float)), np.ravel(np.asarray(b, float))
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def _setup(name, g, precision="double", **solver_kw):
+    m, shots, solver, C, C0 = problems.build(api, name, precision=precision)
+    for k, v in solver_kw.items():
+        setattr(solver, k, v)
+    ts_true = np.arange(int(g["nsteps_true"])) * float(g["dt_true"])
+    for s, d in zip(shots, g["traces"]):
+        s.reset_time_series(ts_true)
+        s.receivers.data[:] = d
+    return m, shots, solver, C, C0
+
+
+@pytest.mark.parametrize("name", NAMES_ALL)
+def test_generate_seismic_data_matches_reference(name, golden):
+    g = golden(name)
+    m, shots, solver, C, C0 = problems.build(api, name)
+    api.generate_seismic_data(shots, solver, solver.ModelParameters(m, {"C": C}))
+    assert solver.nsteps == int(g["nsteps_true"])
+    tr = np.stack([s.receivers.data for s in shots])
+    assert _rel(tr, g["traces"]) < 1e-11
+
+
+@pytest.mark.parametrize("name", NAMES_ALL)
+def test_batched_gradient_matches_reference(name, golden):
+    g = golden(name)
+    m, shots, solver, C, C0 = _setup(name, g)
+    obj = api.TemporalLeastSquares(solver)
+    aux = {"objective_value": (True, None), "residual_norm": (True, None)}
+    grad = obj.compute_gradient(shots, solver.ModelParameters(m, {"C": C0}), aux)
+    assert solver.nsteps == int(g["nsteps0"])
+    assert _rel(grad.data, g["grad"]) < 1e-9
+    assert aux["objective_value"][1] == pytest.approx(float(g["objective"]), rel=1e-10)
+    assert aux["residual_norm"][1] == pytest.approx(float(g["residual_norm"]), rel=1e-10)
+    assert obj.evaluate(shots, solver.ModelParameters(m, {"C": C0})) == pytest.approx(float(g["objective"]),
+                                                                                        rel=1e-10)
+
+
+@pytest.mark.parametrize("name", ["cfg1", "o8", "1d", "3d"])
+def test_plain_per_shot_gradient_matches_reference(name, golden):
+    g = golden(name)
+    m, shots, solver, C, C0 = _setup(name, g)
+    obj = api.TemporalLeastSquares(solver, batched=False)
+    aux = {"objective_value": (True, None)}
+    grad = obj.compute_gradient(shots, solver.ModelParameters(m, {"C": C0}), aux)
+    assert _rel(grad.data, g["grad"]) < 1e-10
+    assert aux["objective_value"][1] == pytest.approx(float(g["objective"]), rel=1e-10)
+
+
+@pytest.mark.parametrize("name", NAMES_2D + ["3d"])
+def test_fp32_batched_gradient_within_tolerance(name, golden):
+    g = golden(name)
+    m, shots, solver, C, C0 = problems.build(api, name, precision="single")
+    api.generate_seismic_data(shots, solver, solver.ModelParameters(m, {"C": C}))
+    tr = np.stack([s.receivers.data for s in shots])
+    assert _rel(tr, g["traces"]) < 1e-4
+    m, shots, solver, C, C0 = _setup(name, g, precision="single")
+    grad = api.TemporalLeastSquares(solver).compute_gradient(shots, solver.ModelParameters(m, {"C": C0}))
+    assert _rel(grad.data, g["grad"]) < 1e-3
+
+
+@pytest.mark.parametrize("p", [2, 3])
+def test_imaging_period_matches_oracle(p, golden):
+    g = golden("o6")
+    m, shots, solver, C, C0 = _setup("o6", g)
+    grad = api.TemporalLeastSquares(solver, imaging_period=p).compute_gradient(
+        shots, solver.ModelParameters(m, {"C": C0}))
+    Ps = [problems.oracle_problem(solver, s) for s in shots]
+    dobs = [s.receivers.interpolate_data(solver.ts()) for s in shots]
+    ref, _ = pipeline.gradient(Ps, dobs, imaging_period=p)
+    assert _rel(grad.data, ref) < 1e-9
+
+
+@pytest.mark.parametrize("kw", [dict(checkpoint_every=1), dict(checkpoint_every=7), dict(checkpoint_every=10 ** 6),
+                                dict(shots_per_launch=1), dict(use_graph=False)])
+def test_schedule_variants_agree(kw, golden):
+    g = golden("o8")
+    m, shots, solver, C, C0 = _setup("o8", g, **kw)
+    grad = api.TemporalLeastSquares(solver).compute_gradient(shots, solver.ModelParameters(m, {"C": C0}))
+    assert _rel(grad.data, g["grad"]) < 1e-9
+
+
+def test_migrate_batched_equals_plain(golden):
+    g = golden("o6")
+    m, shots, solver, C, C0 = _setup("o6", g)
+    m0 = solver.ModelParameters(m, {"C": C0})
+    rng = np.random.default_rng(0)
+    solver.model_parameters = m0
+    op = rng.standard_normal((solver.nsteps, shots[0].receivers.receiver_count))
+    a = api.TemporalModeling(solver, batched=True).migrate_shot(shots[0], m0, op, 1)
+    b = api.TemporalModeling(solver, batched=False).migrate_shot(shots[0], m0, op, 1)
+    assert _rel(a.data, b.data) < 1e-10
+
+
+def test_forward_model_outputs_match_oracle(golden):
+    g = golden("o2")
+    m, shots, solver, C, C0 = problems.build(api, "o2")
+    m1 = solver.ModelParameters(m, {"C": C})
+    tm = api.TemporalModeling(solver)
+    rv = tm.forward_model(shots[0], m1, 1, ["simdata", "dWaveOp", "wavefield"])
+    P = problems.oracle_problem(solver, shots[0])
+    sim, dws = pipeline.forward(P, want_dwaveop=True)
+    assert _rel(rv["simdata"], sim) < 1e-11
+    assert len(rv["dWaveOp"]) == len(dws)
+    assert _rel(np.stack([d.reshape(-1) for d in rv["dWaveOp"]]), np.stack(dws)) < 1e-10
+    assert len(rv["wavefield"]) == solver.nsteps
+    fast = tm.forward_model(shots[0], m1, 1, ["simdata"])["simdata"]
+    assert _rel(fast, sim) < 1e-11
+
+
+def test_time_step_on_host_solver_data_matches_oracle():
+    """The reference-compatible per-step protocol (numpy SolverData) on the GPU kernel."""
+    m, shots, solver, C, C0 = problems.build(api, "o6")
+    solver.model_parameters = solver.ModelParameters(m, {"C": C})
+    P = problems.oracle_problem(solver, shots[0])
+    sd = solver.SolverData()
+    rng = np.random.default_rng(9)
+    dof = m.dof(include_bc=True)
+    sd.k.data[:] = rng.standard_normal((sd.k.data.shape[0], 1)) * 1e-3
+    sd.km1.u[:] = rng.standard_normal((dof, 1)) * 1e-3
+    rhs = rng.standard_normal((dof, 1))
+    solver.time_step(sd, rhs, None)
+    aux = {"Phix": sd.k.Phix.reshape(-1), "Phiz": sd.k.Phiz.reshape(-1)}
+    ref_u, ref_aux = pipeline.step("oracle", 2, P["order"], sd.km1.u.reshape(-1), aux, sd.k.u.reshape(-1), P["C"],
+                                   rhs.reshape(-1), P["profiles"], P["dt"], P["deltas"], P["shape"])
+    assert _rel(sd.kp1.u, ref_u) < 1e-13
+    assert _rel(sd.kp1.Phix, ref_aux["Phix"]) < 1e-13
+    dW = solver.compute_dWaveOp("time", sd)
+    ref_dw = pipeline.dwaveop(P, sd.km1.u.reshape(-1), sd.k.u.reshape(-1), sd.kp1.u.reshape(-1), None)
+    assert _rel(dW, ref_dw) < 1e-12
+
+
+def test_plan_reports_its_kernel_launches(golden):
+    g = golden("o6")
+    m, shots, solver, C, C0 = _setup("o6", g)
+    obj = api.TemporalLeastSquares(solver)
+    obj.compute_gradient(shots, solver.ModelParameters(m, {"C": C0}))
+    n = obj.last_plan.launches()
+    assert n >= 3 * solver.nsteps

@@ -1,0 +1,115 @@
+"""Host-side mirror of the reference API (geometry, acquisition, factory, model
+arithmetic) against the reference's own outputs (golden fixtures, and the live
+reference where it is importable)."""
+import numpy as np
+import pytest
+
+import problems
+import pysit_gb300 as api
+from pysit_gb300.engine import default_checkpoint_every, padded_cells
+from pysit_gb300.solvers.model_parameter import fold_padding
+
+
+@pytest.mark.parametrize("name", list(problems.SPECS))
+def test_geometry_and_operators_match_golden(name, golden):
+    g = golden(name)
+    m, shots, solver, C, C0 = problems.build(api, name)
+    solver.model_parameters = solver.ModelParameters(m, {"C": C})
+    assert solver.nsteps == int(g["nsteps_true"]) and solver.dt == float(g["dt_true"])
+    for a in range(m.dim):
+        p = m.parameters[a]
+        for side, bc in (("l", p.lbc), ("r", p.rbc)):
+            if bc.type == "pml":
+                np.testing.assert_allclose(bc.sigma, g[f"sigma_{a}{side}"], rtol=0, atol=1e-12)
+        axis = {1: "z", 2: "xz", 3: "xyz"}[m.dim][a]
+        np.testing.assert_allclose(solver.operator_components["s" + axis], np.ravel(g[f"sigmap_{a}"]), atol=1e-12)
+    cells, _, w = shots[0].sources.taps()
+    order = np.argsort(cells)
+    np.testing.assert_array_equal(cells[order], g["src_rows"])
+    np.testing.assert_allclose(w[order], g["src_vals"], rtol=1e-15)
+    rc, rr, ws, _ = shots[0].receivers.taps()
+    order = np.lexsort((rc, rr))
+    np.testing.assert_array_equal(rr[order], g["rec_rows"])
+    np.testing.assert_array_equal(rc[order], g["rec_cols"])
+    np.testing.assert_allclose(ws[order], g["rec_vals"], rtol=1e-15)
+    f = problems.SPECS[name]["f"]
+    np.testing.assert_allclose([api.RickerWavelet(f)(t) for t in (0.0, 0.01, 0.05, 0.1)], g["ricker"], rtol=1e-15)
+
+
+def test_padded_cells_roundtrip():
+    m, shots, solver, C, C0 = problems.build(api, "o6")
+    u = np.arange(m.dof()).astype(float)
+    pad = m.pad_array(u.reshape(-1, 1)).reshape(-1)
+    cells = np.arange(m.dof())
+    np.testing.assert_array_equal(pad[padded_cells(m, cells)], u)
+    np.testing.assert_array_equal(m.unpad_array(pad.reshape(-1, 1)).reshape(-1), u)
+
+
+def test_fold_padding_sums_strips_and_preserves_total():
+    m, *_ = problems.build(api, "dirichlet")
+    rng = np.random.default_rng(1)
+    a = rng.standard_normal(m.dof(include_bc=True))
+    f = fold_padding(m, a)
+    assert f.shape == (m.dof(), 1)
+    assert f.sum() == pytest.approx(a.sum(), rel=1e-12)
+
+
+def test_linear_interpolation_matches_scipy():
+    from scipy.interpolate import interp1d
+    rng = np.random.default_rng(5)
+    ts = np.arange(40) * 0.013
+    d = rng.standard_normal((40, 3))
+    tn = np.arange(55) * 0.0101
+    ref = interp1d(ts, d, axis=0, kind="linear", bounds_error=False, fill_value=0.0)(tn)
+    np.testing.assert_allclose(api.linear_interpolate(ts, d, tn), ref, rtol=1e-13, atol=1e-15)
+
+
+@pytest.mark.parametrize("dim,cls", [(1, "ConstantDensityAcousticTimeScalar_1D_cuda"),
+                                     (2, "ConstantDensityAcousticTimeScalar_2D_cuda"),
+                                     (3, "ConstantDensityAcousticTimeScalar_3D_cuda")])
+@pytest.mark.parametrize("order", [2, 4, 6, 8])
+def test_factory_resolves_cuda_solvers(dim, cls, order):
+    """Mirror of pysit/solvers/tests/test_factories.py:55-79 for kernel_implementation='cuda'."""
+    name = {1: "1d", 2: "o6", 3: "3d"}[dim]
+    m, *_ = problems.build(api, name)
+    s = api.ConstantDensityAcousticWave(m, spatial_accuracy_order=order, kernel_implementation="cuda")
+    assert type(s).__name__ == cls
+    assert s.spatial_accuracy_order == order
+
+
+def test_factory_errors():
+    m, *_ = problems.build(api, "o6")
+    with pytest.raises(api.NoMatchError):
+        api.ConstantDensityAcousticWave(m, kernel_implementation="cpp")
+    with pytest.raises(api.NoMatchError):
+        api.ConstantDensityAcousticWave(m, spatial_accuracy_order=5, kernel_implementation="cuda")
+    with pytest.raises(api.NoMatchError):
+        api.ConstantDensityAcousticWave(m, precision="half", kernel_implementation="cuda")
+
+
+def test_model_arithmetic_is_linear_in_m():
+    m, shots, solver, C, C0 = problems.build(api, "o6")
+    a = api.ConstantDensityAcousticParameters(m, {"C": C})
+    b = api.ConstantDensityAcousticParameters(m, {"C": C0})
+    d = a - b
+    np.testing.assert_allclose(d.data, C.reshape(-1, 1) ** -2 - C0.reshape(-1, 1) ** -2)
+    c = b + d
+    np.testing.assert_allclose(c.C, a.C, rtol=1e-12)
+    p = a.with_padding(padding_mode="edge")
+    assert p.data.shape == (m.dof(include_bc=True), 1)
+    np.testing.assert_allclose(p.without_padding().C, a.C)
+    assert d.inner_product(d) == pytest.approx(float(np.sum(d.data ** 2)) * np.prod(m.deltas))
+
+
+def test_default_checkpoint_interval():
+    assert default_checkpoint_every(4000, 2) == 126
+    assert default_checkpoint_every(3000, 3) == 134
+    assert default_checkpoint_every(3, 2) == 3
+
+
+def test_cuda_path_has_no_cpu_fallback(monkeypatch):
+    import torch
+    from pysit_gb300 import _native
+    monkeypatch.setattr(torch.cuda, "is_available", lambda: False)
+    with pytest.raises(_native.PysitCudaError):
+        _native.require_cuda()

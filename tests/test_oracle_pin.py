@@ -1,0 +1,120 @@
+"""Pins of the CPU oracle (test infrastructure) against the reference itself.
+
+* the C restatement of the step (oracle/cda_oracle.c) against the reference's own
+  templates compiled from its headers into oracle/_ref (skipped where the reference
+  tree is absent, i.e. on the GPU host);
+* the oracle pipeline (forward, adjoint, gradient) plus pysit_gb300's host-side
+  geometry against golden outputs of the unmodified reference (tests/golden/).
+"""
+import numpy as np
+import pytest
+
+import pipeline
+import problems
+import pysit_gb300 as api
+
+AUX = pipeline.AUX
+
+
+def _rand_step_inputs(dim, shape, dtype, rng, npml=(3, 4)):
+    n = int(np.prod(shape))
+    km1, k = rng.standard_normal(n).astype(dtype), rng.standard_normal(n).astype(dtype)
+    aux = {a: rng.standard_normal(n).astype(dtype) for a in AUX[dim]}
+    C = (1500 + 1000 * rng.random(n)).astype(dtype)
+    rhs = rng.standard_normal(n).astype(dtype)
+    prof = []
+    for ax in range(dim):
+        nl, nr = npml
+        prof.append((np.linspace(80, 5, nl).astype(dtype), np.linspace(5, 80, nr).astype(dtype)))
+    return km1, aux, k, C, rhs, prof
+
+
+@pytest.mark.skipif(not pipeline.ref_available(), reason="reference templates (oracle/_ref) not built here")
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("order", [2, 4, 6, 8])
+@pytest.mark.parametrize("dim,shape", [(1, [37]), (2, [19, 23]), (3, [11, 12, 13])])
+def test_step_matches_reference_templates(dim, shape, order, dtype):
+    rng = np.random.default_rng(dim * 100 + order)
+    km1, aux, k, C, rhs, prof = _rand_step_inputs(dim, shape, dtype, rng)
+    deltas = [7.0, 9.0, 11.0][:dim]
+    dt = 1e-3
+    ref_u, ref_aux = pipeline.step("ref", dim, order, km1, aux, k, C, rhs, prof, dt, deltas, shape)
+    our_u, our_aux = pipeline.step("oracle", dim, order, km1, aux, k, C, rhs, prof, dt, deltas, shape)
+    tol = 1e-13 if dtype == np.float64 else 2e-5
+    scale = np.abs(ref_u).max()
+    assert np.abs(our_u - ref_u).max() <= tol * scale
+    for a in AUX[dim]:
+        s = max(np.abs(ref_aux[a]).max(), 1e-30)
+        assert np.abs(our_aux[a] - ref_aux[a]).max() <= tol * s, a
+
+
+@pytest.mark.skipif(not pipeline.ref_available(), reason="reference templates (oracle/_ref) not built here")
+@pytest.mark.parametrize("order", [4, 6])
+@pytest.mark.parametrize("dim,shape", [(1, [41]), (2, [21, 25]), (3, [12, 13, 14])])
+def test_step_matches_reference_openmp_variants(dim, shape, order):
+    """The hand-unrolled OpenMP kernels agree with the serial templates, except the
+    2D order-6 one, whose x-stencil branch for row nx-3 tests `k == nx-3`
+    (constant_density_acoustic_time_scalar_2D_6.h, the `else if (k == nx-3)` of the
+    x direction): it drops the +3 x-tap on column k = nx-3 and reads past the
+    array on row nx-3; and the 3D ones, whose Phi_y update differs near the high-y
+    side.  The oracle (and the CUDA path) follow the serial templates, which are
+    what kernel_implementation='cpp' runs."""
+    rng = np.random.default_rng(7 + order)
+    km1, aux, k, C, rhs, prof = _rand_step_inputs(dim, shape, np.float64, rng)
+    deltas = [5.0, 6.0, 7.0][:dim]
+    ref_u, _ = pipeline.step("ref", dim, order, km1, aux, k, C, rhs, prof, 5e-4, deltas, shape, omp=True)
+    our_u, _ = pipeline.step("oracle", dim, order, km1, aux, k, C, rhs, prof, 5e-4, deltas, shape)
+    diff = np.abs(our_u - ref_u).reshape(shape)
+    tol = 1e-12 * np.abs(ref_u).max()
+    if dim == 2 and order == 6:
+        nx = shape[0]
+        bad = np.argwhere(diff > tol)
+        assert len(bad) > 0
+        assert all(kk == nx - 3 or ii == nx - 3 for ii, kk in bad)
+    elif dim == 3:
+        assert diff.max() > tol  # known deviation of the reference's OpenMP 3D kernels
+    else:
+        assert diff.max() <= tol
+
+
+@pytest.mark.skipif(not pipeline.ref_available(), reason="reference templates (oracle/_ref) not built here")
+@pytest.mark.parametrize("sides", [(0, 4), (4, 0), (0, 0)])
+def test_step_dirichlet_sides_match_reference(sides):
+    rng = np.random.default_rng(3)
+    shape = [17, 19]
+    km1, aux, k, C, rhs, prof = _rand_step_inputs(2, shape, np.float64, rng, npml=sides)
+    ref_u, ref_aux = pipeline.step("ref", 2, 8, km1, aux, k, C, rhs, prof, 1e-3, [8.0, 8.0], shape)
+    our_u, our_aux = pipeline.step("oracle", 2, 8, km1, aux, k, C, rhs, prof, 1e-3, [8.0, 8.0], shape)
+    assert np.abs(our_u - ref_u).max() <= 1e-13 * np.abs(ref_u).max()
+    assert np.abs(our_aux["Phix"] - ref_aux["Phix"]).max() <= 1e-13 * np.abs(ref_aux["Phix"]).max()
+
+
+def _rel(a, b):
+    return np.linalg.norm(np.ravel(a) - np.ravel(b)) / max(np.linalg.norm(np.ravel(b)), 1e-300)
+
+
+@pytest.mark.parametrize("name", list(problems.SPECS))
+def test_oracle_pipeline_matches_reference_golden(name, golden):
+    g = golden(name)
+    m, shots, solver, C, C0 = problems.build(api, name)
+    solver.model_parameters = solver.ModelParameters(m, {"C": C})
+    assert solver.nsteps == int(g["nsteps_true"]) and solver.dt == pytest.approx(float(g["dt_true"]), rel=1e-15)
+    traces = np.stack([pipeline.forward(problems.oracle_problem(solver, s))[0] for s in shots])
+    assert _rel(traces, g["traces"]) < 1e-12
+    ts_true = np.arange(int(g["nsteps_true"])) * float(g["dt_true"])
+    for s, d in zip(shots, g["traces"]):
+        s.reset_time_series(ts_true)
+        s.receivers.data[:] = d
+    solver.model_parameters = solver.ModelParameters(m, {"C": C0})
+    assert solver.nsteps == int(g["nsteps0"])
+    dobs = [s.receivers.interpolate_data(solver.ts()) for s in shots]
+    assert _rel(np.stack(dobs), g["dobs0"]) < 1e-14
+    grad, r2 = pipeline.gradient([problems.oracle_problem(solver, s) for s in shots], dobs)
+    assert _rel(grad, g["grad"]) < 1e-11
+    assert 0.5 * r2 * solver.dt == pytest.approx(float(g["objective"]), rel=1e-12)
+
+
+def test_oracle_rejects_bad_arguments():
+    z = np.zeros(10)
+    with pytest.raises(ValueError):
+        pipeline.step("oracle", 1, 5, z, {"Phiz": z}, z, z + 1, z, [(z[:0], z[:0])], 1e-3, [1.0], [10])
