@@ -1,0 +1,282 @@
+"""Benchmark: FWI gradient shots/s (batched, checkpointed, FP32) on the 2D workload.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--scale s]
+
+A step is one full misfit + gradient of the 64-shot batch (1152 x 384 cells at
+12.5 m + 40-cell PML, order 8, 4000 time steps, checkpoints every 64 steps,
+seeded synthetic model: pysit_gb300.workloads.cfg2).  Output: one JSON line.
+  value  shots/s with the observed data already resident in HBM (plan call)
+  e2e    shots/s through the public torch.autograd API (FWIMisfit): every step
+         copies the velocity and the observed traces from pinned host memory to
+         the device and reads the gradient back
+  roofline  the forward step kernel: algorithmic bytes per launch / its mean
+         launch time (CUDA events), against the measured HBM copy peak
+  cpu_baseline  the CPU oracle port of the same pipeline on the host cores, on
+         a bounded sample of steps, extrapolated to a full gradient
+--impl reference times that CPU implementation alone (the reference arm).
+Multi-GPU (torchrun): independent replicas of the workload, one per rank
+(weak scaling); the time is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "FWI gradient shots/s, batched adjoint vs plain, 1xGB300 at <=1e-3 rel err; Gcell/s"
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle port (test infrastructure) on a bounded sample
+# ---------------------------------------------------------------------------
+def _cpu_worker(args):
+    scale, nsample, order = args
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import pipeline
+    import problems
+    from pysit_gb300 import workloads
+    m, shots, solver, C, C0 = workloads.cfg2(scale=scale, nshots=1, nsteps=nsample, order=order,
+                                             precision="double")
+    solver.model_parameters = solver.ModelParameters(m, {"C": C0})
+    P = problems.oracle_problem(solver, shots[0])
+    t0 = time.perf_counter()
+    sim, dws = pipeline.forward(P, want_dwaveop=True)
+    pipeline.adjoint_image(P, np.random.default_rng(0).standard_normal(sim.shape) * 1e-3, dws)
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(nsample=40, procs=None, scale=1.0, nsteps_full=4000, order=8):
+    """Shots/s of the CPU port: `procs` processes, each one shot-gradient of `nsample`
+    steps (forward with the per-step dWaveOp list, adjoint with imaging, FP64),
+    extrapolated to `nsteps_full` steps."""
+    procs = procs or max(1, min(os.cpu_count() or 1, 64))
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(procs) as pool:
+        times = pool.map(_cpu_worker, [(scale, nsample, order)] * procs)
+    wall = time.perf_counter() - t0
+    per_shot = max(times) * nsteps_full / nsample
+    return dict(value=procs / per_shot, unit="shots/s", cores=procs, kind="port",
+                sample=f"{procs} shots x {nsample} of {nsteps_full} steps (forward+dWaveOp+adjoint+imaging, FP64, "
+                       f"oracle/cda_oracle.c one process per shot), extrapolated; wall {wall:.1f}s")
+
+
+# ---------------------------------------------------------------------------
+def _clock_sampler():
+    cmd = ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+           "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+           "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+           "--format=csv,noheader,nounits", "-lms", "200"]
+    try:
+        return subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+    except Exception:
+        return None
+
+
+def _clock_summary(proc, gpu_index):
+    if proc is None:
+        return None
+    proc.terminate()
+    try:
+        out, _ = proc.communicate(timeout=5)
+    except Exception:
+        proc.kill()
+        out = ""
+    sm, mx, reasons = [], [], set()
+    for line in out.strip().splitlines():
+        f = [x.strip() for x in line.split(",")]
+        if len(f) < 9 or f[0] != str(gpu_index):
+            continue
+        try:
+            sm.append(float(f[1]))
+            mx.append(float(f[2]))
+        except ValueError:
+            continue
+        for name, v in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"), f[5:9]):
+            if v.lower() == "active":
+                reasons.add(name)
+    if not sm:
+        return None
+    return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+            "samples": len(sm)}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--scale", type=float, default=1.0, help="shrink the workload (tests only)")
+    ap.add_argument("--shots", type=int, default=64)
+    ap.add_argument("--nsteps", type=int, default=4000)
+    ap.add_argument("--shots-per-launch", type=int, default=None)
+    ap.add_argument("--cpu-sample", type=int, default=40)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    config = {"workload": "cfg2: 2D batched FWI gradient, 1152x384 @12.5m + 40 PML, order 8, 64 shots, "
+                          "1152 receivers, 8 Hz Ricker, 4000 steps, checkpoints every 64",
+              "grid_padded": [int(1152 * args.scale) + 80, int(384 * args.scale) + 80],
+              "shots": args.shots, "nsteps": args.nsteps, "order": 8, "checkpoint_every": 64,
+              "parallelism": f"replicas{world}" if world > 1 else "single",
+              "l2": "inputs larger than L2 (working set > 129 MB per step)"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        vals = []
+        for i in range(args.warmup + args.steps):
+            cb = cpu_baseline(nsample=args.cpu_sample, scale=args.scale, nsteps_full=args.nsteps)
+            if i >= args.warmup:
+                vals.append(cb["value"])
+        v = float(np.median(vals))
+        line = {"metric": METRIC, "value": v, "unit": "shots/s", "n_gpus": 0, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1e3 * args.shots / v, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+                "config": config, "impl": "reference",
+                "cpu_baseline": dict(cb, value=v),
+                "e2e": {"value": v, "unit": "shots/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        torch.cuda.set_device(local)
+    from pysit_gb300 import workloads
+    from pysit_gb300.autograd import FWIMisfit
+    from pysit_gb300.engine import WavePlan
+
+    # ---- setup (untimed): model, observed data on the true model -------------------
+    m, shots, solver, C, C0 = workloads.cfg2(scale=args.scale, nshots=args.shots, nsteps=args.nsteps,
+                                             shots_per_launch=args.shots_per_launch)
+    solver.model_parameters = solver.ModelParameters(m, {"C": C})
+    ts_obs = solver.ts()
+    fplan = WavePlan(solver, shots, checkpoint_every=solver.checkpoint_every,
+                     shots_per_launch=args.shots_per_launch)
+    obs_dev = fplan.forward().clone()
+    # kernel roofline: the forward step kernel, graph of nsteps launches
+    torch.cuda.synchronize()
+    for _ in range(2):
+        fplan.forward()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    nrep = 3
+    e0.record()
+    for _ in range(nrep):
+        fplan.forward()
+    e1.record()
+    torch.cuda.synchronize()
+    fwd_launch_ms = e0.elapsed_time(e1) / (nrep * solver.nsteps)
+    w = 4
+    full = m.shape(include_bc=True, as_grid=True)
+    n_all = int(np.prod(full))
+    n_int = m.dof()
+    n_pml = n_all - n_int
+    bytes_per_launch = w * (4 * n_int + 8 * n_pml) * fplan.shots_per_launch
+    launches_per_fwd = math.ceil(args.shots / fplan.shots_per_launch)
+    achieved = bytes_per_launch * launches_per_fwd / (fwd_launch_ms * 1e-3) / 1e9
+    fwd_gcells = n_all * args.shots / (fwd_launch_ms * 1e-3) / 1e9
+    del fplan
+    obs_host = obs_dev.cpu().pin_memory()
+    del obs_dev
+    torch.cuda.empty_cache()
+
+    # ---- value: gradient with observed data resident in HBM ----------------------------
+    m0 = solver.ModelParameters(m, {"C": C0})
+    solver.model_parameters = m0
+    from pysit_gb300.autograd import resample_linear
+    plan = WavePlan(solver, shots, checkpoint_every=solver.checkpoint_every, shots_per_launch=args.shots_per_launch)
+    plan.dobs.copy_(resample_linear(obs_host.cuda(), ts_obs, solver.ts()))
+    for _ in range(args.warmup):
+        plan.gradient()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clk = _clock_sampler() if rank == 0 else None
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record()
+    for _ in range(args.steps):
+        plan.gradient()
+    ev1.record()
+    torch.cuda.synchronize()
+    t_grad = ev0.elapsed_time(ev1) / 1e3 / args.steps
+    clocks = _clock_summary(clk, local) if rank == 0 else None
+    launches = plan.launches() * args.steps
+    rn = float(plan.rnorm2.item())
+    del plan
+    torch.cuda.empty_cache()
+    if world > 1:
+        tt = torch.tensor([t_grad], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_grad = float(tt.item())
+
+    # ---- e2e: public autograd API, host inputs each step ----------------------------
+    fwi = FWIMisfit(solver, shots, obs_host, ts_obs, checkpoint_every=solver.checkpoint_every,
+                    shots_per_launch=args.shots_per_launch)
+    C_host = torch.tensor(C0, dtype=torch.float32).pin_memory()
+    for _ in range(max(1, args.warmup)):
+        x = C_host.clone().requires_grad_()
+        fwi(x).backward()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        x = C_host.clone().requires_grad_()
+        J = fwi(x)
+        J.backward()
+        g = x.grad
+        _ = float(J.item())
+    torch.cuda.synchronize()
+    t_e2e = (time.perf_counter() - t0) / args.steps
+    h2d = obs_host.numel() * obs_host.element_size() + C_host.numel() * 4
+    d2h = g.numel() * 4 + 8
+
+    cells_per_grad = 3 * n_all * solver.nsteps * args.shots
+    peak, peak_kind = _peaks()
+    line = {"metric": METRIC, "value": world * args.shots / t_grad, "unit": "shots/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_grad, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, no dataset)",
+            "config": config,
+            "gcell_per_s": world * cells_per_grad / t_grad / 1e9,
+            "e2e": {"value": world * args.shots / t_e2e, "unit": "shots/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h)},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                         "kernel": "wave2d forward step (kFwd)", "bytes_per_launch": bytes_per_launch,
+                         "launch_ms": fwd_launch_ms, "fwd_gcell_per_s": fwd_gcells},
+            "gpu_launches": launches, "misfit_rnorm2": rn, "clocks": clocks}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(nsample=args.cpu_sample, scale=args.scale, nsteps_full=args.nsteps)
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -231,7 +231,7 @@ class _CDATimeScalarCuda:
         p = self.mesh.parameters[axis]
         lp = p.lbc.sigma if p.lbc.type == "pml" else np.array([])
         rp = p.rbc.sigma if p.rbc.type == "pml" else np.array([])
-        return np.asarray(lp, dtype=float), np.asarray(rp, dtype=float)
+        return np.ascontiguousarray(lp, dtype=float), np.ascontiguousarray(rp, dtype=float)
 
     # ---- time axis -----------------------------------------------------------
     def ts(self):

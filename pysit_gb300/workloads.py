@@ -1,0 +1,93 @@
+"""Seeded synthetic workloads with the shapes of the benchmark configurations.
+
+No public dataset is involved: each model is generated from a named seed.
+  cfg2  2D batched FWI gradient: 1152 x 384 cells at 12.5 m + 40-cell PML, order 8,
+        layered model 1500 -> 4500 m/s in 12 layers + Gaussian-smoothed (sigma = 8
+        cells) +-10 % random perturbation clipped to [1500, 5500], 64 surface shots,
+        8 Hz Ricker, 1152 receivers, 4000 steps, checkpoints every 64 steps; the
+        gradient is taken at a Gaussian-smoothed (sigma = 30 cells) start model.
+  cfg3  3D FWI gradient: 400 x 400 x 300 cells at 15 m + 20-cell PML, order 8,
+        layered + smoothed perturbation + Gaussian salt body at 4500 m/s,
+        8 shots, 100 x 100 receivers, 6 Hz, 3000 steps.
+``scale`` shrinks a workload uniformly (cells per axis, shots, steps) for tests.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+from scipy.ndimage import gaussian_filter
+
+from . import core, solvers
+
+__all__ = ["layered_model", "cfg2", "cfg3"]
+
+
+def layered_model(shape, nlayers, vmin, vmax, sigma_cells, amp, seed, clip=(1500.0, 5500.0)):
+    """Layers along z (last axis) plus a smoothed uniform perturbation of relative size `amp`."""
+    rng = np.random.default_rng(seed)
+    nz = shape[-1]
+    layer = np.minimum((np.arange(nz) * nlayers) // nz, nlayers - 1)
+    v1d = vmin + (vmax - vmin) * layer / max(nlayers - 1, 1)
+    C = np.broadcast_to(v1d, shape).astype(float).copy()
+    p = gaussian_filter(rng.uniform(-1.0, 1.0, size=shape), sigma=sigma_cells, mode="nearest")
+    p /= max(np.abs(p).max(), 1e-30)
+    C *= 1.0 + amp * p
+    return np.clip(C, *clip)
+
+
+def _steps_T(C0, deltas, cfl, nsteps):
+    dt = cfl * min(deltas) / float(np.abs(C0).max())
+    return (nsteps - 0.5) * dt
+
+
+def cfg2(scale=1.0, nshots=64, nsteps=4000, order=8, precision="single", cfl=0.4, checkpoint_every=64,
+         shots_per_launch=None, seed=2026):
+    """(mesh, shots, solver, C_true, C_start) of the 2D batched-gradient workload."""
+    nx, nz = max(16, int(round(1152 * scale))), max(12, int(round(384 * scale)))
+    npml = max(4, int(round(40 * scale)))
+    dx = 12.5
+    amp = 3 * 4500.0 * math.log(1e3) / (2 * npml * dx)  # 1e-3 reflection for a quadratic profile
+    pml = core.PML(npml * dx, amp)
+    d = core.RectangularDomain((0.0, (nx - 1) * dx, pml, pml), (0.0, (nz - 1) * dx, pml, pml))
+    m = core.CartesianMesh(d, nx, nz)
+    C = layered_model((nx, nz), 12, 1500.0, 4500.0, 8 * max(scale, 0.125), 0.10, seed)
+    C0 = gaussian_filter(C, sigma=30 * max(scale, 0.05), mode="nearest")
+    T = _steps_T(C0, m.deltas, cfl, nsteps)
+    shots = core.equispaced_acquisition(m, core.RickerWavelet(8.0), sources=nshots, receivers="max",
+                                        source_depth=0.0, receiver_depth=0.0)
+    solver = solvers.ConstantDensityAcousticWave(m, spatial_accuracy_order=order, trange=(0.0, T),
+                                                 kernel_implementation="cuda", precision=precision,
+                                                 cfl_safety=cfl, checkpoint_every=checkpoint_every,
+                                                 shots_per_launch=shots_per_launch)
+    return m, shots, solver, C, C0
+
+
+def cfg3(scale=1.0, nshots=8, nsteps=3000, order=8, precision="single", cfl=0.35, checkpoint_every=None,
+         shots_per_launch=1, seed=2027):
+    """(mesh, shots, solver, C_true, C_start) of the 3D gradient workload."""
+    nx, ny, nz = (max(12, int(round(n * scale))) for n in (400, 400, 300))
+    npml = max(4, int(round(20 * scale)))
+    dx = 15.0
+    amp = 3 * 4500.0 * math.log(1e3) / (2 * npml * dx)
+    pml = core.PML(npml * dx, amp)
+    d = core.RectangularDomain((0.0, (nx - 1) * dx, pml, pml), (0.0, (ny - 1) * dx, pml, pml),
+                               (0.0, (nz - 1) * dx, pml, pml))
+    m = core.CartesianMesh(d, nx, ny, nz)
+    C = layered_model((nx, ny, nz), 12, 1500.0, 4000.0, 8 * max(scale, 0.125), 0.10, seed)
+    x, y, z = m.mesh_coords()
+    cx, cy, cz = (nx - 1) * dx / 2, (ny - 1) * dx / 2, (nz - 1) * dx * 0.55
+    r2 = ((x - cx) ** 2 + (y - cy) ** 2) / (0.15 * nx * dx) ** 2 + (z - cz) ** 2 / (0.12 * nz * dx) ** 2
+    salt = np.exp(-r2) > 0.5
+    C = np.where(salt.reshape(C.shape), 4500.0, C)
+    C0 = gaussian_filter(C, sigma=10 * max(scale, 0.1), mode="nearest")
+    T = _steps_T(C0, m.deltas, cfl, nsteps)
+    nsx = max(1, int(round(math.sqrt(nshots))))
+    shots = core.equispaced_acquisition(m, core.RickerWavelet(6.0), sources=(nsx, max(1, nshots // nsx)),
+                                        receivers=(min(100, nx), min(100, ny)), source_depth=0.0,
+                                        receiver_depth=0.0)
+    solver = solvers.ConstantDensityAcousticWave(m, spatial_accuracy_order=order, trange=(0.0, T),
+                                                 kernel_implementation="cuda", precision=precision,
+                                                 cfl_safety=cfl, checkpoint_every=checkpoint_every,
+                                                 shots_per_launch=shots_per_launch)
+    return m, shots, solver, C, C0
