@@ -225,7 +225,7 @@ __device__ __forceinline__ void sweep2d(const WaveParams<T>& p, const int shot, 
                 vst(p.phx_out + sh + o, pxo);
                 vst(p.phz_out + sh + o, pzo);
             }
-            if (MODE == kRecomp) vst_stream(p.dw_out + sh + o, dwo);
+            if (MODE == kRecomp && p.dw_out) vst_stream(p.dw_out + sh + o, dwo);
             if (MODE == kAdj && p.image) {
                 VReg<T> a = vld(p.ic + sh + o);
 #pragma unroll
