@@ -179,6 +179,10 @@ int pysit_plan_migrate(pysit_plan* plan, const void* operand_dev, double* image_
 /* Misfit only (TemporalLeastSquares.evaluate without the 0.5*dt factor). */
 int pysit_plan_misfit(pysit_plan* plan, const void* dobs_dev, double* rnorm2_dev,
                       void* traces_dev, void* stream);
+/* Reads and clears the plan's device status word (synchronises `stream`):
+ * bit 0 (1) = a bounded wait for a bulk copy expired (results invalid),
+ * bit 1 (2) = a non-finite wavefield value appeared (unstable time step). */
+int pysit_plan_status(pysit_plan* plan, int* flags, void* stream);
 /* Number of kernel launches the last forward/gradient/misfit call issued. */
 int pysit_plan_last_launch_count(const pysit_plan* plan, int64_t* launches);
 

@@ -76,6 +76,7 @@ _PROTOS = {
     "pysit_plan_gradient": (_i, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "pysit_plan_misfit": (_i, [_vp, _vp, _vp, _vp, _vp]),
     "pysit_plan_migrate": (_i, [_vp, _vp, _vp, _vp, _vp]),
+    "pysit_plan_status": (_i, [_vp, C.POINTER(_i), _vp]),
     "pysit_plan_last_launch_count": (_i, [_vp, C.POINTER(C.c_int64)]),
 }
 

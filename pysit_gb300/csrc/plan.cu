@@ -168,6 +168,7 @@ struct pysit_plan {
     virtual int forward(void* traces, cudaStream_t s) = 0;
     virtual int gradient(const void* dobs, double* grad, double* rnorm2, void* traces,
                          cudaStream_t s, bool with_grad, bool migrate) = 0;
+    virtual int status(int* flags, cudaStream_t s) = 0;
     int64_t last_launches = 0;
 };
 
@@ -204,7 +205,7 @@ struct PlanT final : public pysit_plan {
         size_t sbox, srpb, srow, spt, sw;          // source injection
         size_t rbox, rrpb, rrow, rpt, rw;          // receiver injection
         size_t recrow, recoff, recw;               // recording
-        size_t gpad, partial, rnorm;
+        size_t gpad, partial, rnorm, err;
     } off{};
     size_t field_bytes = 0;      // one field for G shots
     int ckpt_fields = 0;         // fields per checkpoint
@@ -270,7 +271,7 @@ struct PlanT final : public pysit_plan {
         hx = dim >= 2 ? kHalo : 0;
         hy = dim == 3 ? kHalo : 0;
         rows_y = ny + 2 * hy;
-        ldz = ((kOZ + nz + kHalo) + 31) / 32 * 32;
+        ldz = ((kOZ + nz + kTailZ) + 31) / 32 * 32;
         fstride = (long long)(nx + 2 * hx) * rows_y * ldz;
         fstride = (fstride + 63) / 64 * 64;
         field_bytes = (size_t)fstride * G * sizeof(T);
@@ -295,8 +296,17 @@ struct PlanT final : public pysit_plan {
         constexpr int V = V16<T>::N;
         const char* e = getenv("PYSIT_CUDA_TILE");  // "bz,tx" override (tuning)
         int ebz = 0, etx = 0;
-        if (e && sscanf(e, "%d,%d", &ebz, &etx) == 2 && ebz >= 32 && ebz <= 256 && ebz % 32 == 0 &&
-            etx >= 1) {
+        bool have = e && sscanf(e, "%d,%d", &ebz, &etx) == 2 && ebz >= 32 && ebz <= 256 && ebz % 32 == 0 &&
+                    etx >= 1;
+        if (dim == 2) {
+            // bulk-copy pipelined sweep: fixed 128-thread blocks, tx rows per block
+            bz = wave2d_threads();
+            tx = have ? etx : 64;
+            ntz = (nz + wave2d_tile_z((int)sizeof(T)) - 1) / wave2d_tile_z((int)sizeof(T));
+            ntx = (nx + tx - 1) / tx;
+            return;
+        }
+        if (have) {
             bz = ebz; tx = etx;
         } else {
             // fewest loaded elements (tile + halo) per useful cell, bz >= 64
@@ -432,6 +442,7 @@ struct PlanT final : public pysit_plan {
         off.recoff = take(std::max<size_t>(rec_off.size(), 1) * sizeof(long long));
         off.recw = take(std::max<size_t>(rec_ws.size(), 1) * sizeof(T));
         off.gpad = take((size_t)nx * ny * nz * sizeof(double));
+        off.err = take(sizeof(int));
         off.partial = take(kRedBlocks * sizeof(double));
         off.rnorm = take(sizeof(double));
         ws_need = tot;
@@ -495,7 +506,19 @@ struct PlanT final : public pysit_plan {
         if ((rc = upload(off.recw, tmp = toT(rec_ws), s))) return rc;
         PGB_CHECK_CUDA(cudaStreamSynchronize(s));
         if (!cap) PGB_CHECK_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+        if (dim == 2) wave2d_prepare();
+        PGB_CHECK_CUDA(cudaGetLastError());
         model_set = false;
+        return PYSIT_OK;
+    }
+
+    int status(int* flags, cudaStream_t s) override {
+        PGB_REQUIRE(ws, "no workspace bound");
+        int v = 0;
+        PGB_CHECK_CUDA(cudaMemcpyAsync(&v, ws + off.err, sizeof(int), cudaMemcpyDeviceToHost, s));
+        PGB_CHECK_CUDA(cudaStreamSynchronize(s));
+        PGB_CHECK_CUDA(cudaMemsetAsync(ws + off.err, 0, sizeof(int), s));
+        *flags = v;
         return PYSIT_OK;
     }
 
@@ -527,6 +550,7 @@ struct PlanT final : public pysit_plan {
         p.idx = T(1.0 / dx); p.idx2 = T(1.0 / (T(dx) * T(dx)));
         p.idy = T(1.0 / dy); p.idy2 = T(1.0 / (T(dy) * T(dy)));
         p.idz = T(1.0 / dz); p.idz2 = T(1.0 / (T(dz) * T(dz)));
+        p.err = ws ? at<int>(off.err) : nullptr;
         (void)g0;
         return p;
     }
@@ -884,6 +908,11 @@ extern "C" int pysit_plan_misfit(pysit_plan* p, const void* dobs, double* rnorm2
                                  void* stream) {
     PGB_REQUIRE(p, "NULL plan");
     return p->gradient(dobs, nullptr, rnorm2, traces, (cudaStream_t)stream, false, false);
+}
+
+extern "C" int pysit_plan_status(pysit_plan* p, int* flags, void* stream) {
+    PGB_REQUIRE(p && flags, "NULL argument");
+    return p->status(flags, (cudaStream_t)stream);
 }
 
 extern "C" int pysit_plan_last_launch_count(const pysit_plan* p, int64_t* n) {

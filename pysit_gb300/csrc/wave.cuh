@@ -16,6 +16,11 @@ namespace pgb {
 
 constexpr int kHalo = 4;  // x/y halo rows and smem z halo (max stencil radius)
 constexpr int kOZ = 4;    // z offset of cell k = 0 inside a row
+constexpr int kTailZ = 12;  // zero cells kept after the last cell of a row (>= halo + vector - 1)
+
+// bits of the device error word of a plan
+#define PGB_ERR_TIMEOUT 1    // a bounded wait for a bulk copy expired
+#define PGB_ERR_NONFINITE 2  // a NaN / Inf wavefield value (unstable time step)
 
 template <typename T> struct V16;
 template <> struct V16<float> { using type = float4; static constexpr int N = 4; };
@@ -131,6 +136,7 @@ struct WaveParams {
     const T* dw_in;          // kAdj: imaging operand of this step
     T* ic;                   // kAdj: imaging accumulator (shot 0 base)
     int image;               // kAdj: accumulate this step
+    int* err;                // device error word (PGB_ERR_* bits), may be NULL
 };
 
 template <typename T, int R, int MODE>
@@ -139,5 +145,9 @@ template <typename T, int R, int MODE>
 void launch_wave3d(const WaveParams<T>& p, int bz, cudaStream_t s);
 template <typename T, int R, int MODE>
 void launch_wave1d(const WaveParams<T>& p, int bz, cudaStream_t s);
+// one-time kernel attributes (large dynamic shared memory); call outside graph capture
+void wave2d_prepare();
+int wave2d_threads();
+int wave2d_tile_z(int dtype_bytes);
 
 }  // namespace pgb

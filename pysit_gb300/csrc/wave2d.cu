@@ -15,18 +15,28 @@
 //   kAdj    the time-reversed adjoint step of adjoint_model (:312-365) with the
 //           zero-lag imaging ic += q_k * dWaveOp_k fused (:329-337).
 //
-// Thread mapping (memory-bound stencil, no tensor cores): a block covers a tile
-// of TZ = blockDim.x * V cells along z (V = 16 bytes of T per thread, vector
-// loads) and sweeps `tx` rows along x.  Each thread keeps the 2R+1 rows of u_k
-// (and of Phi_x in PML tiles) that its x-derivatives need in a register queue;
-// the z-neighbours come from a double-buffered shared-memory copy of the centre
-// row (one __syncthreads per row).  Tiles whose halo does not reach the padding
-// never touch the PML state; in PML tiles the PML state is loaded only for
-// vectors inside the padding (elsewhere it is identically zero).
+// Data movement (HBM-bound stencil, no tensor cores).  A block of 128 threads
+// covers a z-tile of TZ = 128 * V cells (V = 16 bytes of T per thread) and
+// sweeps `tx` rows along x.  Thread 0 streams every row the block needs into
+// shared-memory rings with 1-D bulk copies (cp.async.bulk, "TMA"), D rows ahead
+// of the computation, each stage completing on its own mbarrier:
+//   u_k       ring of 2R + D rows with a 4-cell z-halo (x- and z-stencils)
+//   Phi_x     ring of 2R + D rows, Phi_z one row per stage (PML tiles only, and
+//             only the padding segments of interior rows)
+//   u_{k-1}, C^2, [dWaveOp, ic]   one row per stage
+// The 128 threads read their stencils from shared memory (16-byte vector reads)
+// and write results straight to HBM with 16-byte stores.  One __syncthreads per
+// row releases the ring slots.  Waits are bounded: on expiry the kernel sets the
+// error word and finishes the sweep instead of hanging.
+#include "tma.cuh"
 #include "wave.cuh"
 
 namespace pgb {
 namespace {
+
+constexpr int kNT = 128;          // threads per stencil block
+constexpr int kD = 4;             // rows in flight ahead of the computation
+constexpr uint32_t kWaitPolls = 1u << 22;
 
 template <typename T>
 __device__ __forceinline__ long long foff2(const WaveParams<T>& p, int x, int z) {
@@ -59,204 +69,35 @@ __device__ __forceinline__ void record_block(const WaveParams<T>& p, int rb) {
     p.rec.traces[shot * p.rec.tr_sstride + r] = acc;
 }
 
-template <typename T, int R, int MODE, bool PML>
-__device__ __forceinline__ void sweep2d(const WaveParams<T>& p, const int shot, const int x0,
-                                        const int x1, const int z0, T* __restrict__ smem) {
-    constexpr int V = V16<T>::N;
-    constexpr int H = kHalo;
-    constexpr int HV = H / V;            // halo vectors per side
-    constexpr int NW = (V + 2 * H) / V;  // z-window vectors per thread
-    constexpr int Q = 2 * R + 1;
-    const int t = threadIdx.x;
-    const int TZ = blockDim.x * V;
-    const int SROW = TZ + 2 * H;
-    const int zc = z0 + t * V;
-    const bool zin = zc < p.nz;
-    const long long sh = (long long)shot * p.fstride;
-    const T* __restrict__ ucur = p.u_cur + sh;
-    T* __restrict__ uprev = p.u_prev + sh;
-    const T* __restrict__ phx_in = p.phx_in + sh;
-    const T* __restrict__ phz_in = p.phz_in + sh;
+__host__ __device__ constexpr int round_up(int a, int b) { return (a + b - 1) / b * b; }
 
-    // vectors of this thread that may hold non-zero PML state
-    const bool zpad = PML && (zc < p.pzl || zc + V - 1 >= p.nz - p.pzr);
-    const int* bx = p.inj.box + shot * 6;
-    const bool inj_blk = p.inj.on && bx[0] < x1 && bx[1] > x0 && bx[4] < z0 + TZ && bx[5] > z0;
-
-    // per-thread z-axis data
-    T sgz[V], mgz[V];
-    bool zok[V];
-#pragma unroll
-    for (int v = 0; v < V; ++v) {
-        int z = zc + v;
-        zok[v] = z > 0 && z < p.nz - 1;
-        sgz[v] = (PML && z < p.nz) ? __ldg(p.sgz + z) : T(0);
-        mgz[v] = (PML && MODE == kRecomp && z < p.nz) ? __ldg(p.mgz + z) : T(0);
-    }
-
-    VReg<T> q[Q];
-    VReg<T> qx[PML ? Q : 1];
-#pragma unroll
-    for (int j = 0; j < Q; ++j) {
-        const int x = x0 - R + j;
-        q[j] = zin ? vld_ro(ucur + foff2(p, x, zc)) : vzero<T>();
-        if (PML) {
-            const bool xp = x < p.pxl || x >= p.nx - p.pxr;
-            qx[j] = (zin && (zpad || xp)) ? vld_ro(phx_in + foff2(p, x, zc)) : vzero<T>();
-        }
-    }
-
-    int buf = 0;
-    for (int x = x0; x < x1; ++x) {
-        T* su = smem + buf * SROW;
-        T* sp = smem + (2 + buf) * SROW;
-        const long long o = foff2(p, x, zc);
-        const bool xp = PML && (x < p.pxl || x >= p.nx - p.pxr);
-        const bool padv = PML && zin && (zpad || xp);
-
-        // loads of this row issued before the barrier
-        VReg<T> um = zin ? vld(uprev + o) : vzero<T>();
-        VReg<T> cc = zin ? vld_ro(p.c2 + o) : vzero<T>();
-        VReg<T> pzc = padv ? vld_ro(phz_in + o) : vzero<T>();
-        VReg<T> dwi;
-        if (MODE == kAdj) dwi = (zin && p.image) ? vld_stream(p.dw_in + sh + o) : vzero<T>();
-
-        vst(su + H + t * V, q[R]);
-        if (PML) vst(sp + H + t * V, pzc);
-        if (t < HV) {
-            const int zh = z0 - H + t * V;
-            vst(su + t * V, vld_ro(ucur + foff2(p, x, zh)));
-            if (PML) vst(sp + t * V, vld_ro(phz_in + foff2(p, x, zh)));
-        } else if (t < 2 * HV) {
-            const int zh = z0 + TZ + (t - HV) * V;
-            const bool in = zh < p.nz;
-            vst(su + H + TZ + (t - HV) * V, in ? vld_ro(ucur + foff2(p, x, zh)) : vzero<T>());
-            if (PML) vst(sp + H + TZ + (t - HV) * V, in ? vld_ro(phz_in + foff2(p, x, zh)) : vzero<T>());
-        }
-        __syncthreads();
-
-        T w[NW * V];
-        T wp[PML ? NW * V : 1];
-#pragma unroll
-        for (int i = 0; i < NW; ++i) {
-            VReg<T> r = vld(su + t * V + i * V);
-#pragma unroll
-            for (int v = 0; v < V; ++v) w[i * V + v] = r.v[v];
-            if (PML) {
-                VReg<T> rp = vld(sp + t * V + i * V);
-#pragma unroll
-                for (int v = 0; v < V; ++v) wp[i * V + v] = rp.v[v];
-            }
-        }
-
-        const T sgx = PML ? __ldg(p.sgx + x) : T(0);
-        const T mgx = (PML && MODE == kRecomp) ? __ldg(p.mgx + x) : T(0);
-        const bool xok = x > 0 && x < p.nx - 1;
-        const bool inj_row = inj_blk && x >= bx[0] && x < bx[1];
-
-        VReg<T> un, dwo, pxo, pzo, ico;
-        bool any_pml = false;
-#pragma unroll
-        for (int v = 0; v < V; ++v) {
-            const int z = zc + v;
-            const T uc = q[R].v[v];
-            // second derivatives and first derivatives along z (smem window) and x (queue)
-            T lz = T(d2w(R, 0)) * uc, dz1 = T(0);
-            T lx = T(d2w(R, 0)) * uc, dx1 = T(0);
-#pragma unroll
-            for (int m = 1; m <= R; ++m) {
-                const T zp = w[H + v + m], zm = w[H + v - m];
-                const T xpv = q[R + m].v[v], xmv = q[R - m].v[v];
-                lz += T(d2w(R, m)) * (zp + zm);
-                lx += T(d2w(R, m)) * (xpv + xmv);
-                dz1 += T(d1w(R, m)) * (zp - zm);
-                dx1 += T(d1w(R, m)) * (xpv - xmv);
-            }
-            T F = lx * p.idx2 + lz * p.idz2;
-            if (inj_row && z < p.nz) F += inject_rhs(p.inj, bx, shot, x, z);
-            T sx = T(0), sz = T(0);
-            if (PML) {
-                T dpx = T(0), dpz = T(0);
-#pragma unroll
-                for (int m = 1; m <= R; ++m) {
-                    dpx += T(d1w(R, m)) * (qx[R + m].v[v] - qx[R - m].v[v]);
-                    dpz += T(d1w(R, m)) * (wp[H + v + m] - wp[H + v - m]);
-                }
-                F += dpx * p.idx + dpz * p.idz;
-                sx = sgx;
-                sz = sgz[v];
-            }
-            const T uo = um.v[v];
-            const T c2 = cc.v[v];
-            const bool ok = xok && zok[v];
-            T unew;
-            T ph_x = T(0), ph_z = T(0);
-            if (PML && (sx != T(0) || sz != T(0))) {
-                const T dudx = dx1 * p.idx, dudz = dz1 * p.idz;
-                const T phx = qx[R].v[v], phz = pzc.v[v];
-                ph_x = phx - p.dt * sx * phx + p.dt * (sz - sx) * dudx;
-                ph_z = phz - p.dt * sz * phz + p.dt * (sx - sz) * dudz;
-                const T fac1 = T(2) * p.dt2 / (T(2) + p.dt * (sx + sz));
-                const T fac2 = c2 * F - (uo - T(2) * uc) * p.idt2 + (sx + sz) * uo * p.i2dt -
-                               (sx * sz) * uc;
-                unew = fac1 * fac2;
-                any_pml = true;
-            } else {
-                unew = p.dt2 * c2 * F - (uo - T(2) * uc);
-            }
-            if (!ok) { unew = T(0); ph_x = T(0); ph_z = T(0); }
-            un.v[v] = unew;
-            pxo.v[v] = ph_x;
-            pzo.v[v] = ph_z;
-            if (MODE == kRecomp) {
-                T d = c2 * F;
-                if (PML) {
-                    const T mz = mgz[v];
-                    d += ((mgx + mz) - (sx + sz)) * (unew - uo) * p.i2dt + (mgx * mz - sx * sz) * uc;
-                }
-                dwo.v[v] = ok ? d : T(0);
-            }
-            if (MODE == kAdj) ico.v[v] = uc * dwi.v[v];
-        }
-
-        if (zin) {
-            vst(uprev + o, un);
-            if (PML && padv) {
-                vst(p.phx_out + sh + o, pxo);
-                vst(p.phz_out + sh + o, pzo);
-            }
-            if (MODE == kRecomp && p.dw_out) vst_stream(p.dw_out + sh + o, dwo);
-            if (MODE == kAdj && p.image) {
-                VReg<T> a = vld(p.ic + sh + o);
-#pragma unroll
-                for (int v = 0; v < V; ++v) a.v[v] += ico.v[v];
-                vst(p.ic + sh + o, a);
-            }
-        }
-        (void)any_pml;
-
-        // advance the queues by one row
-#pragma unroll
-        for (int j = 0; j < Q - 1; ++j) {
-            q[j] = q[j + 1];
-            if (PML) qx[j] = qx[j + 1];
-        }
-        if (x + 1 < x1) {
-            const int xn = x + 1 + R;
-            q[Q - 1] = zin ? vld_ro(ucur + foff2(p, xn, zc)) : vzero<T>();
-            if (PML) {
-                const bool xpn = xn < p.pxl || xn >= p.nx - p.pxr;
-                qx[Q - 1] = (zin && (zpad || xpn)) ? vld_ro(phx_in + foff2(p, xn, zc)) : vzero<T>();
-            }
-        }
-        buf ^= 1;
-    }
-}
+// shared-memory carve-up (elements of T after a 128-byte barrier area)
+template <typename T, int R>
+struct Smem2 {
+    static constexpr int V = V16<T>::N;
+    static constexpr int TZ = kNT * V;
+    static constexpr int SROW = TZ + 2 * kHalo;
+    static constexpr int NQ = 2 * R + kD;
+    static constexpr int U = 0;
+    static constexpr int PX = U + NQ * SROW;
+    static constexpr int PZ = PX + NQ * SROW;
+    static constexpr int UP = PZ + kD * SROW;
+    static constexpr int CC = UP + kD * TZ;
+    static constexpr int DW = CC + kD * TZ;
+    static constexpr int IC = DW + kD * TZ;
+    static constexpr int END = IC + kD * TZ;
+    static constexpr size_t bytes = 128 + sizeof(T) * (size_t)END;
+};
 
 template <typename T, int R, int MODE>
-__global__ void __launch_bounds__(256) wave2d_kernel(const WaveParams<T> p) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* smem = reinterpret_cast<T*>(smem_raw);
+__global__ void __launch_bounds__(kNT, 2) wave2d_kernel(const WaveParams<T> p) {
+    using L = Smem2<T, R>;
+    constexpr int V = L::V, H = kHalo, TZ = L::TZ, SROW = L::SROW, NQ = L::NQ;
+    constexpr int NW = (V + 2 * H) / V;  // z-window vectors per thread
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
+    T* S = reinterpret_cast<T*>(smem_raw + 128);
+
     const int ntiles = p.ntz * p.ntx;
     const int b = blockIdx.x;
     if (b >= ntiles * p.nshot) {
@@ -266,31 +107,308 @@ __global__ void __launch_bounds__(256) wave2d_kernel(const WaveParams<T> p) {
     const int shot = b / ntiles;
     const int tile = b - shot * ntiles;
     const int tzi = tile % p.ntz, txi = tile / p.ntz;
-    const int TZ = blockDim.x * V16<T>::N;
     const int z0 = tzi * TZ;
-    const int z1 = min(z0 + TZ, p.nz);
+    const int zlen = min(TZ, p.nz - z0);
     const int x0 = txi * p.tx;
     const int x1 = min(x0 + p.tx, p.nx);
+    const int niter = x1 - x0;
+    const int t = threadIdx.x;
+    const long long sh = (long long)shot * p.fstride;
     const bool pml = (p.pxl > 0 && x0 - R < p.pxl) || (p.pxr > 0 && x1 + R > p.nx - p.pxr) ||
-                     (p.pzl > 0 && z0 - R < p.pzl) || (p.pzr > 0 && z1 + R > p.nz - p.pzr);
-    if (pml)
-        sweep2d<T, R, MODE, true>(p, shot, x0, x1, z0, smem);
-    else
-        sweep2d<T, R, MODE, false>(p, shot, x0, x1, z0, smem);
+                     (p.pzl > 0 && z0 - R < p.pzl) || (p.pzr > 0 && z0 + zlen + R > p.nz - p.pzr);
+    const bool zpad_tile_l = p.pzl > 0 && z0 < p.pzl + H;
+    const bool zpad_tile_r = p.pzr > 0 && z0 + zlen + H > p.nz - p.pzr;
+
+    // ---- rings: zero once (copies never touch cells beyond the tile + halo) ----
+    for (int i = t; i < L::END; i += kNT) S[i] = T(0);
+    if (t == 0) {
+        for (int s = 0; s < kD; ++s) mbar_init(&bar[s], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+
+    auto xpad = [&](int x) { return x < p.pxl || x >= p.nx - p.pxr; };
+    auto qslot = [&](int r) { return (r - x0 + R) % NQ; };
+    const T* ucur = p.u_cur + sh;
+    const T* uprev_g = p.u_prev + sh;
+    const T* phx_g = p.phx_in + sh;
+    const T* phz_g = p.phz_in + sh;
+    const int nfull = round_up(zlen + 2 * H, V);   // halo rows
+    const int nplain = round_up(zlen, V);          // rows without halo
+
+    // copies of one PML-state row (halo layout): whole row in x-padding rows,
+    // otherwise only the z-padding segments (the rest of the slot is never read)
+    auto pml_row = [&](T* dst, const T* src_row_start, bool full, bool count_only, uint32_t& bytes,
+                       uint64_t* br) {
+        auto cp = [&](int j0, int j1) {
+            if (j1 <= j0) return;
+            uint32_t nb = (uint32_t)((j1 - j0) * sizeof(T));
+            bytes += nb;
+            if (!count_only) bulk_g2s(dst + j0, src_row_start + j0, nb, br);
+        };
+        if (full) {
+            cp(0, nfull);
+            return;
+        }
+        int l1 = zpad_tile_l ? min(nfull, round_up(p.pzl - z0 + 2 * H, V)) : 0;
+        int r0 = zpad_tile_r ? max(0, ((p.nz - p.pzr - 2 * H) - (z0 - H)) / V * V) : nfull;
+        if (l1 >= r0) {
+            cp(0, nfull);
+            return;
+        }
+        cp(0, l1);
+        cp(r0, nfull);
+    };
+
+    // all copies of iteration i (row x0 + i); first pass counts bytes
+    auto issue = [&](int i) {
+        const int x = x0 + i;
+        const int s = i % kD;
+        uint64_t* br = &bar[s];
+        for (int pass = 0; pass < 2; ++pass) {
+            const bool count = pass == 0;
+            uint32_t bytes = 0;
+            auto cp = [&](T* dst, const T* src, int n) {
+                uint32_t nb = (uint32_t)(n * sizeof(T));
+                bytes += nb;
+                if (!count) bulk_g2s(dst, src, nb, br);
+            };
+            const int rlo = (i == 0) ? x - R : x + R;
+            for (int r = rlo; r <= x + R; ++r) {
+                cp(S + L::U + qslot(r) * SROW, ucur + foff2(p, r, z0 - H), nfull);
+                if (pml) pml_row(S + L::PX + qslot(r) * SROW, phx_g + foff2(p, r, z0 - H), xpad(r), count, bytes, br);
+            }
+            cp(S + L::UP + s * TZ, uprev_g + foff2(p, x, z0), nplain);
+            cp(S + L::CC + s * TZ, p.c2 + foff2(p, x, z0), nplain);
+            if (pml) pml_row(S + L::PZ + s * SROW, phz_g + foff2(p, x, z0 - H), xpad(x), count, bytes, br);
+            if (MODE == kAdj && p.image) {
+                cp(S + L::DW + s * TZ, p.dw_in + sh + foff2(p, x, z0), nplain);
+                cp(S + L::IC + s * TZ, p.ic + sh + foff2(p, x, z0), nplain);
+            }
+            if (count) mbar_arrive_expect_tx(br, bytes);
+        }
+    };
+
+    if (t == 0) {
+        fence_proxy_async();
+        for (int i = 0; i < min(kD, niter); ++i) issue(i);
+    }
+
+    // ---- per-thread constants ----
+    const int zc = z0 + t * V;
+    const bool zin = zc < p.nz;
+    T sgz[V], mgz[V];
+    bool zok[V], zpe[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+        const int z = zc + v;
+        zok[v] = z > 0 && z < p.nz - 1;
+        zpe[v] = z < p.pzl || z >= p.nz - p.pzr;
+        sgz[v] = (z < p.nz) ? __ldg(p.sgz + z) : T(0);
+        mgz[v] = (MODE == kRecomp && z < p.nz) ? __ldg(p.mgz + z) : T(0);
+    }
+    bool zpw[NW * V];  // z-padding test of each element of the z-window
+#pragma unroll
+    for (int j = 0; j < NW * V; ++j) {
+        const int z = zc - H + j;
+        zpw[j] = z < p.pzl || z >= p.nz - p.pzr;
+    }
+    bool zpad_vec = false;
+#pragma unroll
+    for (int v = 0; v < V; ++v) zpad_vec |= zpe[v];
+    const int* bx = p.inj.box + shot * 6;
+    const bool inj_blk = p.inj.on && bx[0] < x1 && bx[1] > x0 && bx[4] < z0 + zlen && bx[5] > z0;
+    T* uprev_out = p.u_prev + sh;
+    bool bad = false;
+
+    for (int i = 0; i < niter; ++i) {
+        const int x = x0 + i;
+        const int s = i % kD;
+        if (!mbar_wait_bounded(&bar[s], (uint32_t)((i / kD) & 1), kWaitPolls)) {
+            if ((t & 31) == 0 && p.err) atomicOr(p.err, PGB_ERR_TIMEOUT);
+        }
+        const bool xp = xpad(x);
+        const long long o = foff2(p, x, zc);
+        const T* uc_row = S + L::U + qslot(x) * SROW;
+
+        // z-window of u_k (and Phi_z) around this thread's V cells
+        T w[NW * V];
+#pragma unroll
+        for (int j = 0; j < NW; ++j) {
+            VReg<T> r = vld(uc_row + t * V + j * V);
+#pragma unroll
+            for (int v = 0; v < V; ++v) w[j * V + v] = r.v[v];
+        }
+        T xm[R][V], xpv[R][V];
+#pragma unroll
+        for (int m = 1; m <= R; ++m) {
+            VReg<T> a = vld(S + L::U + qslot(x + m) * SROW + H + t * V);
+            VReg<T> c = vld(S + L::U + qslot(x - m) * SROW + H + t * V);
+#pragma unroll
+            for (int v = 0; v < V; ++v) { xpv[m - 1][v] = a.v[v]; xm[m - 1][v] = c.v[v]; }
+        }
+        const VReg<T> um = vld(S + L::UP + s * TZ + t * V);
+        const VReg<T> cc = vld(S + L::CC + s * TZ + t * V);
+        VReg<T> dwi, ici;
+        if (MODE == kAdj && p.image) {
+            dwi = vld(S + L::DW + s * TZ + t * V);
+            ici = vld(S + L::IC + s * TZ + t * V);
+        }
+        const T sgx = __ldg(p.sgx + x);
+        const T mgx = (MODE == kRecomp) ? __ldg(p.mgx + x) : T(0);
+        const bool xok = x > 0 && x < p.nx - 1;
+        const bool inj_row = inj_blk && x >= bx[0] && x < bx[1];
+
+        VReg<T> un, dwo, pxo, pzo;
+        if (pml) {
+            // PML state taps: rows / elements outside the padding are zero
+            T px_c[V], pz_c[V], dpx[V], dpz[V];
+            T wp[NW * V];
+            const T* pz_row = S + L::PZ + s * SROW;
+#pragma unroll
+            for (int j = 0; j < NW; ++j) {
+                VReg<T> r = vld(pz_row + t * V + j * V);
+#pragma unroll
+                for (int v = 0; v < V; ++v) wp[j * V + v] = (xp || zpw[j * V + v]) ? r.v[v] : T(0);
+            }
+            {
+                VReg<T> r = vld(S + L::PX + qslot(x) * SROW + H + t * V);
+#pragma unroll
+                for (int v = 0; v < V; ++v) {
+                    px_c[v] = (xp || zpe[v]) ? r.v[v] : T(0);
+                    pz_c[v] = wp[H + v];
+                    dpx[v] = T(0);
+                    dpz[v] = T(0);
+                }
+            }
+#pragma unroll
+            for (int m = 1; m <= R; ++m) {
+                const bool xpp = xpad(x + m), xpm = xpad(x - m);
+                VReg<T> a = vld(S + L::PX + qslot(x + m) * SROW + H + t * V);
+                VReg<T> c = vld(S + L::PX + qslot(x - m) * SROW + H + t * V);
+#pragma unroll
+                for (int v = 0; v < V; ++v) {
+                    const T ap = (xpp || zpe[v]) ? a.v[v] : T(0);
+                    const T am = (xpm || zpe[v]) ? c.v[v] : T(0);
+                    dpx[v] += T(d1w(R, m)) * (ap - am);
+                    dpz[v] += T(d1w(R, m)) * (wp[H + v + m] - wp[H + v - m]);
+                }
+            }
+#pragma unroll
+            for (int v = 0; v < V; ++v) {
+                const int z = zc + v;
+                const T uc = w[H + v];
+                T lz = T(d2w(R, 0)) * uc, lx = T(d2w(R, 0)) * uc, dz1 = T(0), dx1 = T(0);
+#pragma unroll
+                for (int m = 1; m <= R; ++m) {
+                    lz += T(d2w(R, m)) * (w[H + v + m] + w[H + v - m]);
+                    lx += T(d2w(R, m)) * (xpv[m - 1][v] + xm[m - 1][v]);
+                    dz1 += T(d1w(R, m)) * (w[H + v + m] - w[H + v - m]);
+                    dx1 += T(d1w(R, m)) * (xpv[m - 1][v] - xm[m - 1][v]);
+                }
+                T F = lx * p.idx2 + lz * p.idz2 + dpx[v] * p.idx + dpz[v] * p.idz;
+                if (inj_row && z < p.nz) F += inject_rhs(p.inj, bx, shot, x, z);
+                const T sx = sgx, sz = sgz[v];
+                const T uo = um.v[v], c2 = cc.v[v];
+                const bool ok = xok && zok[v];
+                T unew, ph_x = T(0), ph_z = T(0);
+                if (sx != T(0) || sz != T(0)) {
+                    const T dudx = dx1 * p.idx, dudz = dz1 * p.idz;
+                    ph_x = px_c[v] - p.dt * sx * px_c[v] + p.dt * (sz - sx) * dudx;
+                    ph_z = pz_c[v] - p.dt * sz * pz_c[v] + p.dt * (sx - sz) * dudz;
+                    const T fac1 = T(2) * p.dt2 / (T(2) + p.dt * (sx + sz));
+                    const T fac2 = c2 * F - (uo - T(2) * uc) * p.idt2 + (sx + sz) * uo * p.i2dt - (sx * sz) * uc;
+                    unew = fac1 * fac2;
+                } else {
+                    unew = p.dt2 * c2 * F - (uo - T(2) * uc);
+                }
+                if (!ok) { unew = T(0); ph_x = T(0); ph_z = T(0); }
+                un.v[v] = unew;
+                pxo.v[v] = ph_x;
+                pzo.v[v] = ph_z;
+                if (MODE == kRecomp) {
+                    const T mz = mgz[v];
+                    T d = c2 * F + ((mgx + mz) - (sx + sz)) * (unew - uo) * p.i2dt + (mgx * mz - sx * sz) * uc;
+                    dwo.v[v] = ok ? d : T(0);
+                }
+            }
+        } else {
+#pragma unroll
+            for (int v = 0; v < V; ++v) {
+                const int z = zc + v;
+                const T uc = w[H + v];
+                T lz = T(d2w(R, 0)) * uc, lx = T(d2w(R, 0)) * uc;
+#pragma unroll
+                for (int m = 1; m <= R; ++m) {
+                    lz += T(d2w(R, m)) * (w[H + v + m] + w[H + v - m]);
+                    lx += T(d2w(R, m)) * (xpv[m - 1][v] + xm[m - 1][v]);
+                }
+                T F = lx * p.idx2 + lz * p.idz2;
+                if (inj_row && z < p.nz) F += inject_rhs(p.inj, bx, shot, x, z);
+                const T c2 = cc.v[v];
+                const bool ok = xok && zok[v];
+                T unew = p.dt2 * c2 * F - (um.v[v] - T(2) * uc);
+                un.v[v] = ok ? unew : T(0);
+                if (MODE == kRecomp) dwo.v[v] = ok ? c2 * F : T(0);
+            }
+        }
+
+        if (MODE == kFwd) {
+#pragma unroll
+            for (int v = 0; v < V; ++v) bad |= !isfinite(un.v[v]);
+        }
+        if (zin) {
+            vst(uprev_out + o, un);
+            if (pml && (xp || zpad_vec)) {
+                vst(p.phx_out + sh + o, pxo);
+                vst(p.phz_out + sh + o, pzo);
+            }
+            if (MODE == kRecomp && p.dw_out) vst_stream(p.dw_out + sh + o, dwo);
+            if (MODE == kAdj && p.image) {
+                VReg<T> a;
+#pragma unroll
+                for (int v = 0; v < V; ++v) a.v[v] = ici.v[v] + w[H + v] * dwi.v[v];
+                vst(p.ic + sh + o, a);
+            }
+        }
+        __syncthreads();  // every thread is done with row x's slots
+        if (t == 0 && i + kD < niter) {
+            fence_proxy_async();
+            issue(i + kD);
+        }
+    }
+    if (MODE == kFwd && bad && p.err) atomicOr(p.err, PGB_ERR_NONFINITE);
 }
 
 }  // namespace
 
 template <typename T, int R, int MODE>
 void launch_wave2d(const WaveParams<T>& p, int bz, cudaStream_t s) {
+    (void)bz;
     const int ntiles = p.ntz * p.ntx;
     int grid = ntiles * p.nshot + (MODE == kFwd ? p.rec.blocks : 0);
-    const int srow = bz * V16<T>::N + 2 * kHalo;
-    size_t smem = 4 * srow * sizeof(T);
-    wave2d_kernel<T, R, MODE><<<grid, bz, smem, s>>>(p);
+    wave2d_kernel<T, R, MODE><<<grid, kNT, Smem2<T, R>::bytes, s>>>(p);
 }
 
-#define PGB_INST2D(T, R)                                                    \
+template <typename T, int R>
+static void prep_one() {
+    cudaFuncSetAttribute(wave2d_kernel<T, R, kFwd>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)Smem2<T, R>::bytes);
+    cudaFuncSetAttribute(wave2d_kernel<T, R, kRecomp>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)Smem2<T, R>::bytes);
+    cudaFuncSetAttribute(wave2d_kernel<T, R, kAdj>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)Smem2<T, R>::bytes);
+}
+
+void wave2d_prepare() {
+    prep_one<float, 1>(); prep_one<float, 2>(); prep_one<float, 3>(); prep_one<float, 4>();
+    prep_one<double, 1>(); prep_one<double, 2>(); prep_one<double, 3>(); prep_one<double, 4>();
+}
+
+int wave2d_threads() { return kNT; }
+int wave2d_tile_z(int dtype_bytes) { return kNT * (16 / dtype_bytes); }
+
+#define PGB_INST2D(T, R)                                                                 \
     template void launch_wave2d<T, R, kFwd>(const WaveParams<T>&, int, cudaStream_t);    \
     template void launch_wave2d<T, R, kRecomp>(const WaveParams<T>&, int, cudaStream_t); \
     template void launch_wave2d<T, R, kAdj>(const WaveParams<T>&, int, cudaStream_t);
