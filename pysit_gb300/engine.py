@@ -219,6 +219,21 @@ class WavePlan:
             C.c_void_p(_native.stream_handle())))
         return self.grad, self.rnorm2
 
+    def migrate(self, operand):
+        """F* of a data-space operand [nshots, nsteps, nrec] summed over shots (unpadded, FP64)."""
+        self.set_model()
+        self.dobs.copy_(operand)
+        _native.check(_native.load().pysit_plan_migrate(
+            self._h, C.c_void_p(self.dobs.data_ptr()), C.c_void_p(self.grad.data_ptr()),
+            C.c_void_p(self.rnorm2.data_ptr()), C.c_void_p(_native.stream_handle())))
+        return self.grad
+
+    def status(self):
+        """Device status flags (1: bulk-copy wait expired, 2: non-finite wavefield); clears them."""
+        f = C.c_int()
+        _native.check(_native.load().pysit_plan_status(self._h, C.byref(f), C.c_void_p(_native.stream_handle())))
+        return int(f.value)
+
     def misfit(self, with_traces=False):
         self.set_model()
         _native.check(_native.load().pysit_plan_misfit(

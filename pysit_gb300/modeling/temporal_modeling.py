@@ -138,14 +138,8 @@ class TemporalModeling:
             plan = plan_for(solver, [shot], imaging_period)
             op = np.zeros((1, solver.nsteps, plan.nrec))
             op[0, :, :shot.receivers.receiver_count] = np.asarray(operand_simdata)
-            plan.dobs.copy_(torch.as_tensor(op, dtype=plan.tdtype))
-            lib = _native.load()
-            import ctypes as C
-            _native.check(lib.pysit_plan_migrate(plan._h, C.c_void_p(plan.dobs.data_ptr()),
-                                                 C.c_void_p(plan.grad.data_ptr()),
-                                                 C.c_void_p(plan.rnorm2.data_ptr()),
-                                                 C.c_void_p(_native.stream_handle())))
-            return m0.perturbation(data=plan.grad.cpu().numpy().reshape(-1, 1))
+            img = plan.migrate(torch.as_tensor(op, dtype=plan.tdtype, device="cuda"))
+            return m0.perturbation(data=img.cpu().numpy().reshape(-1, 1))
         if dWaveOp is None:
             dWaveOp = self._forward_plain(shot, imaging_period, {"dWaveOp"}, device_outputs=True)["dWaveOp"]
         rp = ["imaging_condition"]

@@ -161,3 +161,20 @@ def test_plan_reports_its_kernel_launches(golden):
     obj.compute_gradient(shots, solver.ModelParameters(m, {"C": C0}))
     n = obj.last_plan.launches()
     assert n >= 3 * solver.nsteps
+
+
+def test_status_word_clear_after_stable_run_and_flags_instability():
+    from pysit_gb300.engine import WavePlan
+    m, shots, solver, C, C0 = problems.build(api, "o6")
+    solver.model_parameters = solver.ModelParameters(m, {"C": C})
+    plan = WavePlan(solver, shots)
+    plan.forward()
+    assert plan.status() == 0
+    # far beyond the leapfrog stability limit: the forward sweep reports non-finite values
+    m, shots, solver, C, C0 = problems.build(api, "o6")
+    solver.cfl_safety = 3.0
+    solver.model_parameters = solver.ModelParameters(m, {"C": C})
+    plan = WavePlan(solver, shots)
+    plan.forward()
+    assert plan.status() & 2
+    assert plan.status() == 0  # reading clears the word
