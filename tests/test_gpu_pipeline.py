@@ -170,9 +170,12 @@ def test_status_word_clear_after_stable_run_and_flags_instability():
     plan = WavePlan(solver, shots)
     plan.forward()
     assert plan.status() == 0
-    # far beyond the leapfrog stability limit: the forward sweep reports non-finite values
+    # far beyond the leapfrog stability limit: after enough steps the wavefield
+    # overflows and the forward sweep reports non-finite values
     m, shots, solver, C, C0 = problems.build(api, "o6")
     solver.cfl_safety = 3.0
+    solver.trange = (0.0, 30.0)
+    solver.t0, solver.tf = solver.trange
     solver.model_parameters = solver.ModelParameters(m, {"C": C})
     plan = WavePlan(solver, shots)
     plan.forward()

@@ -92,8 +92,12 @@ def test_dwaveop_matches_oracle(dim, shape):
     ref = pipeline.dwaveop(P, um, uc, up, psi if dim == 3 else None)
     t = lambda a: torch.as_tensor(a, device="cuda")  # noqa: E731
     out = torch.zeros(n, dtype=torch.float64, device="cuda")
-    dims = {1: (1, 1, shape[0]), 2: (shape[0], 1, shape[1]), 3: tuple(shape)}[dim]
-    sg = {1: (None, None, t(maps[0])), 2: (t(maps[0]), None, t(maps[1])), 3: tuple(t(m) for m in maps)}[dim]
+    if dim == 1:
+        dims, sg = (1, 1, shape[0]), (None, None, t(maps[0]))
+    elif dim == 2:
+        dims, sg = (shape[0], 1, shape[1]), (t(maps[0]), None, t(maps[1]))
+    else:
+        dims, sg = tuple(shape), tuple(t(m) for m in maps)
     ptr = lambda x: None if x is None else C.c_void_p(x.data_ptr())  # noqa: E731
     tensors = [t(um), t(uc), t(up), t(psi)]
     _native.check(_native.load().pysit_cda_dwaveop(_native.PYSIT_F64, dim, *[ptr(x) for x in tensors[:3]],
