@@ -188,6 +188,8 @@ struct PlanT final : public pysit_plan {
     long long fstride;  // elements per field per shot (256-byte multiple)
     int bz, tx, ntz, ntx;
     int nseg;
+    bool warp2d = true;          // 2D: warp-task sweep (true) or bulk-copy row pipeline (false)
+    std::vector<int> tasks2d;    // [ntasks][5] warp tasks of the 2D sweep
     // ---- acquisition (host) ----------------------------------------------------
     std::vector<CSRBox> src_inj, rec_inj;
     std::vector<int> rec_rows;        // [nshots*nrec+1]
@@ -205,7 +207,7 @@ struct PlanT final : public pysit_plan {
         size_t sbox, srpb, srow, spt, sw;          // source injection
         size_t rbox, rrpb, rrow, rpt, rw;          // receiver injection
         size_t recrow, recoff, recw;               // recording
-        size_t gpad, partial, rnorm, err;
+        size_t gpad, partial, rnorm, err, tasks;
     } off{};
     size_t field_bytes = 0;      // one field for G shots
     int ckpt_fields = 0;         // fields per checkpoint
@@ -299,6 +301,15 @@ struct PlanT final : public pysit_plan {
         bool have = e && sscanf(e, "%d,%d", &ebz, &etx) == 2 && ebz >= 32 && ebz <= 256 && ebz % 32 == 0 &&
                     etx >= 1;
         if (dim == 2) {
+            const char* k = getenv("PYSIT_CUDA_2D");  // "tma" selects the bulk-copy pipeline
+            warp2d = !(k && strcmp(k, "tma") == 0);
+            if (warp2d) {
+                bz = wave2d_warp_threads();
+                tx = have ? etx : 32;
+                build_tasks2d();
+                ntz = ntx = 1;
+                return;
+            }
             // bulk-copy pipelined sweep: fixed 128-thread blocks, tx rows per block
             bz = wave2d_threads();
             tx = have ? etx : 64;
@@ -320,6 +331,42 @@ struct PlanT final : public pysit_plan {
         }
         ntz = (nz + bz * V - 1) / (bz * V);
         ntx = (nx + tx - 1) / tx;
+    }
+
+    // Warp tasks covering the padded grid once.  Interior (kind 0): cells at least
+    // R away from the padding; PML shell (kind 1): the rest.  z boundaries are
+    // multiples of 4 cells (vectors never straddle two tasks) except the grid end.
+    void split(int a, int b, int w, std::vector<std::pair<int, int>>& out) const {
+        if (b <= a) return;
+        int n = (b - a + w - 1) / w;
+        int width = ((b - a + n - 1) / n + 3) / 4 * 4;
+        for (int z = a; z < b; z += width) out.push_back({z, std::min(b, z + width)});
+    }
+    void add_tasks(int xa, int xb, int za, int zb, int kind) {
+        if (xb <= xa || zb <= za) return;
+        std::vector<std::pair<int, int>> zs;
+        split(za, zb, wave2d_warp_seg((int)sizeof(T), order, kind), zs);
+        for (int x = xa; x < xb; x += tx)
+            for (auto& z : zs) {
+                int t[5] = {x, std::min(xb, x + tx), z.first, z.second, kind};
+                tasks2d.insert(tasks2d.end(), t, t + 5);
+            }
+    }
+    void build_tasks2d() {
+        tasks2d.clear();
+        const int xa = pl[0] > 0 ? pl[0] + R : 0;
+        const int xb = pr[0] > 0 ? nx - pr[0] - R : nx;
+        int za = pl[2] > 0 ? (pl[2] + R + 3) / 4 * 4 : 0;
+        int zb = pr[2] > 0 ? (nz - pr[2] - R) / 4 * 4 : nz;
+        if (xa >= xb || za >= zb) {  // no interior: the whole grid is shell
+            add_tasks(0, nx, 0, nz, 1);
+            return;
+        }
+        add_tasks(xa, xb, za, zb, 0);   // interior
+        add_tasks(0, xa, 0, nz, 1);     // low-x band
+        add_tasks(xb, nx, 0, nz, 1);    // high-x band
+        add_tasks(xa, xb, 0, za, 1);    // low-z band
+        add_tasks(xa, xb, zb, nz, 1);   // high-z band
     }
 
     long long internal_offset(long long cell) const {
@@ -443,6 +490,7 @@ struct PlanT final : public pysit_plan {
         off.recw = take(std::max<size_t>(rec_ws.size(), 1) * sizeof(T));
         off.gpad = take((size_t)nx * ny * nz * sizeof(double));
         off.err = take(sizeof(int));
+        off.tasks = take(std::max<size_t>(tasks2d.size(), 1) * sizeof(int));
         off.partial = take(kRedBlocks * sizeof(double));
         off.rnorm = take(sizeof(double));
         ws_need = tot;
@@ -504,6 +552,7 @@ struct PlanT final : public pysit_plan {
         if ((rc = upload_inj(rec_inj, off.rbox, off.rrpb, off.rrow, off.rpt, off.rw, s))) return rc;
         if ((rc = upload(off.recrow, rec_rows, s)) || (rc = upload(off.recoff, rec_off, s))) return rc;
         if ((rc = upload(off.recw, tmp = toT(rec_ws), s))) return rc;
+        if ((rc = upload(off.tasks, tasks2d, s))) return rc;
         PGB_CHECK_CUDA(cudaStreamSynchronize(s));
         if (!cap) PGB_CHECK_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
         if (dim == 2) wave2d_prepare();
@@ -582,7 +631,13 @@ struct PlanT final : public pysit_plan {
         ++launches;
 #define PGB_L(RR)                                                              \
     do {                                                                       \
-        if (dim == 2) {                                                        \
+        if (dim == 2 && warp2d) {                                              \
+            const int* tk = at<int>(off.tasks);                                \
+            const int nt = (int)(tasks2d.size() / 5);                          \
+            if (mode == kFwd) launch_wave2d_warp_tasks<T, RR, kFwd>(p, tk, nt, s);            \
+            else if (mode == kRecomp) launch_wave2d_warp_tasks<T, RR, kRecomp>(p, tk, nt, s); \
+            else launch_wave2d_warp_tasks<T, RR, kAdj>(p, tk, nt, s);                         \
+        } else if (dim == 2) {                                                 \
             if (mode == kFwd) launch_wave2d<T, RR, kFwd>(p, bz, s);            \
             else if (mode == kRecomp) launch_wave2d<T, RR, kRecomp>(p, bz, s); \
             else launch_wave2d<T, RR, kAdj>(p, bz, s);                         \

@@ -139,8 +139,48 @@ struct WaveParams {
     int* err;                // device error word (PGB_ERR_* bits), may be NULL
 };
 
+// ---- helpers shared by the 2D kernels ---------------------------------------
+template <typename T>
+__device__ __forceinline__ long long foff2(const WaveParams<T>& p, int x, int z) {
+    return (long long)(x + kHalo) * p.ldz + kOZ + z;
+}
+
+// rhs of one cell from the injection operator of its shot
+template <typename T>
+__device__ __forceinline__ T inject_rhs(const Inject<T>& inj, const int* bx, int shot, int x, int z) {
+    if (x < bx[0] || x >= bx[1] || z < bx[4] || z >= bx[5]) return T(0);
+    int c = (x - bx[0]) * (bx[5] - bx[4]) + (z - bx[4]);
+    const int* rp = inj.rowptr + inj.rpbase[shot];
+    int e0 = __ldg(rp + c), e1 = __ldg(rp + c + 1);
+    const T* amp = inj.amp + shot * inj.amp_sstride;
+    T acc = T(0);
+    for (int e = e0; e < e1; ++e) acc += __ldg(inj.w + e) * __ldg(amp + __ldg(inj.pt + e));
+    return acc;
+}
+
+// trace recorder block: one thread per (shot, receiver), taps summed in order
+template <typename T>
+__device__ __forceinline__ void record_block(const WaveParams<T>& p, int rb) {
+    int id = rb * blockDim.x + threadIdx.x;
+    int total = p.nshot * p.rec.nrec;
+    if (id >= total) return;
+    int shot = id / p.rec.nrec, r = id - shot * p.rec.nrec;
+    int e0 = __ldg(p.rec.rowptr + id), e1 = __ldg(p.rec.rowptr + id + 1);
+    const T* u = p.u_cur + (long long)shot * p.fstride;
+    T acc = T(0);
+    for (int e = e0; e < e1; ++e) acc += __ldg(p.rec.w + e) * u[__ldg(p.rec.off + e)];
+    p.rec.traces[shot * p.rec.tr_sstride + r] = acc;
+}
+
 template <typename T, int R, int MODE>
 void launch_wave2d(const WaveParams<T>& p, int bz, cudaStream_t s);
+// warp-independent 2D sweep (shuffles for the z-halo, register queue along x);
+// tasks = [ntasks][5] ints (x0, x1, zs, ze, kind), shared by all shots
+template <typename T, int R, int MODE>
+void launch_wave2d_warp_tasks(const WaveParams<T>& p, const int* tasks, int ntasks, cudaStream_t s);
+int wave2d_warp_threads();
+int wave2d_warp_seg(int dtype_bytes, int order, int pml);
+int wave2d_warp_vec(int dtype_bytes, int pml);
 template <typename T, int R, int MODE>
 void launch_wave3d(const WaveParams<T>& p, int bz, cudaStream_t s);
 template <typename T, int R, int MODE>

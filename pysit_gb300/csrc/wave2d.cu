@@ -38,37 +38,6 @@ constexpr int kNT = 128;          // threads per stencil block
 constexpr int kD = 4;             // rows in flight ahead of the computation
 constexpr uint32_t kWaitPolls = 1u << 22;
 
-template <typename T>
-__device__ __forceinline__ long long foff2(const WaveParams<T>& p, int x, int z) {
-    return (long long)(x + kHalo) * p.ldz + kOZ + z;
-}
-
-template <typename T>
-__device__ __forceinline__ T inject_rhs(const Inject<T>& inj, const int* bx, int shot, int x,
-                                        int z) {
-    if (x < bx[0] || x >= bx[1] || z < bx[4] || z >= bx[5]) return T(0);
-    int c = (x - bx[0]) * (bx[5] - bx[4]) + (z - bx[4]);
-    const int* rp = inj.rowptr + inj.rpbase[shot];
-    int e0 = __ldg(rp + c), e1 = __ldg(rp + c + 1);
-    const T* amp = inj.amp + shot * inj.amp_sstride;
-    T acc = T(0);
-    for (int e = e0; e < e1; ++e) acc += __ldg(inj.w + e) * __ldg(amp + __ldg(inj.pt + e));
-    return acc;
-}
-
-template <typename T>
-__device__ __forceinline__ void record_block(const WaveParams<T>& p, int rb) {
-    int id = rb * blockDim.x + threadIdx.x;
-    int total = p.nshot * p.rec.nrec;
-    if (id >= total) return;
-    int shot = id / p.rec.nrec, r = id - shot * p.rec.nrec;
-    int e0 = __ldg(p.rec.rowptr + id), e1 = __ldg(p.rec.rowptr + id + 1);
-    const T* u = p.u_cur + (long long)shot * p.fstride;
-    T acc = T(0);
-    for (int e = e0; e < e1; ++e) acc += __ldg(p.rec.w + e) * u[__ldg(p.rec.off + e)];
-    p.rec.traces[shot * p.rec.tr_sstride + r] = acc;
-}
-
 __host__ __device__ constexpr int round_up(int a, int b) { return (a + b - 1) / b * b; }
 
 // shared-memory carve-up (elements of T after a 128-byte barrier area)
