@@ -555,7 +555,7 @@ struct PlanT final : public pysit_plan {
         if ((rc = upload(off.tasks, tasks2d, s))) return rc;
         PGB_CHECK_CUDA(cudaStreamSynchronize(s));
         if (!cap) PGB_CHECK_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
-        if (dim == 2) wave2d_prepare();
+        if (dim == 2) { wave2d_prepare(); wave2d_warp_prepare(); }
         PGB_CHECK_CUDA(cudaGetLastError());
         model_set = false;
         return PYSIT_OK;

@@ -180,7 +180,7 @@ template <typename T, int R, int MODE>
 void launch_wave2d_warp_tasks(const WaveParams<T>& p, const int* tasks, int ntasks, cudaStream_t s);
 int wave2d_warp_threads();
 int wave2d_warp_seg(int dtype_bytes, int order, int pml);
-int wave2d_warp_vec(int dtype_bytes, int pml);
+void wave2d_warp_prepare();
 template <typename T, int R, int MODE>
 void launch_wave3d(const WaveParams<T>& p, int bz, cudaStream_t s);
 template <typename T, int R, int MODE>

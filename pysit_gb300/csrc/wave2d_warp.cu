@@ -2,30 +2,41 @@
 //
 // Same maths as the reference step cda_time_scalar_2D (pysit/solvers/
 // constant_density_acoustic/time/scalar/constant_density_acoustic_time_scalar_2D.h:88-179)
-// with the mode-specific fusions described in wave2d.cu (trace recording,
-// dWaveOp from the stencil bracket, adjoint imaging).
+// with the fusions of the batched pipeline:
+//   kFwd    trace recording of u_k (appended recorder blocks, receivers.py:462-510);
+//   kRecomp the imaging operand dWaveOp_k (constant_density_acoustic_base.py:24-40)
+//           from the stencil's own bracket F: C^2 F where the step and mesh
+//           sigmas agree, plus the sigma differences elsewhere (the right PML,
+//           whose step profile is read one node further out, _2D.h:143-157);
+//   kAdj    the time-reversed adjoint step with ic += q_k * dWaveOp_k fused
+//           (temporal_modeling.py:312-365).
 //
 // Work decomposition: a table of warp tasks (x0, x1, zs, ze, kind) covers the
-// padded grid once; the same table serves every shot.  A warp owns the cells
-// z in [zs, ze) and sweeps rows x0..x1-1.  Its lanes hold VV consecutive cells
-// each; the HL lanes at each end only load the z-halo.  Per row a lane
-//   * keeps the 2R+1 rows of u_k its x-derivatives need in a register queue,
-//   * gets its z-neighbours from the adjacent lanes with warp shuffles,
-//   * prefetches the next row (u_k head, u_{k-1}, C^2, [dWaveOp, ic]) before
-//     computing the current one, so loads overlap arithmetic,
-// with no shared memory and no block barrier: warps never wait for each other.
-// Two task kinds, selected per warp (warp-uniform branch):
-//   kind 0  interior: cells at least R away from the padding; 16-byte vectors,
-//           no PML state at all;
-//   kind 1  PML shell: the padding and its R-wide rim; 8-byte vectors (half the
-//           register queue), Phi_x in a register queue, Phi_z by shuffles, PML
-//           state loaded only for vectors inside the padding.
+// padded grid once and serves every shot.  A warp owns cells z in [zs, ze) and
+// sweeps rows x0..x1-1.  Lanes hold VV consecutive cells; the HL lanes at each
+// end only carry the z-halo.  Per row:
+//   * lane 0 streams the rows the warp needs D iterations ahead into the warp's
+//     own shared-memory ring with 1-D bulk copies (cp.async.bulk), one mbarrier
+//     per stage; every lane reads its 16-byte vector back (no global-load latency
+//     on the critical path, no block barrier, warps never wait for each other);
+//   * the 2R+1 rows of u_k the x-derivatives need live in a register queue that
+//     rotates by renaming (the row loop is unrolled by 2R+1);
+//   * z-neighbours come from the adjacent lanes with warp shuffles.
+// Task kinds (warp-uniform branch):
+//   kind 0  interior: at least R cells away from the padding, 16-byte vectors,
+//           no PML state;
+//   kind 1  PML shell: the padding and its R-wide rim, 8-byte vectors, Phi_x in a
+//           register queue, Phi_z through shuffles.
+// Waits are bounded: on expiry the kernel sets the plan's error word and goes on.
+#include "tma.cuh"
 #include "wave.cuh"
 
 namespace pgb {
 namespace {
 
-constexpr int kWarps = 4;  // warps per block
+constexpr int kWarps = 4;   // warps per block
+constexpr int kStages = 3;  // rows in flight ahead of the computation
+constexpr uint32_t kPolls = 1u << 22;
 
 template <typename T, int N> struct VecT;
 template <> struct VecT<float, 4> { using type = float4; };
@@ -38,42 +49,48 @@ template <typename T, int N>
 struct alignas(sizeof(T) * N) Vec {
     T v[N];
 };
-
 template <typename T, int N>
-__device__ __forceinline__ Vec<T, N> zvec() {
-    Vec<T, N> r;
-#pragma unroll
-    for (int i = 0; i < N; ++i) r.v[i] = T(0);
-    return r;
-}
-template <typename T, int N>
-__device__ __forceinline__ Vec<T, N> ldv(const T* p) {
+__device__ __forceinline__ Vec<T, N> lds(const T* p) {
     Vec<T, N> r;
     *reinterpret_cast<typename VecT<T, N>::type*>(r.v) = *reinterpret_cast<const typename VecT<T, N>::type*>(p);
     return r;
 }
 template <typename T, int N>
-__device__ __forceinline__ Vec<T, N> ldv_ro(const T* p) {
-    Vec<T, N> r;
-    *reinterpret_cast<typename VecT<T, N>::type*>(r.v) = __ldg(reinterpret_cast<const typename VecT<T, N>::type*>(p));
-    return r;
-}
-template <typename T, int N>
-__device__ __forceinline__ Vec<T, N> ldv_cs(const T* p) {
-    Vec<T, N> r;
-    *reinterpret_cast<typename VecT<T, N>::type*>(r.v) = __ldcs(reinterpret_cast<const typename VecT<T, N>::type*>(p));
-    return r;
-}
-template <typename T, int N>
-__device__ __forceinline__ void stv(T* p, const Vec<T, N>& r) {
+__device__ __forceinline__ void stg(T* p, const Vec<T, N>& r) {
     *reinterpret_cast<typename VecT<T, N>::type*>(p) = *reinterpret_cast<const typename VecT<T, N>::type*>(r.v);
 }
 template <typename T, int N>
-__device__ __forceinline__ void stv_cs(T* p, const Vec<T, N>& r) {
+__device__ __forceinline__ void stg_cs(T* p, const Vec<T, N>& r) {
     __stcs(reinterpret_cast<typename VecT<T, N>::type*>(p), *reinterpret_cast<const typename VecT<T, N>::type*>(r.v));
 }
 
-// window of the row held by lanes lane-HL .. lane+HL (HL*VV cells of halo per side)
+// per-kind geometry
+template <typename T, int R, int KIND>
+struct Geo {
+    static constexpr int V = V16<T>::N;
+    static constexpr int VV = KIND == 0 ? V : (V > 1 ? V / 2 : 1);
+    // halo lanes per side: enough for R cells, and a whole number of 16-byte
+    // vectors so every bulk copy starts 16-byte aligned
+    static constexpr int A = V / VV;
+    static constexpr int HL = ((R + VV - 1) / VV + A - 1) / A * A;
+    static constexpr int W = 32 * VV;                 // cells held by the warp (with halo lanes)
+    static constexpr int SEG = (32 - 2 * HL) * VV;    // cells owned by the warp at most
+    static constexpr int Q = 2 * R + 1;
+    // ring layout per warp (elements): prologue rows of u (and Phi_x), then stages
+    static constexpr int NF = KIND == 0 ? 5 : 7;      // u_head, u_prev, c2, dw, ic, [phx_head, phz]
+    static constexpr int PRO = (KIND == 0 ? 1 : 2) * 2 * R * W;
+    static constexpr int STAGE = NF * W;
+    static constexpr int ELEMS = PRO + kStages * STAGE;
+};
+
+template <typename T, int R>
+struct WarpSmem {
+    static constexpr int e0 = Geo<T, R, 0>::ELEMS, e1 = Geo<T, R, 1>::ELEMS;
+    static constexpr int ELEMS = e0 > e1 ? e0 : e1;
+    static constexpr size_t per_warp = 128 + sizeof(T) * (size_t)ELEMS;  // barriers + ring
+    static constexpr size_t bytes = kWarps * per_warp;
+};
+
 template <typename T, int VV, int HL>
 __device__ __forceinline__ void zwindow(const Vec<T, VV>& c, T (&w)[(2 * HL + 1) * VV]) {
 #pragma unroll
@@ -88,212 +105,293 @@ __device__ __forceinline__ void zwindow(const Vec<T, VV>& c, T (&w)[(2 * HL + 1)
     }
 }
 
-template <typename T, int R, int MODE, int VV, bool PML>
-__device__ __forceinline__ void sweep(const WaveParams<T>& p, const int shot, const int x0, const int x1,
-                                      const int zs, const int ze) {
-    constexpr int HL = (R + VV - 1) / VV;
-    constexpr int Q = 2 * R + 1;
+template <typename T, int R, int MODE, int KIND>
+__device__ __forceinline__ void sweep(const WaveParams<T>& p, unsigned char* wsm, const int shot, const int x0,
+                                      const int x1, const int zs, const int ze) {
+    using G = Geo<T, R, KIND>;
+    constexpr int VV = G::VV, HL = G::HL, W = G::W, Q = G::Q;
+    constexpr bool PML = KIND == 1;
     constexpr int NWIN = (2 * HL + 1) * VV;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(wsm);
+    T* ring = reinterpret_cast<T*>(wsm + 128);
+    T* pro = ring;                    // 2R rows of u (then 2R rows of Phi_x)
+    T* stg0 = ring + G::PRO;          // stage s at stg0 + s*STAGE, field f at + f*W
     const int lane = threadIdx.x & 31;
-    const int zl = zs + (lane - HL) * VV;                 // first cell of this lane's vector
-    const bool ldz = zl < p.nz;                            // vector holds grid cells (else zeros)
+    const int niter = x1 - x0;
+    const int zw0 = zs - HL * VV;                         // first cell held by lane 0
+    const int zl = zw0 + lane * VV;                       // first cell of this lane's vector
     const bool own = lane >= HL && lane < 32 - HL && zl < ze;
     const long long sh = (long long)shot * p.fstride;
-    const T* __restrict__ ucur = p.u_cur + sh;
-    T* __restrict__ uprev = p.u_prev + sh;
-    const T* __restrict__ phx_in = p.phx_in + sh;
-    const T* __restrict__ phz_in = p.phz_in + sh;
+    const T* ucur = p.u_cur + sh;
+    T* uprev = p.u_prev + sh;
     const bool zpad = PML && (zl < p.pzl || zl + VV - 1 >= p.nz - p.pzr);
     auto xpad = [&](int x) { return x < p.pxl || x >= p.nx - p.pxr; };
-    auto off = [&](int x) { return (long long)(x + kHalo) * p.ldz + kOZ + zl; };
-    const int* bx = p.inj.box + shot * 6;
-    const bool inj_task = p.inj.on && bx[0] < x1 && bx[1] > x0 && bx[4] < ze && bx[5] > zs;
+    auto rowoff = [&](int x) { return (long long)(x + kHalo) * p.ldz + kOZ; };
 
+    // copy extents (elements): full lane range for u / Phi_z (clamped to the row
+    // storage), owned range for the rest; both multiples of 4 elements (16 bytes)
+    const int nfull = min(W, (p.ldz - kOZ - zw0) / 4 * 4);
+    const int own0 = HL * VV;                              // lane HL's offset in a slot
+    const int nown = ((min(ze, zs + G::SEG) - zs) + 3) / 4 * 4;
+
+    if (lane == 0) {
+        for (int s = 0; s < kStages; ++s) mbar_init(&bar[s], 1);
+        fence_mbar_init();
+    }
+    __syncwarp();
+
+    auto issue = [&](int i) {  // copies of iteration i (row x0 + i) into stage i % kStages
+        const int x = x0 + i;
+        const int s = i % kStages;
+        T* st = stg0 + s * G::STAGE;
+        uint32_t bytes = (uint32_t)(nfull + 2 * nown) * sizeof(T);
+        if (MODE == kAdj && p.image) bytes += 2u * nown * sizeof(T);
+        if (PML) bytes += (uint32_t)(nown + nfull) * sizeof(T);
+        if (i == 0) bytes += (uint32_t)(2 * R * nfull * (PML ? 2 : 1)) * sizeof(T);
+        mbar_arrive_expect_tx(&bar[s], bytes);
+        if (i == 0)
+            for (int j = 0; j < 2 * R; ++j) {
+                bulk_g2s(pro + j * W, ucur + rowoff(x0 - R + j) + zw0, nfull * sizeof(T), &bar[s]);
+                if (PML) bulk_g2s(pro + (2 * R + j) * W, p.phx_in + sh + rowoff(x0 - R + j) + zw0,
+                                  nfull * sizeof(T), &bar[s]);
+            }
+        bulk_g2s(st, ucur + rowoff(x + R) + zw0, nfull * sizeof(T), &bar[s]);
+        bulk_g2s(st + W + own0, uprev + rowoff(x) + zs, nown * sizeof(T), &bar[s]);
+        bulk_g2s(st + 2 * W + own0, p.c2 + rowoff(x) + zs, nown * sizeof(T), &bar[s]);
+        if (MODE == kAdj && p.image) {
+            bulk_g2s(st + 3 * W + own0, p.dw_in + sh + rowoff(x) + zs, nown * sizeof(T), &bar[s]);
+            bulk_g2s(st + 4 * W + own0, p.ic + sh + rowoff(x) + zs, nown * sizeof(T), &bar[s]);
+        }
+        if (PML) {
+            bulk_g2s(st + 5 * W + own0, p.phx_in + sh + rowoff(x + R) + zs, nown * sizeof(T), &bar[s]);
+            bulk_g2s(st + 6 * W, p.phz_in + sh + rowoff(x) + zw0, nfull * sizeof(T), &bar[s]);
+        }
+    };
+    if (lane == 0) {
+        fence_proxy_async();
+        for (int i = 0; i < min(kStages, niter); ++i) issue(i);
+    }
+
+    // per-lane constants
     T sgz[VV], mgz[VV];
-    bool zok[VV];
+    bool zok[VV], zpe[VV];
 #pragma unroll
     for (int v = 0; v < VV; ++v) {
         const int z = zl + v;
         zok[v] = z > 0 && z < p.nz - 1;
+        zpe[v] = z < p.pzl || z >= p.nz - p.pzr;
         sgz[v] = (PML && z >= 0 && z < p.nz) ? __ldg(p.sgz + z) : T(0);
         mgz[v] = (PML && MODE == kRecomp && z >= 0 && z < p.nz) ? __ldg(p.mgz + z) : T(0);
     }
+    bool zpw[NWIN];  // padding test of each z-window element (PML tasks)
+#pragma unroll
+    for (int j = 0; j < NWIN; ++j) {
+        const int z = zl - HL * VV + j;
+        zpw[j] = z < p.pzl || z >= p.nz - p.pzr;
+    }
+    // combined Laplacian weights
+    T cx[R + 1], cz[R + 1];
+#pragma unroll
+    for (int m = 0; m <= R; ++m) {
+        cx[m] = T(d2w(R, m)) * p.idx2;
+        cz[m] = T(d2w(R, m)) * p.idz2;
+    }
+    const T c0 = cx[0] + cz[0];
+    const int* bx = p.inj.box + shot * 6;
+    const bool inj_task = p.inj.on && bx[0] < x1 && bx[1] > x0 && bx[4] < ze && bx[5] > zs;
+    bool bad = false;
+    bool late = false;
 
     Vec<T, VV> q[Q];
-    Vec<T, VV> qx[Q];  // used by PML tasks only
-#pragma unroll
-    for (int j = 0; j < Q - 1; ++j) {
-        const int x = x0 - R + j;
-        q[j] = ldz ? ldv_ro<T, VV>(ucur + off(x)) : zvec<T, VV>();
-        if (PML) qx[j] = (ldz && (zpad || xpad(x))) ? ldv_ro<T, VV>(phx_in + off(x)) : zvec<T, VV>();
-    }
-    // prefetch registers of the first row
-    Vec<T, VV> nq = ldz ? ldv_ro<T, VV>(ucur + off(x0 + R)) : zvec<T, VV>();
-    Vec<T, VV> nqx;
-    if (PML) nqx = (ldz && (zpad || xpad(x0 + R))) ? ldv_ro<T, VV>(phx_in + off(x0 + R)) : zvec<T, VV>();
-    Vec<T, VV> num = ldz ? ldv<T, VV>(uprev + off(x0)) : zvec<T, VV>();
-    Vec<T, VV> ncc = ldz ? ldv_ro<T, VV>(p.c2 + off(x0)) : zvec<T, VV>();
-    Vec<T, VV> npz;
-    if (PML) npz = (ldz && (zpad || xpad(x0))) ? ldv_ro<T, VV>(phz_in + off(x0)) : zvec<T, VV>();
-    Vec<T, VV> ndw, nic;
-    if (MODE == kAdj && p.image) {
-        ndw = own ? ldv_cs<T, VV>(p.dw_in + sh + off(x0)) : zvec<T, VV>();
-        nic = own ? ldv<T, VV>(p.ic + sh + off(x0)) : zvec<T, VV>();
-    }
-    bool bad = false;
+    Vec<T, VV> qx[Q];  // Phi_x queue (PML tasks)
 
-    for (int x = x0; x < x1; ++x) {
-        q[Q - 1] = nq;
-        if (PML) qx[Q - 1] = nqx;
-        const Vec<T, VV> um = num, cc = ncc;
-        Vec<T, VV> pzc;
-        if (PML) pzc = npz;
-        Vec<T, VV> dwi, ici;
-        if (MODE == kAdj && p.image) { dwi = ndw; ici = nic; }
-        // prefetch row x + 1
-        if (x + 1 < x1) {
-            const int xn = x + 1;
-            nq = ldz ? ldv_ro<T, VV>(ucur + off(xn + R)) : zvec<T, VV>();
-            if (PML) nqx = (ldz && (zpad || xpad(xn + R))) ? ldv_ro<T, VV>(phx_in + off(xn + R)) : zvec<T, VV>();
-            num = ldz ? ldv<T, VV>(uprev + off(xn)) : zvec<T, VV>();
-            ncc = ldz ? ldv_ro<T, VV>(p.c2 + off(xn)) : zvec<T, VV>();
-            if (PML) npz = (ldz && (zpad || xpad(xn))) ? ldv_ro<T, VV>(phz_in + off(xn)) : zvec<T, VV>();
-            if (MODE == kAdj && p.image) {
-                ndw = own ? ldv_cs<T, VV>(p.dw_in + sh + off(xn)) : zvec<T, VV>();
-                nic = own ? ldv<T, VV>(p.ic + sh + off(xn)) : zvec<T, VV>();
-            }
-        }
-        T w[NWIN];
-        zwindow<T, VV, HL>(q[R], w);
-        T wp[NWIN];  // Phi_z window, PML tasks only
-        if (PML) zwindow<T, VV, HL>(pzc, wp);
-        const bool xok = x > 0 && x < p.nx - 1;
-        const bool xp = PML && xpad(x);
-        const T sgx = PML ? __ldg(p.sgx + x) : T(0);
-        const T mgx = (PML && MODE == kRecomp) ? __ldg(p.mgx + x) : T(0);
-        const bool inj_row = inj_task && x >= bx[0] && x < bx[1];
-        Vec<T, VV> un, dwo, pxo, pzo, ico;
+    for (int ib = 0; ib < niter; ib += Q) {
 #pragma unroll
-        for (int v = 0; v < VV; ++v) {
-            const int z = zl + v;
-            const T uc = w[HL * VV + v];
-            T lz = T(d2w(R, 0)) * uc, lx = T(d2w(R, 0)) * uc, dz1 = T(0), dx1 = T(0);
+        for (int so = 0; so < Q; ++so) {
+            const int i = ib + so;
+            if (i >= niter) break;
+            const int x = x0 + i;
+            const int s = i % kStages;
+            const T* st = stg0 + s * G::STAGE;
+            if (!mbar_wait_bounded(&bar[s], (uint32_t)((i / kStages) & 1), kPolls)) late = true;
+            if (i == 0) {
 #pragma unroll
-            for (int m = 1; m <= R; ++m) {
-                const T zp = w[HL * VV + v + m], zm = w[HL * VV + v - m];
-                const T xpv = q[R + m].v[v], xmv = q[R - m].v[v];
-                lz += T(d2w(R, m)) * (zp + zm);
-                lx += T(d2w(R, m)) * (xpv + xmv);
-                if (PML) {
-                    dz1 += T(d1w(R, m)) * (zp - zm);
-                    dx1 += T(d1w(R, m)) * (xpv - xmv);
+                for (int j = 0; j < 2 * R; ++j) {
+                    q[(so + j) % Q] = lds<T, VV>(pro + j * W + lane * VV);
+                    if (PML) {
+                        Vec<T, VV> a = lds<T, VV>(pro + (2 * R + j) * W + lane * VV);
+                        const bool use = zpad || xpad(x0 - R + j);
+#pragma unroll
+                        for (int v = 0; v < VV; ++v) a.v[v] = use ? a.v[v] : T(0);
+                        qx[(so + j) % Q] = a;
+                    }
                 }
             }
-            T F = lx * p.idx2 + lz * p.idz2;
-            if (inj_row && own && z < p.nz) F += inject_rhs(p.inj, bx, shot, x, z);
-            const T uo = um.v[v], c2 = cc.v[v];
-            const bool ok = xok && zok[v];
-            T unew;
+            q[(so + 2 * R) % Q] = lds<T, VV>(st + lane * VV);
+            const Vec<T, VV> um = lds<T, VV>(st + W + lane * VV);
+            const Vec<T, VV> cc = lds<T, VV>(st + 2 * W + lane * VV);
+            Vec<T, VV> dwi, ici, pzc;
+            if (MODE == kAdj && p.image) {
+                dwi = lds<T, VV>(st + 3 * W + lane * VV);
+                ici = lds<T, VV>(st + 4 * W + lane * VV);
+            }
             if (PML) {
-                T dpx = T(0), dpz = T(0);
+                Vec<T, VV> a = lds<T, VV>(st + 5 * W + lane * VV);
+                const bool use = zpad || xpad(x + R);
+#pragma unroll
+                for (int v = 0; v < VV; ++v) a.v[v] = use ? a.v[v] : T(0);
+                qx[(so + 2 * R) % Q] = a;
+                pzc = lds<T, VV>(st + 6 * W + lane * VV);
+            }
+            __syncwarp();  // every lane has read stage s: lane 0 may refill it
+            if (lane == 0 && i + kStages < niter) {
+                fence_proxy_async();
+                issue(i + kStages);
+            }
+
+            const Vec<T, VV>& qc = q[(so + R) % Q];
+            T w[NWIN];
+            zwindow<T, VV, HL>(qc, w);
+            T wp[NWIN];  // Phi_z window (PML tasks)
+            if (PML) {
+                zwindow<T, VV, HL>(pzc, wp);
+                const bool xp = xpad(x);
+#pragma unroll
+                for (int j = 0; j < NWIN; ++j) wp[j] = (xp || zpw[j]) ? wp[j] : T(0);
+            }
+            const bool xok = x > 0 && x < p.nx - 1;
+            const bool inj_row = inj_task && x >= bx[0] && x < bx[1];
+            Vec<T, VV> un, dwo, pxo, pzo, ico;
+            T sgx = T(0), mgx = T(0);
+            if (PML) {
+                sgx = __ldg(p.sgx + x);
+                if (MODE == kRecomp) mgx = __ldg(p.mgx + x);
+            }
+#pragma unroll
+            for (int v = 0; v < VV; ++v) {
+                const int z = zl + v;
+                const T uc = w[HL * VV + v];
+                T F = c0 * uc;
 #pragma unroll
                 for (int m = 1; m <= R; ++m) {
-                    dpx += T(d1w(R, m)) * (qx[R + m].v[v] - qx[R - m].v[v]);
-                    dpz += T(d1w(R, m)) * (wp[HL * VV + v + m] - wp[HL * VV + v - m]);
+                    F += cx[m] * (q[(so + R + m) % Q].v[v] + q[(so + R - m) % Q].v[v]);
+                    F += cz[m] * (w[HL * VV + v + m] + w[HL * VV + v - m]);
                 }
-                F += dpx * p.idx + dpz * p.idz;
-                const T sx = sgx, sz = sgz[v];
-                T ph_x = T(0), ph_z = T(0);
-                if (sx != T(0) || sz != T(0)) {
-                    const T dudx = dx1 * p.idx, dudz = dz1 * p.idz;
-                    const T phx = qx[R].v[v], phz = wp[HL * VV + v];
-                    ph_x = phx - p.dt * sx * phx + p.dt * (sz - sx) * dudx;
-                    ph_z = phz - p.dt * sz * phz + p.dt * (sx - sz) * dudz;
-                    const T fac1 = T(2) * p.dt2 / (T(2) + p.dt * (sx + sz));
-                    const T fac2 = c2 * F - (uo - T(2) * uc) * p.idt2 + (sx + sz) * uo * p.i2dt - (sx * sz) * uc;
-                    unew = fac1 * fac2;
-                } else {
-                    unew = p.dt2 * c2 * F - (uo - T(2) * uc);
-                }
-                if (!ok) { unew = T(0); ph_x = T(0); ph_z = T(0); }
-                pxo.v[v] = ph_x;
-                pzo.v[v] = ph_z;
-                if (MODE == kRecomp) {
-                    const T mz = mgz[v];
-                    T d = c2 * F + ((mgx + mz) - (sx + sz)) * (unew - uo) * p.i2dt + (mgx * mz - sx * sz) * uc;
-                    dwo.v[v] = ok ? d : T(0);
-                }
-            } else {
-                unew = p.dt2 * c2 * F - (uo - T(2) * uc);
-                if (!ok) unew = T(0);
-                if (MODE == kRecomp) dwo.v[v] = ok ? c2 * F : T(0);
-            }
-            un.v[v] = unew;
-            if (MODE == kFwd) bad |= !isfinite(unew);
-            if (MODE == kAdj) ico.v[v] = ici.v[v] + uc * dwi.v[v];
-        }
-        if (own) {
-            const long long o = off(x);
-            stv<T, VV>(uprev + o, un);
-            if (PML && (xp || zpad)) {
-                stv<T, VV>(p.phx_out + sh + o, pxo);
-                stv<T, VV>(p.phz_out + sh + o, pzo);
-            }
-            if (MODE == kRecomp && p.dw_out) stv_cs<T, VV>(p.dw_out + sh + o, dwo);
-            if (MODE == kAdj && p.image) stv<T, VV>(p.ic + sh + o, ico);
-        }
+                if (inj_row && own && z < p.nz) F += inject_rhs(p.inj, bx, shot, x, z);
+                const T uo = um.v[v], c2 = cc.v[v];
+                const bool ok = xok && zok[v];
+                T unew;
+                if (PML) {
+                    T dpx = T(0), dpz = T(0), dx1 = T(0), dz1 = T(0);
 #pragma unroll
-        for (int j = 0; j < Q - 1; ++j) {
-            q[j] = q[j + 1];
-            if (PML) qx[j] = qx[j + 1];
+                    for (int m = 1; m <= R; ++m) {
+                        const T a = T(d1w(R, m));
+                        dpx += a * (qx[(so + R + m) % Q].v[v] - qx[(so + R - m) % Q].v[v]);
+                        dpz += a * (wp[HL * VV + v + m] - wp[HL * VV + v - m]);
+                        dx1 += a * (q[(so + R + m) % Q].v[v] - q[(so + R - m) % Q].v[v]);
+                        dz1 += a * (w[HL * VV + v + m] - w[HL * VV + v - m]);
+                    }
+                    F += dpx * p.idx + dpz * p.idz;
+                    const T sx = sgx, sz = sgz[v];
+                    T ph_x = T(0), ph_z = T(0);
+                    if (sx != T(0) || sz != T(0)) {
+                        const T dudx = dx1 * p.idx, dudz = dz1 * p.idz;
+                        const T phx = qx[(so + R) % Q].v[v], phz = wp[HL * VV + v];
+                        ph_x = phx - p.dt * sx * phx + p.dt * (sz - sx) * dudx;
+                        ph_z = phz - p.dt * sz * phz + p.dt * (sx - sz) * dudz;
+                        const T fac1 = T(2) * p.dt2 / (T(2) + p.dt * (sx + sz));
+                        const T fac2 = c2 * F - (uo - T(2) * uc) * p.idt2 + (sx + sz) * uo * p.i2dt - (sx * sz) * uc;
+                        unew = fac1 * fac2;
+                    } else {
+                        unew = p.dt2 * c2 * F - (uo - T(2) * uc);
+                    }
+                    if (!ok) { unew = T(0); ph_x = T(0); ph_z = T(0); }
+                    pxo.v[v] = ph_x;
+                    pzo.v[v] = ph_z;
+                    if (MODE == kRecomp) {
+                        const T mz = mgz[v];
+                        const T d = c2 * F + ((mgx + mz) - (sx + sz)) * (unew - uo) * p.i2dt + (mgx * mz - sx * sz) * uc;
+                        dwo.v[v] = ok ? d : T(0);
+                    }
+                } else {
+                    unew = ok ? p.dt2 * c2 * F - (uo - T(2) * uc) : T(0);
+                    if (MODE == kRecomp) dwo.v[v] = ok ? c2 * F : T(0);
+                }
+                un.v[v] = unew;
+                if (MODE == kFwd) bad |= !isfinite(unew);
+                if (MODE == kAdj) ico.v[v] = ici.v[v] + uc * dwi.v[v];
+            }
+            if (own) {
+                const long long o = rowoff(x) + zl;
+                stg<T, VV>(uprev + o, un);
+                if (PML && (zpad || xpad(x))) {
+                    stg<T, VV>(p.phx_out + sh + o, pxo);
+                    stg<T, VV>(p.phz_out + sh + o, pzo);
+                }
+                if (MODE == kRecomp && p.dw_out) stg_cs<T, VV>(p.dw_out + sh + o, dwo);
+                if (MODE == kAdj && p.image) stg<T, VV>(p.ic + sh + o, ico);
+            }
         }
     }
-    if (MODE == kFwd && bad && own && p.err) atomicOr(p.err, PGB_ERR_NONFINITE);
+    if (p.err) {
+        if (MODE == kFwd && bad && own) atomicOr(p.err, PGB_ERR_NONFINITE);
+        if (late && lane == 0) atomicOr(p.err, PGB_ERR_TIMEOUT);
+    }
 }
 
 template <typename T, int R, int MODE>
 __global__ void __launch_bounds__(kWarps * 32) wave2d_warp_kernel(const WaveParams<T> p, const int* __restrict__ tasks,
                                                                   int ntasks, int task_blocks) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     if ((int)blockIdx.x >= task_blocks) {
         if (MODE == kFwd) record_block(p, blockIdx.x - task_blocks);
         return;
     }
-    const int gw = blockIdx.x * kWarps + (threadIdx.x >> 5);
+    const int warp = threadIdx.x >> 5;
+    const int gw = blockIdx.x * kWarps + warp;
     if (gw >= ntasks * p.nshot) return;  // warp-uniform
     const int shot = gw / ntasks;
     const int* tk = tasks + 5 * (gw - shot * ntasks);
     const int x0 = __ldg(tk), x1 = __ldg(tk + 1), zs = __ldg(tk + 2), ze = __ldg(tk + 3), kind = __ldg(tk + 4);
-    constexpr int V = V16<T>::N;
+    unsigned char* wsm = smem_raw + warp * WarpSmem<T, R>::per_warp;
     if (kind == 0)
-        sweep<T, R, MODE, V, false>(p, shot, x0, x1, zs, ze);
+        sweep<T, R, MODE, 0>(p, wsm, shot, x0, x1, zs, ze);
     else
-        sweep<T, R, MODE, (V > 1 ? V / 2 : 1), true>(p, shot, x0, x1, zs, ze);
+        sweep<T, R, MODE, 1>(p, wsm, shot, x0, x1, zs, ze);
+}
+
+template <typename T, int R>
+void prep_warp() {
+    const int b = (int)WarpSmem<T, R>::bytes;
+    cudaFuncSetAttribute(wave2d_warp_kernel<T, R, kFwd>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    cudaFuncSetAttribute(wave2d_warp_kernel<T, R, kRecomp>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    cudaFuncSetAttribute(wave2d_warp_kernel<T, R, kAdj>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
 }
 
 }  // namespace
 
-// The task table of a launch sits in p.rec-independent storage: the plan passes it
-// through p.inj-free fields below (tasks pointer and count are launch arguments).
 template <typename T, int R, int MODE>
 void launch_wave2d_warp_tasks(const WaveParams<T>& p, const int* tasks, int ntasks, cudaStream_t s) {
     const int task_blocks = (ntasks * p.nshot + kWarps - 1) / kWarps;
     const int grid = task_blocks + (MODE == kFwd ? p.rec.blocks : 0);
-    wave2d_warp_kernel<T, R, MODE><<<grid, kWarps * 32, 0, s>>>(p, tasks, ntasks, task_blocks);
+    wave2d_warp_kernel<T, R, MODE><<<grid, kWarps * 32, WarpSmem<T, R>::bytes, s>>>(p, tasks, ntasks, task_blocks);
+}
+
+void wave2d_warp_prepare() {
+    prep_warp<float, 1>(); prep_warp<float, 2>(); prep_warp<float, 3>(); prep_warp<float, 4>();
+    prep_warp<double, 1>(); prep_warp<double, 2>(); prep_warp<double, 3>(); prep_warp<double, 4>();
 }
 
 int wave2d_warp_threads() { return kWarps * 32; }
 
-// widest z-range a task of each kind may cover: (32 - 2*HL) * VV cells
+// widest z-range a task of each kind may own: (32 - 2*HL) * VV cells (same rule as Geo)
 int wave2d_warp_seg(int dtype_bytes, int order, int pml) {
     const int V = 16 / dtype_bytes;
     const int VV = pml ? (V > 1 ? V / 2 : 1) : V;
     const int R = order / 2;
-    const int HL = (R + VV - 1) / VV;
+    const int A = V / VV;
+    const int HL = ((R + VV - 1) / VV + A - 1) / A * A;
     return (32 - 2 * HL) * VV;
-}
-int wave2d_warp_vec(int dtype_bytes, int pml) {
-    const int V = 16 / dtype_bytes;
-    return pml ? (V > 1 ? V / 2 : 1) : V;
 }
 
 #define PGB_INSTW(T, R)                                                                                   \
