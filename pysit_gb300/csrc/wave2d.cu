@@ -267,11 +267,11 @@ __global__ void __launch_bounds__(kNT, 2) wave2d_kernel(const WaveParams<T> p) {
             for (int v = 0; v < V; ++v) {
                 const int z = zc + v;
                 const T uc = w[H + v];
-                T lz = T(d2w(R, 0)) * uc, lx = T(d2w(R, 0)) * uc, dz1 = T(0), dx1 = T(0);
+                T lz = T(0), lx = T(0), dz1 = T(0), dx1 = T(0);  // difference form (weights sum to 0)
 #pragma unroll
                 for (int m = 1; m <= R; ++m) {
-                    lz += T(d2w(R, m)) * (w[H + v + m] + w[H + v - m]);
-                    lx += T(d2w(R, m)) * (xpv[m - 1][v] + xm[m - 1][v]);
+                    lz += T(d2w(R, m)) * ((w[H + v + m] - uc) + (w[H + v - m] - uc));
+                    lx += T(d2w(R, m)) * ((xpv[m - 1][v] - uc) + (xm[m - 1][v] - uc));
                     dz1 += T(d1w(R, m)) * (w[H + v + m] - w[H + v - m]);
                     dx1 += T(d1w(R, m)) * (xpv[m - 1][v] - xm[m - 1][v]);
                 }
@@ -306,11 +306,11 @@ __global__ void __launch_bounds__(kNT, 2) wave2d_kernel(const WaveParams<T> p) {
             for (int v = 0; v < V; ++v) {
                 const int z = zc + v;
                 const T uc = w[H + v];
-                T lz = T(d2w(R, 0)) * uc, lx = T(d2w(R, 0)) * uc;
+                T lz = T(0), lx = T(0);  // difference form (weights sum to 0)
 #pragma unroll
                 for (int m = 1; m <= R; ++m) {
-                    lz += T(d2w(R, m)) * (w[H + v + m] + w[H + v - m]);
-                    lx += T(d2w(R, m)) * (xpv[m - 1][v] + xm[m - 1][v]);
+                    lz += T(d2w(R, m)) * ((w[H + v + m] - uc) + (w[H + v - m] - uc));
+                    lx += T(d2w(R, m)) * ((xpv[m - 1][v] - uc) + (xm[m - 1][v] - uc));
                 }
                 T F = lx * p.idx2 + lz * p.idz2;
                 if (inj_row && z < p.nz) F += inject_rhs(p.inj, bx, shot, x, z);

@@ -196,7 +196,6 @@ __device__ __forceinline__ void sweep(const WaveParams<T>& p, unsigned char* wsm
         cx[m] = T(d2w(R, m)) * p.idx2;
         cz[m] = T(d2w(R, m)) * p.idz2;
     }
-    const T c0 = cx[0] + cz[0];
     const int* bx = p.inj.box + shot * 6;
     const bool inj_task = p.inj.on && bx[0] < x1 && bx[1] > x0 && bx[4] < ze && bx[5] > zs;
     bool bad = false;
@@ -271,11 +270,14 @@ __device__ __forceinline__ void sweep(const WaveParams<T>& p, unsigned char* wsm
             for (int v = 0; v < VV; ++v) {
                 const int z = zl + v;
                 const T uc = w[HL * VV + v];
-                T F = c0 * uc;
+                // Laplacian in difference form: sum_m w_m ((u_+m - u_0) + (u_-m - u_0)),
+                // equal to the central stencil because the weights sum to zero, and free
+                // of the large cancellation of w_0 u_0 (the FP32 path depends on this)
+                T F = T(0);
 #pragma unroll
                 for (int m = 1; m <= R; ++m) {
-                    F += cx[m] * (q[(so + R + m) % Q].v[v] + q[(so + R - m) % Q].v[v]);
-                    F += cz[m] * (w[HL * VV + v + m] + w[HL * VV + v - m]);
+                    F += cx[m] * ((q[(so + R + m) % Q].v[v] - uc) + (q[(so + R - m) % Q].v[v] - uc));
+                    F += cz[m] * ((w[HL * VV + v + m] - uc) + (w[HL * VV + v - m] - uc));
                 }
                 if (inj_row && own && z < p.nz) F += inject_rhs(p.inj, bx, shot, x, z);
                 const T uo = um.v[v], c2 = cc.v[v];

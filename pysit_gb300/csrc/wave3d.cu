@@ -45,11 +45,15 @@ __device__ __forceinline__ T dd1(const T* __restrict__ v, long long o, long long
     for (int m = 1; m <= R; ++m) a += T(d1w(R, m)) * (v[o + m * s] - v[o - m * s]);
     return a;
 }
+// second derivative in difference form: sum_m w_m ((v_+m - v_0) + (v_-m - v_0)),
+// equal to the central stencil (the weights sum to zero) with far less FP32
+// cancellation than w_0 v_0 + sum_m w_m (v_+m + v_-m)
 template <typename T, int R>
 __device__ __forceinline__ T dd2(const T* __restrict__ v, long long o, long long s) {
-    T a = T(d2w(R, 0)) * v[o];
+    const T c = v[o];
+    T a = T(0);
 #pragma unroll
-    for (int m = 1; m <= R; ++m) a += T(d2w(R, m)) * (v[o + m * s] + v[o - m * s]);
+    for (int m = 1; m <= R; ++m) a += T(d2w(R, m)) * ((v[o + m * s] - c) + (v[o - m * s] - c));
     return a;
 }
 
