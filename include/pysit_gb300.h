@@ -183,6 +183,19 @@ int pysit_plan_misfit(pysit_plan* plan, const void* dobs_dev, double* rnorm2_dev
  * bit 0 (1) = a bounded wait for a bulk copy expired (results invalid),
  * bit 1 (2) = a non-finite wavefield value appeared (unstable time step). */
 int pysit_plan_status(pysit_plan* plan, int* flags, void* stream);
+/* ------------------------------------------------------------------------
+ * Allocation-free per-shot misfit.  No counterpart in the reference: it exists
+ * for callers that cannot allocate device memory (applications that reserve all
+ * device memory in their own pool up front, C/Fortran codes that link no
+ * allocator).  Inputs dobs, dsim and output resid (may be NULL) are
+ * [nshots][per_shot] arrays of `dtype`; rnorm2 (FP64, dev) receives
+ * sum_i (dobs - dsim)^2 per shot.  No allocation: the reduction scratch is a
+ * fixed 128 KiB device array (nshots <= 256, larger counts are rejected).  The
+ * first call on a device looks its address up (make it before any stream
+ * capture).  All calls share that array: calls that overlap on the GPU race.
+ * ------------------------------------------------------------------------ */
+int pysit_misfit_per_shot_noalloc(int dtype, const void* dobs, const void* dsim, int nshots,
+                                  int64_t per_shot, void* resid, double* rnorm2, void* stream);
 /* Number of kernel launches the last forward/gradient/misfit call issued. */
 int pysit_plan_last_launch_count(const pysit_plan* plan, int64_t* launches);
 
