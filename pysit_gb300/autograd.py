@@ -4,8 +4,11 @@
 tensor ``C`` (unpadded grid, any device, requires_grad optional) and returns
 the objective of TemporalLeastSquares.evaluate (0.5*dt*sum||r||^2,
 pysit/objective_functions/temporal_least_squares.py:67-82).  Its backward
-returns dJ/dC = dJ/dm * dm/dC with dJ/dm the reference's compute_gradient
-(m = C**-2, model_parameter.py:80-92), i.e. dJ/dC = grad_m * (-2 C**-3).
+returns the partial derivatives dJ/dC_i = dJ/dm_i * dm_i/dC_i (m = C**-2,
+model_parameter.py:80-92).  The reference's compute_gradient g is the gradient
+for the cell-volume inner product of model space (mesh.inner_product; the
+adjoint test of temporal_modeling.py:982-984 pairs it with prod(deltas)), so
+dJ/dm_i = g_i * dV and dJ/dC_i = g_i * dV * (-2 C_i**-3), dV = prod(mesh.deltas).
 
 Per call: C goes to the device, is edge-padded there (solver_base.py:111),
 dt/nsteps follow from max|C| (constant_density_acoustic_time_base.py:54-70),
@@ -58,10 +61,6 @@ def _edge_pad(C, mesh):
     return out
 
 
-class _Misfit:
-    pass
-
-
 def _make_function():
     torch = _native.require_cuda()
 
@@ -71,13 +70,14 @@ def _make_function():
             J, grad_m = obj._run(C, want_grad=C.requires_grad)
             if grad_m is not None:
                 ctx.save_for_backward(C.detach(), grad_m)
+                ctx.dV = float(np.prod(obj.solver.mesh.deltas))
             return J
 
         @staticmethod
         def backward(ctx, gJ):
             C, grad_m = ctx.saved_tensors
             Cd = C.to(device=grad_m.device, dtype=torch.float64)
-            dC = grad_m * (-2.0) * Cd ** -3
+            dC = grad_m * (-2.0 * ctx.dV) * Cd ** -3
             return (gJ.to(dC.device) * dC).to(dtype=C.dtype, device=C.device), None
 
     return MisfitFunction
@@ -123,7 +123,8 @@ class FWIMisfit:
         plan.dobs.copy_(resample_linear(obs, self.ts_observed, self.solver.ts()))
         if want_grad:
             g, rn = plan.gradient()
-            grad_m = g.reshape(self.solver.mesh.shape(as_grid=True)).clone()
+            # flat, x-major like PySIT's model vectors: takes the caller's shape of C
+            grad_m = g.reshape(C.shape).clone()
         else:
             rn = plan.misfit()
             grad_m = None

@@ -190,6 +190,8 @@ struct PlanT final : public pysit_plan {
     int nseg;
     bool warp2d = true;          // 2D: warp-task sweep (true) or bulk-copy row pipeline (false)
     std::vector<int> tasks2d;    // [ntasks][5] warp tasks of the 2D sweep
+    int blocks2d[3] = {1, 1, 1}; // resident task blocks of the 2D sweep per mode (whole GPU)
+    unsigned long long ctr_next = 0;  // task-counter value the next 2D launch starts at
     // ---- acquisition (host) ----------------------------------------------------
     std::vector<CSRBox> src_inj, rec_inj;
     std::vector<int> rec_rows;        // [nshots*nrec+1]
@@ -207,7 +209,7 @@ struct PlanT final : public pysit_plan {
         size_t sbox, srpb, srow, spt, sw;          // source injection
         size_t rbox, rrpb, rrow, rpt, rw;          // receiver injection
         size_t recrow, recoff, recw;               // recording
-        size_t gpad, partial, rnorm, err, tasks;
+        size_t gpad, partial, rnorm, err, tasks, ctr;
     } off{};
     size_t field_bytes = 0;      // one field for G shots
     int ckpt_fields = 0;         // fields per checkpoint
@@ -346,9 +348,10 @@ struct PlanT final : public pysit_plan {
         if (xb <= xa || zb <= za) return;
         std::vector<std::pair<int, int>> zs;
         split(za, zb, wave2d_warp_seg((int)sizeof(T), order, kind), zs);
-        for (int x = xa; x < xb; x += tx)
+        const int nxc = (xb - xa + tx - 1) / tx, wx = (xb - xa + nxc - 1) / nxc;  // even x chunks
+        for (int x = xa; x < xb; x += wx)
             for (auto& z : zs) {
-                int t[5] = {x, std::min(xb, x + tx), z.first, z.second, kind};
+                int t[5] = {x, std::min(xb, x + wx), z.first, z.second, kind};
                 tasks2d.insert(tasks2d.end(), t, t + 5);
             }
     }
@@ -490,6 +493,7 @@ struct PlanT final : public pysit_plan {
         off.recw = take(std::max<size_t>(rec_ws.size(), 1) * sizeof(T));
         off.gpad = take((size_t)nx * ny * nz * sizeof(double));
         off.err = take(sizeof(int));
+        off.ctr = take(sizeof(unsigned long long));
         off.tasks = take(std::max<size_t>(tasks2d.size(), 1) * sizeof(int));
         off.partial = take(kRedBlocks * sizeof(double));
         off.rnorm = take(sizeof(double));
@@ -555,7 +559,11 @@ struct PlanT final : public pysit_plan {
         if ((rc = upload(off.tasks, tasks2d, s))) return rc;
         PGB_CHECK_CUDA(cudaStreamSynchronize(s));
         if (!cap) PGB_CHECK_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
-        if (dim == 2) { wave2d_prepare(); wave2d_warp_prepare(); }
+        if (dim == 2) {
+            wave2d_prepare();
+            wave2d_warp_prepare();
+            for (int m = 0; m < 3; ++m) blocks2d[m] = wave2d_warp_blocks((int)sizeof(T), order, m, 1ll << 40);
+        }
         PGB_CHECK_CUDA(cudaGetLastError());
         model_set = false;
         return PYSIT_OK;
@@ -600,6 +608,7 @@ struct PlanT final : public pysit_plan {
         p.idy = T(1.0 / dy); p.idy2 = T(1.0 / (T(dy) * T(dy)));
         p.idz = T(1.0 / dz); p.idz2 = T(1.0 / (T(dz) * T(dz)));
         p.err = ws ? at<int>(off.err) : nullptr;
+        p.task_ctr = ws ? at<unsigned long long>(off.ctr) : nullptr;
         (void)g0;
         return p;
     }
@@ -634,9 +643,14 @@ struct PlanT final : public pysit_plan {
         if (dim == 2 && warp2d) {                                              \
             const int* tk = at<int>(off.tasks);                                \
             const int nt = (int)(tasks2d.size() / 5);                          \
-            if (mode == kFwd) launch_wave2d_warp_tasks<T, RR, kFwd>(p, tk, nt, s);            \
-            else if (mode == kRecomp) launch_wave2d_warp_tasks<T, RR, kRecomp>(p, tk, nt, s); \
-            else launch_wave2d_warp_tasks<T, RR, kAdj>(p, tk, nt, s);                         \
+            const long long wpb = wave2d_warp_threads() / 32;                  \
+            const long long need = ((long long)nt * p.nshot + wpb - 1) / wpb;  \
+            const int nb = (int)std::min<long long>(need, blocks2d[mode]);     \
+            WaveParams<T> q = p;                                               \
+            q.task_base = ctr_next;                                            \
+            if (mode == kFwd) ctr_next += launch_wave2d_warp_tasks<T, RR, kFwd>(q, tk, nt, nb, s);            \
+            else if (mode == kRecomp) ctr_next += launch_wave2d_warp_tasks<T, RR, kRecomp>(q, tk, nt, nb, s); \
+            else ctr_next += launch_wave2d_warp_tasks<T, RR, kAdj>(q, tk, nt, nb, s);                         \
         } else if (dim == 2) {                                                 \
             if (mode == kFwd) launch_wave2d<T, RR, kFwd>(p, bz, s);            \
             else if (mode == kRecomp) launch_wave2d<T, RR, kRecomp>(p, bz, s); \
@@ -775,7 +789,14 @@ struct PlanT final : public pysit_plan {
         }
     }
 
+    // the 2D sweep's task counter restarts at zero with every run (eager or graph replay)
+    void reset_task_counter(cudaStream_t s) {
+        cudaMemsetAsync(ws + off.ctr, 0, sizeof(unsigned long long), s);
+        ctr_next = 0;
+    }
+
     void enqueue_forward(void* traces_out, cudaStream_t s) {
+        reset_task_counter(s);
         const size_t tr_group = (size_t)nsteps * nrec * sizeof(T);
         for (int g0 = 0; g0 < nshots; g0 += G) {
             int gn = std::min(G, nshots - g0);
@@ -788,6 +809,7 @@ struct PlanT final : public pysit_plan {
 
     void enqueue_gradient(const void* dobs, double* grad, double* rnorm2, void* traces_out, bool with_grad,
                           bool migrate, cudaStream_t s) {
+        reset_task_counter(s);
         const size_t tr_group = (size_t)nsteps * nrec * sizeof(T);
         if (with_grad) cudaMemsetAsync(ws + off.gpad, 0, (size_t)nx * ny * nz * sizeof(double), s);
         cudaMemsetAsync(ws + off.rnorm, 0, sizeof(double), s);

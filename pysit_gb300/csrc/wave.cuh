@@ -137,6 +137,10 @@ struct WaveParams {
     T* ic;                   // kAdj: imaging accumulator (shot 0 base)
     int image;               // kAdj: accumulate this step
     int* err;                // device error word (PGB_ERR_* bits), may be NULL
+    // 2D persistent sweep: task counter shared by the launches of one run; this
+    // launch's tasks are the counter values task_base .. task_base + tasks - 1
+    unsigned long long* task_ctr;
+    unsigned long long task_base;
 };
 
 // ---- helpers shared by the 2D kernels ---------------------------------------
@@ -174,12 +178,16 @@ __device__ __forceinline__ void record_block(const WaveParams<T>& p, int rb) {
 
 template <typename T, int R, int MODE>
 void launch_wave2d(const WaveParams<T>& p, int bz, cudaStream_t s);
-// warp-independent 2D sweep (shuffles for the z-halo, register queue along x);
-// tasks = [ntasks][5] ints (x0, x1, zs, ze, kind), shared by all shots
+// persistent-warp 2D sweep fed by shared-memory row rings; tasks = [ntasks][5]
+// ints (x0, x1, zs, ze, kind) of one shot, shared by all shots; `blocks` task
+// blocks.  Returns the number of task-counter values the launch consumes.
 template <typename T, int R, int MODE>
-void launch_wave2d_warp_tasks(const WaveParams<T>& p, const int* tasks, int ntasks, cudaStream_t s);
+long long launch_wave2d_warp_tasks(const WaveParams<T>& p, const int* tasks, int ntasks, int blocks,
+                                   cudaStream_t s);
 int wave2d_warp_threads();
 int wave2d_warp_seg(int dtype_bytes, int order, int pml);
+// resident task blocks of the whole GPU for one (dtype, order, mode), at most `tasks`/warps
+int wave2d_warp_blocks(int dtype_bytes, int order, int mode, long long tasks);
 void wave2d_warp_prepare();
 template <typename T, int R, int MODE>
 void launch_wave3d(const WaveParams<T>& p, int bz, cudaStream_t s);

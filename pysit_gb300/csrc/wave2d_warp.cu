@@ -1,9 +1,11 @@
-// Batched 2D leapfrog step, warp-independent sweep (forward, recompute, adjoint).
+// Batched 2D leapfrog step: persistent warps fed by per-warp shared-memory row
+// rings (forward, recompute, adjoint).
 //
 // Same maths as the reference step cda_time_scalar_2D (pysit/solvers/
 // constant_density_acoustic/time/scalar/constant_density_acoustic_time_scalar_2D.h:88-179)
 // with the fusions of the batched pipeline:
-//   kFwd    trace recording of u_k (appended recorder blocks, receivers.py:462-510);
+//   kFwd    trace recording of u_k (recorder blocks at the front of the grid,
+//           receivers.py:462-510);
 //   kRecomp the imaging operand dWaveOp_k (constant_density_acoustic_base.py:24-40)
 //           from the stencil's own bracket F: C^2 F where the step and mesh
 //           sigmas agree, plus the sigma differences elsewhere (the right PML,
@@ -12,31 +14,38 @@
 //           (temporal_modeling.py:312-365).
 //
 // Work decomposition: a table of warp tasks (x0, x1, zs, ze, kind) covers the
-// padded grid once and serves every shot.  A warp owns cells z in [zs, ze) and
-// sweeps rows x0..x1-1.  Lanes hold VV consecutive cells; the HL lanes at each
-// end only carry the z-halo.  Per row:
-//   * lane 0 streams the rows the warp needs D iterations ahead into the warp's
-//     own shared-memory ring with 1-D bulk copies (cp.async.bulk), one mbarrier
-//     per stage; every lane reads its 16-byte vector back (no global-load latency
-//     on the critical path, no block barrier, warps never wait for each other);
-//   * the 2R+1 rows of u_k the x-derivatives need live in a register queue that
-//     rotates by renaming (the row loop is unrolled by 2R+1);
-//   * z-neighbours come from the adjacent lanes with warp shuffles.
+// padded grid of one shot once.  The warps of the launch are persistent: each
+// takes the next (shot, task) from a global counter until the launch's tasks
+// are used up, so no wave of blocks runs half empty at the end.  A task owns the
+// cells z in [zs, ze) of the rows x0..x1-1; lane L holds the V consecutive cells
+// from zs + L*V.  Per row x, lane 0 has already asked (A rows ahead) for
+//   * row x+R of u_k, with an R-cell z-halo each side, into the warp's x-ring
+//     of 2R+A rows (the x-derivatives read rows x-R..x+R from it);
+//   * the centre rows of u_{k-1}, C^2 (and dWaveOp, ic for the adjoint; Phi_z
+//     with its halo, row x+R of Phi_x for the PML) into one of A stages,
+// with 1-D bulk copies (cp.async.bulk) completing on the stage's mbarrier.  Every
+// operand then comes from shared memory with aligned vector loads; the loop body
+// is one row (no unrolling), which keeps the kernel small enough for the
+// instruction cache.  Warps never wait for each other.
 // Task kinds (warp-uniform branch):
-//   kind 0  interior: at least R cells away from the padding, 16-byte vectors,
-//           no PML state;
-//   kind 1  PML shell: the padding and its R-wide rim, 8-byte vectors, Phi_x in a
-//           register queue, Phi_z through shuffles.
-// Waits are bounded: on expiry the kernel sets the plan's error word and goes on.
+//   kind 0  interior: at least R cells away from the padding, 16-byte lane
+//           vectors, no PML state;
+//   kind 1  PML shell: the padding and its R-wide rim, 8-byte lane vectors (more
+//           busy lanes on the narrow z-bands), Phi_x / Phi_z carried where both
+//           sigmas vanish as in the reference.
+// Waits are bounded: on expiry the kernel sets the plan's error word, waits (again
+// bounded) for the copies it issued, and carries on.
 #include "tma.cuh"
 #include "wave.cuh"
 
 namespace pgb {
 namespace {
 
-constexpr int kWarps = 4;   // warps per block
-constexpr int kStages = 3;  // rows in flight ahead of the computation
+constexpr int kWarps = 4;  // warps per block
 constexpr uint32_t kPolls = 1u << 22;
+#ifndef PGB_RING_AHEAD
+#define PGB_RING_AHEAD 4   // rows whose copies are in flight ahead of the computation
+#endif
 
 template <typename T, int N> struct VecT;
 template <> struct VecT<float, 4> { using type = float4; };
@@ -64,133 +73,111 @@ __device__ __forceinline__ void stg_cs(T* p, const Vec<T, N>& r) {
     __stcs(reinterpret_cast<typename VecT<T, N>::type*>(p), *reinterpret_cast<const typename VecT<T, N>::type*>(r.v));
 }
 
-// per-kind geometry
-template <typename T, int R, int KIND>
-struct Geo {
-    static constexpr int V = V16<T>::N;
-    static constexpr int VV = KIND == 0 ? V : (V > 1 ? V / 2 : 1);
-    // halo lanes per side: enough for R cells, and a whole number of 16-byte
-    // vectors so every bulk copy starts 16-byte aligned
-    static constexpr int A = V / VV;
-    static constexpr int HL = ((R + VV - 1) / VV + A - 1) / A * A;
-    static constexpr int W = 32 * VV;                 // cells held by the warp (with halo lanes)
-    static constexpr int SEG = (32 - 2 * HL) * VV;    // cells owned by the warp at most
-    static constexpr int Q = 2 * R + 1;
-    // ring layout per warp (elements): prologue rows of u (and Phi_x), then stages
-    static constexpr int NF = KIND == 0 ? 5 : 7;      // u_head, u_prev, c2, dw, ic, [phx_head, phz]
-    static constexpr int PRO = (KIND == 0 ? 1 : 2) * 2 * R * W;
-    static constexpr int STAGE = NF * W;
-    static constexpr int ELEMS = PRO + kStages * STAGE;
+// Ring geometry of one task kind.  All slot widths are whole 16-byte units, so
+// every bulk copy starts and ends 16-byte aligned (task z-bounds are multiples
+// of 4 cells, rows start 128-byte aligned).
+template <typename T, int R, int MODE, int KIND>
+struct Ring {
+    static constexpr int AL = 16 / (int)sizeof(T);              // elements per 16 bytes
+    static constexpr int V = KIND == 0 ? AL : (AL > 1 ? AL / 2 : 1);  // cells per lane
+    static constexpr int HZ = (R + AL - 1) / AL * AL;            // z-halo cells per side
+    static constexpr int NB = HZ / V;                            // halo vectors per side
+    static constexpr int SEG = 32 * V;                           // cells a task owns at most
+    static constexpr int WS = SEG + 2 * HZ;                      // slot with halo (elements)
+    static constexpr int A = MODE == kAdj && PGB_RING_AHEAD > 2 ? PGB_RING_AHEAD - 1 : PGB_RING_AHEAD;
+    static constexpr int NU = 2 * R + A;                         // x-ring slots
+    static constexpr bool PML = KIND == 1;
+    static constexpr int NPF = MODE == kAdj ? 4 : 2;             // centre rows per stage
+    static constexpr int PST = NPF * SEG + (PML ? WS : 0);       // stage (elements)
+    static constexpr int ELEMS = NU * WS + (PML ? NU * SEG : 0) + A * PST;
+    static_assert(A >= 1 && A <= 16, "the barrier block holds 16 mbarriers");
 };
 
-template <typename T, int R>
+template <typename T, int R, int MODE>
 struct WarpSmem {
-    static constexpr int e0 = Geo<T, R, 0>::ELEMS, e1 = Geo<T, R, 1>::ELEMS;
-    static constexpr int ELEMS = e0 > e1 ? e0 : e1;
-    static constexpr size_t per_warp = 128 + sizeof(T) * (size_t)ELEMS;  // barriers + ring
+    static constexpr int e0 = Ring<T, R, MODE, 0>::ELEMS, e1 = Ring<T, R, MODE, 1>::ELEMS;
+    static constexpr size_t per_warp = 128 + sizeof(T) * (size_t)(e0 > e1 ? e0 : e1);  // barriers + rings
     static constexpr size_t bytes = kWarps * per_warp;
+    static_assert(per_warp % 16 == 0, "warp regions stay 16-byte aligned");
 };
 
-template <typename T, int VV, int HL>
-__device__ __forceinline__ void zwindow(const Vec<T, VV>& c, T (&w)[(2 * HL + 1) * VV]) {
-#pragma unroll
-    for (int v = 0; v < VV; ++v) w[HL * VV + v] = c.v[v];
-#pragma unroll
-    for (int d = 1; d <= HL; ++d) {
-#pragma unroll
-        for (int v = 0; v < VV; ++v) {
-            w[(HL - d) * VV + v] = __shfl_up_sync(0xffffffffu, c.v[v], d);
-            w[(HL + d) * VV + v] = __shfl_down_sync(0xffffffffu, c.v[v], d);
-        }
-    }
-}
+// Pipeline position of a warp, carried across its tasks: the stage the next row
+// uses and that stage's mbarrier phase parity.
+struct Pipe {
+    int s;
+    uint32_t ph;
+};
 
 template <typename T, int R, int MODE, int KIND>
-__device__ __forceinline__ void sweep(const WaveParams<T>& p, unsigned char* wsm, const int shot, const int x0,
-                                      const int x1, const int zs, const int ze) {
-    using G = Geo<T, R, KIND>;
-    constexpr int VV = G::VV, HL = G::HL, W = G::W, Q = G::Q;
-    constexpr bool PML = KIND == 1;
-    constexpr int NWIN = (2 * HL + 1) * VV;
+__device__ __forceinline__ void sweep(const WaveParams<T>& p, unsigned char* wsm, Pipe& pp, const int shot,
+                                      const int x0, const int x1, const int zs, const int ze, bool& bad,
+                                      bool& late) {
+    using G = Ring<T, R, MODE, KIND>;
+    constexpr int V = G::V, HZ = G::HZ, NB = G::NB, SEG = G::SEG, WS = G::WS, A = G::A, NU = G::NU;
+    constexpr bool PML = G::PML;
+    constexpr int NW = (2 * NB + 1) * V;  // z-window of a lane
+    constexpr int C0 = NB * V;            // its centre
     uint64_t* bar = reinterpret_cast<uint64_t*>(wsm);
-    T* ring = reinterpret_cast<T*>(wsm + 128);
-    T* pro = ring;                    // 2R rows of u (then 2R rows of Phi_x)
-    T* stg0 = ring + G::PRO;          // stage s at stg0 + s*STAGE, field f at + f*W
+    T* uring = reinterpret_cast<T*>(wsm + 128);
+    T* xring = uring + NU * WS;           // Phi_x rows (PML tasks)
+    T* pring = xring + (PML ? NU * SEG : 0);
     const int lane = threadIdx.x & 31;
     const int niter = x1 - x0;
-    const int zw0 = zs - HL * VV;                         // first cell held by lane 0
-    const int zl = zw0 + lane * VV;                       // first cell of this lane's vector
-    const bool own = lane >= HL && lane < 32 - HL && zl < ze;
+    const int zl = zs + lane * V;
+    const bool own = zl < ze;
     const long long sh = (long long)shot * p.fstride;
     const T* ucur = p.u_cur + sh;
     T* uprev = p.u_prev + sh;
-    const bool zpad = PML && (zl < p.pzl || zl + VV - 1 >= p.nz - p.pzr);
-    auto xpad = [&](int x) { return x < p.pxl || x >= p.nx - p.pxr; };
+    const bool img = MODE == kAdj && p.image;
     auto rowoff = [&](int x) { return (long long)(x + kHalo) * p.ldz + kOZ; };
+    const int ncen = (ze - zs + G::AL - 1) / G::AL * G::AL;
+    const uint32_t bu = (uint32_t)(ncen + 2 * HZ) * sizeof(T);
+    const uint32_t bc = (uint32_t)ncen * sizeof(T);
+    const uint32_t bstage = bu + 2 * bc + (img ? 2 * bc : 0) + (PML ? bc + bu : 0);
 
-    // copy extents (elements): full lane range for u / Phi_z (clamped to the row
-    // storage), owned range for the rest; both multiples of 4 elements (16 bytes)
-    const int nfull = min(W, (p.ldz - kOZ - zw0) / 4 * 4);
-    const int own0 = HL * VV;                              // lane HL's offset in a slot
-    const int nown = ((min(ze, zs + G::SEG) - zs) + 3) / 4 * 4;
-
-    if (lane == 0) {
-        for (int s = 0; s < kStages; ++s) mbar_init(&bar[s], 1);
-        fence_mbar_init();
-    }
-    __syncwarp();
-
-    auto issue = [&](int i) {  // copies of iteration i (row x0 + i) into stage i % kStages
+    // copies for row x0 + i: u_k row x+R into x-ring slot `slot`, centre rows into stage s
+    auto issue = [&](int i, int s, int slot, uint32_t extra) {
         const int x = x0 + i;
-        const int s = i % kStages;
-        T* st = stg0 + s * G::STAGE;
-        uint32_t bytes = (uint32_t)(nfull + 2 * nown) * sizeof(T);
-        if (MODE == kAdj && p.image) bytes += 2u * nown * sizeof(T);
-        if (PML) bytes += (uint32_t)(nown + nfull) * sizeof(T);
-        if (i == 0) bytes += (uint32_t)(2 * R * nfull * (PML ? 2 : 1)) * sizeof(T);
-        mbar_arrive_expect_tx(&bar[s], bytes);
-        if (i == 0)
-            for (int j = 0; j < 2 * R; ++j) {
-                bulk_g2s(pro + j * W, ucur + rowoff(x0 - R + j) + zw0, nfull * sizeof(T), &bar[s]);
-                if (PML) bulk_g2s(pro + (2 * R + j) * W, p.phx_in + sh + rowoff(x0 - R + j) + zw0,
-                                  nfull * sizeof(T), &bar[s]);
-            }
-        bulk_g2s(st, ucur + rowoff(x + R) + zw0, nfull * sizeof(T), &bar[s]);
-        bulk_g2s(st + W + own0, uprev + rowoff(x) + zs, nown * sizeof(T), &bar[s]);
-        bulk_g2s(st + 2 * W + own0, p.c2 + rowoff(x) + zs, nown * sizeof(T), &bar[s]);
-        if (MODE == kAdj && p.image) {
-            bulk_g2s(st + 3 * W + own0, p.dw_in + sh + rowoff(x) + zs, nown * sizeof(T), &bar[s]);
-            bulk_g2s(st + 4 * W + own0, p.ic + sh + rowoff(x) + zs, nown * sizeof(T), &bar[s]);
+        T* st = pring + s * G::PST;
+        mbar_arrive_expect_tx(&bar[s], bstage + extra);
+        bulk_g2s(uring + slot * WS, ucur + rowoff(x + R) + zs - HZ, bu, &bar[s]);
+        bulk_g2s(st, uprev + rowoff(x) + zs, bc, &bar[s]);
+        bulk_g2s(st + SEG, p.c2 + rowoff(x) + zs, bc, &bar[s]);
+        if (img) {
+            bulk_g2s(st + 2 * SEG, p.dw_in + sh + rowoff(x) + zs, bc, &bar[s]);
+            bulk_g2s(st + 3 * SEG, p.ic + sh + rowoff(x) + zs, bc, &bar[s]);
         }
         if (PML) {
-            bulk_g2s(st + 5 * W + own0, p.phx_in + sh + rowoff(x + R) + zs, nown * sizeof(T), &bar[s]);
-            bulk_g2s(st + 6 * W, p.phz_in + sh + rowoff(x) + zw0, nfull * sizeof(T), &bar[s]);
+            bulk_g2s(xring + slot * SEG, p.phx_in + sh + rowoff(x + R) + zs, bc, &bar[s]);
+            bulk_g2s(st + G::NPF * SEG, p.phz_in + sh + rowoff(x) + zs - HZ, bu, &bar[s]);
         }
     };
     if (lane == 0) {
-        fence_proxy_async();
-        for (int i = 0; i < min(kStages, niter); ++i) issue(i);
+        fence_proxy_async();  // earlier generic reads of the rings before the new copies
+        // rows x0-R .. x0+R-1 ride on the first row's stage
+        issue(0, pp.s, 2 * R, 2 * R * (bu + (PML ? bc : 0)));
+        for (int j = 0; j < 2 * R; ++j) {
+            bulk_g2s(uring + j * WS, ucur + rowoff(x0 - R + j) + zs - HZ, bu, &bar[pp.s]);
+            if (PML) bulk_g2s(xring + j * SEG, p.phx_in + sh + rowoff(x0 - R + j) + zs, bc, &bar[pp.s]);
+        }
+        int s = pp.s;
+        for (int i = 1; i < min(A, niter); ++i) {
+            if (++s == A) s = 0;
+            issue(i, s, 2 * R + i, 0);
+        }
     }
 
     // per-lane constants
-    T sgz[VV], mgz[VV];
-    bool zok[VV], zpe[VV];
+    bool zok[V];
+    T sgz[V], mgz[V];
 #pragma unroll
-    for (int v = 0; v < VV; ++v) {
+    for (int v = 0; v < V; ++v) {
         const int z = zl + v;
         zok[v] = z > 0 && z < p.nz - 1;
-        zpe[v] = z < p.pzl || z >= p.nz - p.pzr;
-        sgz[v] = (PML && z >= 0 && z < p.nz) ? __ldg(p.sgz + z) : T(0);
-        mgz[v] = (PML && MODE == kRecomp && z >= 0 && z < p.nz) ? __ldg(p.mgz + z) : T(0);
+        sgz[v] = (PML && z < p.nz) ? __ldg(p.sgz + z) : T(0);
+        mgz[v] = (PML && MODE == kRecomp && z < p.nz) ? __ldg(p.mgz + z) : T(0);
     }
-    bool zpw[NWIN];  // padding test of each z-window element (PML tasks)
-#pragma unroll
-    for (int j = 0; j < NWIN; ++j) {
-        const int z = zl - HL * VV + j;
-        zpw[j] = z < p.pzl || z >= p.nz - p.pzr;
-    }
-    // combined Laplacian weights
-    T cx[R + 1], cz[R + 1];
+    T cx[R + 1], cz[R + 1];  // second-derivative weights with the grid spacing folded in
 #pragma unroll
     for (int m = 0; m <= R; ++m) {
         cx[m] = T(d2w(R, m)) * p.idx2;
@@ -198,185 +185,221 @@ __device__ __forceinline__ void sweep(const WaveParams<T>& p, unsigned char* wsm
     }
     const int* bx = p.inj.box + shot * 6;
     const bool inj_task = p.inj.on && bx[0] < x1 && bx[1] > x0 && bx[4] < ze && bx[5] > zs;
-    bool bad = false;
-    bool late = false;
 
-    Vec<T, VV> q[Q];
-    Vec<T, VV> qx[Q];  // Phi_x queue (PML tasks)
+    int b = 0;  // x-ring slot of row x - R
+    for (int i = 0; i < niter; ++i) {
+        const int x = x0 + i;
+        const int s = pp.s;
+        if (!mbar_wait_bounded(&bar[s], pp.ph, kPolls)) late = true;
+        const T* st = pring + s * G::PST;
+        auto slot = [&](int j) {  // x-ring slot of row x - R + j
+            const int t = b + j;
+            return t >= NU ? t - NU : t;
+        };
 
-    for (int ib = 0; ib < niter; ib += Q) {
+        // ---- every shared-memory read of this row --------------------------------
+        T w[NW];  // u_k row x around the lane's cells
+        {
+            const T* r = uring + slot(R) * WS + lane * V;
 #pragma unroll
-        for (int so = 0; so < Q; ++so) {
-            const int i = ib + so;
-            if (i >= niter) break;
-            const int x = x0 + i;
-            const int s = i % kStages;
-            const T* st = stg0 + s * G::STAGE;
-            if (!mbar_wait_bounded(&bar[s], (uint32_t)((i / kStages) & 1), kPolls)) late = true;
-            if (i == 0) {
+            for (int j = 0; j <= 2 * NB; ++j) {
+                const Vec<T, V> a = lds<T, V>(r + j * V);
 #pragma unroll
-                for (int j = 0; j < 2 * R; ++j) {
-                    q[(so + j) % Q] = lds<T, VV>(pro + j * W + lane * VV);
-                    if (PML) {
-                        Vec<T, VV> a = lds<T, VV>(pro + (2 * R + j) * W + lane * VV);
-                        const bool use = zpad || xpad(x0 - R + j);
-#pragma unroll
-                        for (int v = 0; v < VV; ++v) a.v[v] = use ? a.v[v] : T(0);
-                        qx[(so + j) % Q] = a;
-                    }
-                }
-            }
-            q[(so + 2 * R) % Q] = lds<T, VV>(st + lane * VV);
-            const Vec<T, VV> um = lds<T, VV>(st + W + lane * VV);
-            const Vec<T, VV> cc = lds<T, VV>(st + 2 * W + lane * VV);
-            Vec<T, VV> dwi, ici, pzc;
-            if (MODE == kAdj && p.image) {
-                dwi = lds<T, VV>(st + 3 * W + lane * VV);
-                ici = lds<T, VV>(st + 4 * W + lane * VV);
-            }
-            if (PML) {
-                Vec<T, VV> a = lds<T, VV>(st + 5 * W + lane * VV);
-                const bool use = zpad || xpad(x + R);
-#pragma unroll
-                for (int v = 0; v < VV; ++v) a.v[v] = use ? a.v[v] : T(0);
-                qx[(so + 2 * R) % Q] = a;
-                pzc = lds<T, VV>(st + 6 * W + lane * VV);
-            }
-            __syncwarp();  // every lane has read stage s: lane 0 may refill it
-            if (lane == 0 && i + kStages < niter) {
-                fence_proxy_async();
-                issue(i + kStages);
-            }
-
-            const Vec<T, VV>& qc = q[(so + R) % Q];
-            T w[NWIN];
-            zwindow<T, VV, HL>(qc, w);
-            T wp[NWIN];  // Phi_z window (PML tasks)
-            if (PML) {
-                zwindow<T, VV, HL>(pzc, wp);
-                const bool xp = xpad(x);
-#pragma unroll
-                for (int j = 0; j < NWIN; ++j) wp[j] = (xp || zpw[j]) ? wp[j] : T(0);
-            }
-            const bool xok = x > 0 && x < p.nx - 1;
-            const bool inj_row = inj_task && x >= bx[0] && x < bx[1];
-            Vec<T, VV> un, dwo, pxo, pzo, ico;
-            T sgx = T(0), mgx = T(0);
-            if (PML) {
-                sgx = __ldg(p.sgx + x);
-                if (MODE == kRecomp) mgx = __ldg(p.mgx + x);
-            }
-#pragma unroll
-            for (int v = 0; v < VV; ++v) {
-                const int z = zl + v;
-                const T uc = w[HL * VV + v];
-                // Laplacian in difference form: sum_m w_m ((u_+m - u_0) + (u_-m - u_0)),
-                // equal to the central stencil because the weights sum to zero, and free
-                // of the large cancellation of w_0 u_0 (the FP32 path depends on this)
-                T F = T(0);
-#pragma unroll
-                for (int m = 1; m <= R; ++m) {
-                    F += cx[m] * ((q[(so + R + m) % Q].v[v] - uc) + (q[(so + R - m) % Q].v[v] - uc));
-                    F += cz[m] * ((w[HL * VV + v + m] - uc) + (w[HL * VV + v - m] - uc));
-                }
-                if (inj_row && own && z < p.nz) F += inject_rhs(p.inj, bx, shot, x, z);
-                const T uo = um.v[v], c2 = cc.v[v];
-                const bool ok = xok && zok[v];
-                T unew;
-                if (PML) {
-                    T dpx = T(0), dpz = T(0), dx1 = T(0), dz1 = T(0);
-#pragma unroll
-                    for (int m = 1; m <= R; ++m) {
-                        const T a = T(d1w(R, m));
-                        dpx += a * (qx[(so + R + m) % Q].v[v] - qx[(so + R - m) % Q].v[v]);
-                        dpz += a * (wp[HL * VV + v + m] - wp[HL * VV + v - m]);
-                        dx1 += a * (q[(so + R + m) % Q].v[v] - q[(so + R - m) % Q].v[v]);
-                        dz1 += a * (w[HL * VV + v + m] - w[HL * VV + v - m]);
-                    }
-                    F += dpx * p.idx + dpz * p.idz;
-                    const T sx = sgx, sz = sgz[v];
-                    T ph_x = T(0), ph_z = T(0);
-                    if (sx != T(0) || sz != T(0)) {
-                        const T dudx = dx1 * p.idx, dudz = dz1 * p.idz;
-                        const T phx = qx[(so + R) % Q].v[v], phz = wp[HL * VV + v];
-                        ph_x = phx - p.dt * sx * phx + p.dt * (sz - sx) * dudx;
-                        ph_z = phz - p.dt * sz * phz + p.dt * (sx - sz) * dudz;
-                        const T fac1 = T(2) * p.dt2 / (T(2) + p.dt * (sx + sz));
-                        const T fac2 = c2 * F - (uo - T(2) * uc) * p.idt2 + (sx + sz) * uo * p.i2dt - (sx * sz) * uc;
-                        unew = fac1 * fac2;
-                    } else {
-                        unew = p.dt2 * c2 * F - (uo - T(2) * uc);
-                    }
-                    if (!ok) { unew = T(0); ph_x = T(0); ph_z = T(0); }
-                    pxo.v[v] = ph_x;
-                    pzo.v[v] = ph_z;
-                    if (MODE == kRecomp) {
-                        const T mz = mgz[v];
-                        const T d = c2 * F + ((mgx + mz) - (sx + sz)) * (unew - uo) * p.i2dt + (mgx * mz - sx * sz) * uc;
-                        dwo.v[v] = ok ? d : T(0);
-                    }
-                } else {
-                    unew = ok ? p.dt2 * c2 * F - (uo - T(2) * uc) : T(0);
-                    if (MODE == kRecomp) dwo.v[v] = ok ? c2 * F : T(0);
-                }
-                un.v[v] = unew;
-                if (MODE == kFwd) bad |= !isfinite(unew);
-                if (MODE == kAdj) ico.v[v] = ici.v[v] + uc * dwi.v[v];
-            }
-            if (own) {
-                const long long o = rowoff(x) + zl;
-                stg<T, VV>(uprev + o, un);
-                if (PML && (zpad || xpad(x))) {
-                    stg<T, VV>(p.phx_out + sh + o, pxo);
-                    stg<T, VV>(p.phz_out + sh + o, pzo);
-                }
-                if (MODE == kRecomp && p.dw_out) stg_cs<T, VV>(p.dw_out + sh + o, dwo);
-                if (MODE == kAdj && p.image) stg<T, VV>(p.ic + sh + o, ico);
+                for (int v = 0; v < V; ++v) w[j * V + v] = a.v[v];
             }
         }
-    }
-    if (p.err) {
-        if (MODE == kFwd && bad && own) atomicOr(p.err, PGB_ERR_NONFINITE);
-        if (late && lane == 0) atomicOr(p.err, PGB_ERR_TIMEOUT);
+        Vec<T, V> ux[2 * R];  // u_k rows x-R..x-1, x+1..x+R at the lane's cells
+#pragma unroll
+        for (int m = 1; m <= R; ++m) {
+            ux[R - m] = lds<T, V>(uring + slot(R - m) * WS + HZ + lane * V);
+            ux[R + m - 1] = lds<T, V>(uring + slot(R + m) * WS + HZ + lane * V);
+        }
+        const Vec<T, V> um = lds<T, V>(st + lane * V);
+        const Vec<T, V> cc = lds<T, V>(st + SEG + lane * V);
+        Vec<T, V> dwi, ici;
+        if (MODE == kAdj && img) {
+            dwi = lds<T, V>(st + 2 * SEG + lane * V);
+            ici = lds<T, V>(st + 3 * SEG + lane * V);
+        }
+        Vec<T, V> px[2 * R + 1];  // Phi_x rows x-R..x+R (PML tasks)
+        T wp[NW];                 // Phi_z row x around the lane's cells (PML tasks)
+        if (PML) {
+#pragma unroll
+            for (int j = 0; j <= 2 * R; ++j) px[j] = lds<T, V>(xring + slot(j) * SEG + lane * V);
+            const T* r = st + G::NPF * SEG + lane * V;
+#pragma unroll
+            for (int j = 0; j <= 2 * NB; ++j) {
+                const Vec<T, V> a = lds<T, V>(r + j * V);
+#pragma unroll
+                for (int v = 0; v < V; ++v) wp[j * V + v] = a.v[v];
+            }
+        }
+        __syncwarp();  // every lane has read stage s and row x-R: lane 0 may refill them
+        if (lane == 0 && i + A < niter) {
+            fence_proxy_async();
+            issue(i + A, s, b, 0);
+        }
+        if (++pp.s == A) { pp.s = 0; pp.ph ^= 1u; }
+        if (++b == NU) b = 0;
+
+        // ---- the update -------------------------------------------------------------
+        const bool xok = x > 0 && x < p.nx - 1;
+        const bool inj_row = inj_task && own && x >= bx[0] && x < bx[1];
+        T sgx = T(0), mgx = T(0);
+        if (PML) {
+            sgx = __ldg(p.sgx + x);
+            if (MODE == kRecomp) mgx = __ldg(p.mgx + x);
+        }
+        Vec<T, V> un, dwo, pxo, pzo, ico;
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+            const int z = zl + v;
+            const T uc = w[C0 + v];
+            // Laplacian in difference form: sum_m w_m ((u_+m - u_0) + (u_-m - u_0)),
+            // equal to the central stencil because the weights sum to zero, and free
+            // of the large cancellation of w_0 u_0 (the FP32 path depends on this)
+            T F = T(0);
+#pragma unroll
+            for (int m = 1; m <= R; ++m) {
+                F += cx[m] * ((ux[R + m - 1].v[v] - uc) + (ux[R - m].v[v] - uc));
+                F += cz[m] * ((w[C0 + v + m] - uc) + (w[C0 + v - m] - uc));
+            }
+            if (inj_row && z < p.nz) F += inject_rhs(p.inj, bx, shot, x, z);
+            const T uo = um.v[v], c2 = cc.v[v];
+            const bool ok = xok && zok[v];
+            T unew;
+            if (PML) {
+                T dpx = T(0), dpz = T(0), dx1 = T(0), dz1 = T(0);
+#pragma unroll
+                for (int m = 1; m <= R; ++m) {
+                    const T a = T(d1w(R, m));
+                    dpx += a * (px[R + m].v[v] - px[R - m].v[v]);
+                    dpz += a * (wp[C0 + v + m] - wp[C0 + v - m]);
+                    dx1 += a * (ux[R + m - 1].v[v] - ux[R - m].v[v]);
+                    dz1 += a * (w[C0 + v + m] - w[C0 + v - m]);
+                }
+                F += dpx * p.idx + dpz * p.idz;
+                const T sx = sgx, sz = sgz[v];
+                const T phx = px[R].v[v], phz = wp[C0 + v];
+                T ph_x = phx, ph_z = phz;  // carried where both sigmas vanish (_2D.h:172-176)
+                if (sx != T(0) || sz != T(0)) {
+                    const T dudx = dx1 * p.idx, dudz = dz1 * p.idz;
+                    ph_x = phx - p.dt * sx * phx + p.dt * (sz - sx) * dudx;
+                    ph_z = phz - p.dt * sz * phz + p.dt * (sx - sz) * dudz;
+                    const T fac1 = T(2) * p.dt2 / (T(2) + p.dt * (sx + sz));
+                    const T fac2 = c2 * F - (uo - T(2) * uc) * p.idt2 + (sx + sz) * uo * p.i2dt - (sx * sz) * uc;
+                    unew = fac1 * fac2;
+                } else {
+                    unew = p.dt2 * c2 * F - (uo - T(2) * uc);
+                }
+                if (!ok) { unew = T(0); ph_x = T(0); ph_z = T(0); }
+                pxo.v[v] = ph_x;
+                pzo.v[v] = ph_z;
+                if (MODE == kRecomp) {
+                    const T mz = mgz[v];
+                    const T d = c2 * F + ((mgx + mz) - (sx + sz)) * (unew - uo) * p.i2dt + (mgx * mz - sx * sz) * uc;
+                    dwo.v[v] = ok ? d : T(0);
+                }
+            } else {
+                unew = ok ? p.dt2 * c2 * F - (uo - T(2) * uc) : T(0);
+                if (MODE == kRecomp) dwo.v[v] = ok ? c2 * F : T(0);
+            }
+            un.v[v] = unew;
+            if (MODE == kFwd) bad |= own && !isfinite(unew);
+            if (MODE == kAdj) ico.v[v] = ici.v[v] + uc * dwi.v[v];
+        }
+        if (own) {
+            const long long o = rowoff(x) + zl;
+            stg<T, V>(uprev + o, un);
+            if (PML) {
+                stg<T, V>(p.phx_out + sh + o, pxo);
+                stg<T, V>(p.phz_out + sh + o, pzo);
+            }
+            if (MODE == kRecomp && p.dw_out) stg_cs<T, V>(p.dw_out + sh + o, dwo);
+            if (MODE == kAdj && img) stg<T, V>(p.ic + sh + o, ico);
+        }
     }
 }
 
 template <typename T, int R, int MODE>
 __global__ void __launch_bounds__(kWarps * 32) wave2d_warp_kernel(const WaveParams<T> p, const int* __restrict__ tasks,
-                                                                  int ntasks, int task_blocks) {
+                                                                  int ntasks, int rec_blocks) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    if ((int)blockIdx.x >= task_blocks) {
-        if (MODE == kFwd) record_block(p, blockIdx.x - task_blocks);
+    if ((int)blockIdx.x < rec_blocks) {
+        if (MODE == kFwd) record_block(p, blockIdx.x);
         return;
     }
-    const int warp = threadIdx.x >> 5;
-    const int gw = blockIdx.x * kWarps + warp;
-    if (gw >= ntasks * p.nshot) return;  // warp-uniform
-    const int shot = gw / ntasks;
-    const int* tk = tasks + 5 * (gw - shot * ntasks);
-    const int x0 = __ldg(tk), x1 = __ldg(tk + 1), zs = __ldg(tk + 2), ze = __ldg(tk + 3), kind = __ldg(tk + 4);
-    unsigned char* wsm = smem_raw + warp * WarpSmem<T, R>::per_warp;
-    if (kind == 0)
-        sweep<T, R, MODE, 0>(p, wsm, shot, x0, x1, zs, ze);
-    else
-        sweep<T, R, MODE, 1>(p, wsm, shot, x0, x1, zs, ze);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    unsigned char* wsm = smem_raw + warp * WarpSmem<T, R, MODE>::per_warp;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(wsm);
+    constexpr int A = Ring<T, R, MODE, 0>::A;
+    static_assert(A == Ring<T, R, MODE, 1>::A, "both kinds share the stage barriers");
+    if (lane == 0) {
+        for (int s = 0; s < A; ++s) mbar_init(&bar[s], 1);
+        fence_mbar_init();
+    }
+    __syncwarp();
+    const unsigned long long total = (unsigned long long)ntasks * (unsigned)p.nshot;
+    Pipe pp{0, 0u};
+    int issued[A];  // rows issued per stage (for the drain after an expired wait)
+    (void)issued;
+    bool bad = false, late = false;
+    for (;;) {
+        unsigned long long t = 0;
+        if (lane == 0) t = atomicAdd(p.task_ctr, 1ull) - p.task_base;
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= total) break;
+        const int shot = (int)(t / (unsigned)ntasks);
+        const int* tk = tasks + 5 * (int)(t - (unsigned long long)shot * ntasks);
+        const int x0 = __ldg(tk), x1 = __ldg(tk + 1), zs = __ldg(tk + 2), ze = __ldg(tk + 3), kind = __ldg(tk + 4);
+        if (kind == 0)
+            sweep<T, R, MODE, 0>(p, wsm, pp, shot, x0, x1, zs, ze, bad, late);
+        else
+            sweep<T, R, MODE, 1>(p, wsm, pp, shot, x0, x1, zs, ze, bad, late);
+    }
+    late = __any_sync(0xffffffffu, late);
+    if (late) {
+        // a stage whose wait expired may still have copies in flight: wait for the
+        // last phase of every stage (bounded) before the shared memory is released
+        // pp.s is the next stage to use; stage j's last armed phase has parity
+        // pp.ph for j < pp.s and pp.ph ^ 1 otherwise
+        for (int j = 0; j < A; ++j) mbar_wait_bounded(&bar[j], j < pp.s ? pp.ph : (pp.ph ^ 1u), kPolls);
+    }
+    if (p.err) {
+        if (MODE == kFwd && bad) atomicOr(p.err, PGB_ERR_NONFINITE);
+        if (late && lane == 0) atomicOr(p.err, PGB_ERR_TIMEOUT);
+    }
 }
 
 template <typename T, int R>
 void prep_warp() {
-    const int b = (int)WarpSmem<T, R>::bytes;
-    cudaFuncSetAttribute(wave2d_warp_kernel<T, R, kFwd>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
-    cudaFuncSetAttribute(wave2d_warp_kernel<T, R, kRecomp>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
-    cudaFuncSetAttribute(wave2d_warp_kernel<T, R, kAdj>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    cudaFuncSetAttribute(wave2d_warp_kernel<T, R, kFwd>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)WarpSmem<T, R, kFwd>::bytes);
+    cudaFuncSetAttribute(wave2d_warp_kernel<T, R, kRecomp>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)WarpSmem<T, R, kRecomp>::bytes);
+    cudaFuncSetAttribute(wave2d_warp_kernel<T, R, kAdj>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)WarpSmem<T, R, kAdj>::bytes);
+}
+
+template <typename T, int R, int MODE>
+int occupancy() {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, wave2d_warp_kernel<T, R, MODE>, kWarps * 32,
+                                                      WarpSmem<T, R, MODE>::bytes) != cudaSuccess)
+        n = 1;
+    return n > 0 ? n : 1;
 }
 
 }  // namespace
 
 template <typename T, int R, int MODE>
-void launch_wave2d_warp_tasks(const WaveParams<T>& p, const int* tasks, int ntasks, cudaStream_t s) {
-    const int task_blocks = (ntasks * p.nshot + kWarps - 1) / kWarps;
-    const int grid = task_blocks + (MODE == kFwd ? p.rec.blocks : 0);
-    wave2d_warp_kernel<T, R, MODE><<<grid, kWarps * 32, WarpSmem<T, R>::bytes, s>>>(p, tasks, ntasks, task_blocks);
+long long launch_wave2d_warp_tasks(const WaveParams<T>& p, const int* tasks, int ntasks, int blocks,
+                                   cudaStream_t s) {
+    const int rec = MODE == kFwd ? p.rec.blocks : 0;
+    wave2d_warp_kernel<T, R, MODE><<<rec + blocks, kWarps * 32, WarpSmem<T, R, MODE>::bytes, s>>>(p, tasks, ntasks,
+                                                                                                 rec);
+    // counter values the launch consumes: one per task plus one final fetch per warp
+    return (long long)ntasks * p.nshot + (long long)blocks * kWarps;
 }
 
 void wave2d_warp_prepare() {
@@ -386,20 +409,43 @@ void wave2d_warp_prepare() {
 
 int wave2d_warp_threads() { return kWarps * 32; }
 
-// widest z-range a task of each kind may own: (32 - 2*HL) * VV cells (same rule as Geo)
-int wave2d_warp_seg(int dtype_bytes, int order, int pml) {
-    const int V = 16 / dtype_bytes;
-    const int VV = pml ? (V > 1 ? V / 2 : 1) : V;
+// persistent blocks of one launch: resident blocks per SM x SMs, no more than the tasks need
+int wave2d_warp_blocks(int dtype_bytes, int order, int mode, long long tasks) {
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int R = order / 2;
-    const int A = V / VV;
-    const int HL = ((R + VV - 1) / VV + A - 1) / A * A;
-    return (32 - 2 * HL) * VV;
+    int occ = 1;
+#define PGB_OCC(TT, RR)                                                  \
+    occ = mode == kFwd ? occupancy<TT, RR, kFwd>()                       \
+        : mode == kRecomp ? occupancy<TT, RR, kRecomp>() : occupancy<TT, RR, kAdj>()
+    if (dtype_bytes == 4) {
+        switch (R) { case 1: PGB_OCC(float, 1); break; case 2: PGB_OCC(float, 2); break;
+                     case 3: PGB_OCC(float, 3); break; default: PGB_OCC(float, 4); break; }
+    } else {
+        switch (R) { case 1: PGB_OCC(double, 1); break; case 2: PGB_OCC(double, 2); break;
+                     case 3: PGB_OCC(double, 3); break; default: PGB_OCC(double, 4); break; }
+    }
+#undef PGB_OCC
+    const long long need = (tasks + kWarps - 1) / kWarps;
+    const long long have = (long long)occ * sms;
+    return (int)(need < have ? need : have);
 }
 
-#define PGB_INSTW(T, R)                                                                                   \
-    template void launch_wave2d_warp_tasks<T, R, kFwd>(const WaveParams<T>&, const int*, int, cudaStream_t);    \
-    template void launch_wave2d_warp_tasks<T, R, kRecomp>(const WaveParams<T>&, const int*, int, cudaStream_t); \
-    template void launch_wave2d_warp_tasks<T, R, kAdj>(const WaveParams<T>&, const int*, int, cudaStream_t);
+// widest z-range a task of each kind may own: 32 lanes x V cells (same rule as Ring)
+int wave2d_warp_seg(int dtype_bytes, int order, int pml) {
+    (void)order;
+    const int AL = 16 / dtype_bytes;
+    const int V = pml ? (AL > 1 ? AL / 2 : 1) : AL;
+    return 32 * V;
+}
+
+#define PGB_INSTW(T, R)                                                                                          \
+    template long long launch_wave2d_warp_tasks<T, R, kFwd>(const WaveParams<T>&, const int*, int, int,          \
+                                                            cudaStream_t);                                       \
+    template long long launch_wave2d_warp_tasks<T, R, kRecomp>(const WaveParams<T>&, const int*, int, int,       \
+                                                               cudaStream_t);                                    \
+    template long long launch_wave2d_warp_tasks<T, R, kAdj>(const WaveParams<T>&, const int*, int, int, cudaStream_t);
 PGB_INSTW(float, 1)
 PGB_INSTW(float, 2)
 PGB_INSTW(float, 3)

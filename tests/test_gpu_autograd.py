@@ -1,0 +1,64 @@
+"""torch.autograd entry (velocity -> misfit): chain rule against the reference
+gradient, and finite differences of the misfit (the reference's
+examples/temp/GradientTest.py checks the gradient the same way, by plots)."""
+import numpy as np
+import pytest
+
+import problems
+import pysit_gb300 as api
+
+pytestmark = pytest.mark.gpu
+
+
+def _observed(name, precision="double"):
+    import torch
+    m, shots, solver, C, C0 = problems.build(api, name, precision=precision)
+    api.generate_seismic_data(shots, solver, solver.ModelParameters(m, {"C": C}))
+    obs = torch.as_tensor(np.stack([s.receivers.data for s in shots]))
+    return m, shots, solver, C, C0, obs, solver.ts().copy()
+
+
+def test_autograd_gradient_equals_chain_rule_of_reference_gradient(golden):
+    import torch
+    from pysit_gb300.autograd import FWIMisfit
+    g = golden("o6")
+    m, shots, solver, C, C0, obs, ts = _observed("o6")
+    fwi = FWIMisfit(solver, shots, obs, ts)
+    c = torch.tensor(C0, dtype=torch.float64, requires_grad=True)
+    J = fwi(c)
+    J.backward()
+    assert float(J) == pytest.approx(float(g["objective"]), rel=1e-10)
+    gm = g["grad"].reshape(C0.shape)
+    # the reference gradient is the representer for the cell-volume inner product
+    expect = gm * np.prod(m.deltas) * (-2.0) * C0 ** -3
+    got = c.grad.numpy()
+    assert np.linalg.norm(got - expect) / np.linalg.norm(expect) < 1e-9
+
+
+def test_autograd_forward_without_grad_gives_the_misfit(golden):
+    import torch
+    from pysit_gb300.autograd import FWIMisfit
+    g = golden("o6")
+    m, shots, solver, C, C0, obs, ts = _observed("o6")
+    J = FWIMisfit(solver, shots, obs, ts)(torch.tensor(C0, dtype=torch.float64))
+    assert float(J) == pytest.approx(float(g["objective"]), rel=1e-10)
+
+
+@pytest.mark.parametrize("precision,tol", [("double", 2e-2), ("single", 3e-2)])
+def test_directional_derivative_matches_finite_difference(precision, tol):
+    import torch
+    from pysit_gb300.autograd import FWIMisfit
+    m, shots, solver, C, C0, obs, ts = _observed("o6", precision)
+    fwi = FWIMisfit(solver, shots, obs, ts)
+    x, z = m.mesh_coords()
+    # smooth bump in the shallow part, where C0 is below its maximum (dt stays fixed)
+    dC = 30.0 * np.exp(-((x - 260.0) ** 2 + (z - 120.0) ** 2) / (2 * 40.0 ** 2))
+    c = torch.tensor(C0, dtype=torch.float64, requires_grad=True)
+    fwi(c).backward()
+    gd = float((c.grad * torch.as_tensor(dC)).sum())
+    h = 0.5
+    with torch.no_grad():
+        jp = float(fwi(torch.tensor(C0 + h * dC)))
+        jm = float(fwi(torch.tensor(C0 - h * dC)))
+    fd = (jp - jm) / (2 * h)
+    assert abs(fd - gd) / abs(fd) < tol
