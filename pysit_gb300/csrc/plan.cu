@@ -189,9 +189,12 @@ struct PlanT final : public pysit_plan {
     int bz, tx, ntz, ntx;
     int nseg;
     bool warp2d = true;          // 2D: warp-task sweep (true) or bulk-copy row pipeline (false)
-    std::vector<int> tasks2d;    // [ntasks][5] warp tasks of the 2D sweep
-    int blocks2d[3] = {1, 1, 1}; // resident task blocks of the 2D sweep per mode (whole GPU)
-    unsigned long long ctr_next = 0;  // task-counter value the next 2D launch starts at
+    std::vector<int> tasks2d;    // [ntasks][5] warp tasks of the 2D sweep: interior first, then shell
+    int ntask2d[2] = {0, 0};     // tasks of each kind
+    int blocks2d[3][2] = {{1, 1}, {1, 1}, {1, 1}};  // resident task blocks per mode and kind (whole GPU)
+    unsigned long long ctr_next[2] = {0, 0};  // task-counter values the next 2D launch starts at
+    cudaStream_t aux = nullptr;  // second stream of the 2D step (shell kernel beside the interior one)
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     // ---- acquisition (host) ----------------------------------------------------
     std::vector<CSRBox> src_inj, rec_inj;
     std::vector<int> rec_rows;        // [nshots*nrec+1]
@@ -238,6 +241,9 @@ struct PlanT final : public pysit_plan {
         for (auto& kv : graphs)
             if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
         if (cap) cudaStreamDestroy(cap);
+        if (aux) cudaStreamDestroy(aux);
+        if (ev_fork) cudaEventDestroy(ev_fork);
+        if (ev_join) cudaEventDestroy(ev_join);
     }
 
     template <typename U>
@@ -357,10 +363,17 @@ struct PlanT final : public pysit_plan {
     }
     void build_tasks2d() {
         tasks2d.clear();
-        const int xa = pl[0] > 0 ? pl[0] + R : 0;
-        const int xb = pr[0] > 0 ? nx - pr[0] - R : nx;
-        int za = pl[2] > 0 ? (pl[2] + R + 3) / 4 * 4 : 0;
-        int zb = pr[2] > 0 ? (nz - pr[2] - R) / 4 * 4 : nz;
+        build_tasks2d_();
+        // interior tasks were added first
+        ntask2d[0] = ntask2d[1] = 0;
+        for (size_t t = 0; t < tasks2d.size(); t += 5) ++ntask2d[tasks2d[t + 4] ? 1 : 0];
+    }
+    void build_tasks2d_() {
+        // interior: R cells clear of the padding and off the outer (Dirichlet) ring
+        const int xa = pl[0] > 0 ? pl[0] + R : 1;
+        const int xb = pr[0] > 0 ? nx - pr[0] - R : nx - 1;
+        int za = ((pl[2] > 0 ? pl[2] + R : 1) + 3) / 4 * 4;
+        int zb = (pr[2] > 0 ? nz - pr[2] - R : nz - 1) / 4 * 4;
         if (xa >= xb || za >= zb) {  // no interior: the whole grid is shell
             add_tasks(0, nx, 0, nz, 1);
             return;
@@ -493,7 +506,7 @@ struct PlanT final : public pysit_plan {
         off.recw = take(std::max<size_t>(rec_ws.size(), 1) * sizeof(T));
         off.gpad = take((size_t)nx * ny * nz * sizeof(double));
         off.err = take(sizeof(int));
-        off.ctr = take(sizeof(unsigned long long));
+        off.ctr = take(2 * sizeof(unsigned long long));
         off.tasks = take(std::max<size_t>(tasks2d.size(), 1) * sizeof(int));
         off.partial = take(kRedBlocks * sizeof(double));
         off.rnorm = take(sizeof(double));
@@ -562,7 +575,11 @@ struct PlanT final : public pysit_plan {
         if (dim == 2) {
             wave2d_prepare();
             wave2d_warp_prepare();
-            for (int m = 0; m < 3; ++m) blocks2d[m] = wave2d_warp_blocks((int)sizeof(T), order, m, 1ll << 40);
+            for (int m = 0; m < 3; ++m)
+                for (int k = 0; k < 2; ++k) blocks2d[m][k] = wave2d_warp_blocks((int)sizeof(T), order, m, k);
+            if (!aux) PGB_CHECK_CUDA(cudaStreamCreateWithFlags(&aux, cudaStreamNonBlocking));
+            if (!ev_fork) PGB_CHECK_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+            if (!ev_join) PGB_CHECK_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
         }
         PGB_CHECK_CUDA(cudaGetLastError());
         model_set = false;
@@ -636,21 +653,49 @@ struct PlanT final : public pysit_plan {
         }
     }
 
+    // One 2D step: the interior kernel on s and the PML-shell kernel on the
+    // auxiliary stream, forked from and joined back into s (graph branches when
+    // captured), each a persistent grid drawing (shot, task) pairs from its counter.
+    template <int RR, int MODE>
+    void launch2d(const WaveParams<T>& p, cudaStream_t s) {
+        const int* tk = at<int>(off.tasks);
+        const long long wpb = wave2d_warp_threads() / 32;
+        WaveParams<T> q = p;
+        q.task_base = ctr_next[0];
+        q.task_base2 = ctr_next[1];
+        int nb[2];
+        for (int k = 0; k < 2; ++k) {
+            const long long need = ((long long)ntask2d[k] * p.nshot + wpb - 1) / wpb;
+            nb[k] = (int)std::min<long long>(need, blocks2d[MODE][k]);
+        }
+        const bool fork = ntask2d[1] > 0 && ntask2d[0] > 0;
+        if (fork) {
+            cudaEventRecord(ev_fork, s);
+            cudaStreamWaitEvent(aux, ev_fork, 0);
+            ctr_next[1] += launch_wave2d_warp_tasks<T, RR, MODE, 1>(q, tk + 5 * ntask2d[0], ntask2d[1], nb[1], aux);
+            ++launches;
+        }
+        if (ntask2d[0] > 0 || (MODE == kFwd && p.rec.blocks > 0)) {
+            ctr_next[0] += launch_wave2d_warp_tasks<T, RR, MODE, 0>(q, tk, ntask2d[0], ntask2d[0] ? nb[0] : 0, s);
+            ++launches;
+        }
+        if (fork) {
+            cudaEventRecord(ev_join, aux);
+            cudaStreamWaitEvent(s, ev_join, 0);
+        } else if (ntask2d[1] > 0) {
+            ctr_next[1] += launch_wave2d_warp_tasks<T, RR, MODE, 1>(q, tk + 5 * ntask2d[0], ntask2d[1], nb[1], s);
+            ++launches;
+        }
+    }
+
     void launch(const WaveParams<T>& p, int mode, cudaStream_t s) {
-        ++launches;
+        if (!(dim == 2 && warp2d)) ++launches;
 #define PGB_L(RR)                                                              \
     do {                                                                       \
         if (dim == 2 && warp2d) {                                              \
-            const int* tk = at<int>(off.tasks);                                \
-            const int nt = (int)(tasks2d.size() / 5);                          \
-            const long long wpb = wave2d_warp_threads() / 32;                  \
-            const long long need = ((long long)nt * p.nshot + wpb - 1) / wpb;  \
-            const int nb = (int)std::min<long long>(need, blocks2d[mode]);     \
-            WaveParams<T> q = p;                                               \
-            q.task_base = ctr_next;                                            \
-            if (mode == kFwd) ctr_next += launch_wave2d_warp_tasks<T, RR, kFwd>(q, tk, nt, nb, s);            \
-            else if (mode == kRecomp) ctr_next += launch_wave2d_warp_tasks<T, RR, kRecomp>(q, tk, nt, nb, s); \
-            else ctr_next += launch_wave2d_warp_tasks<T, RR, kAdj>(q, tk, nt, nb, s);                         \
+            if (mode == kFwd) launch2d<RR, kFwd>(p, s);                        \
+            else if (mode == kRecomp) launch2d<RR, kRecomp>(p, s);             \
+            else launch2d<RR, kAdj>(p, s);                                     \
         } else if (dim == 2) {                                                 \
             if (mode == kFwd) launch_wave2d<T, RR, kFwd>(p, bz, s);            \
             else if (mode == kRecomp) launch_wave2d<T, RR, kRecomp>(p, bz, s); \
@@ -791,8 +836,8 @@ struct PlanT final : public pysit_plan {
 
     // the 2D sweep's task counter restarts at zero with every run (eager or graph replay)
     void reset_task_counter(cudaStream_t s) {
-        cudaMemsetAsync(ws + off.ctr, 0, sizeof(unsigned long long), s);
-        ctr_next = 0;
+        cudaMemsetAsync(ws + off.ctr, 0, 2 * sizeof(unsigned long long), s);
+        ctr_next[0] = ctr_next[1] = 0;
     }
 
     void enqueue_forward(void* traces_out, cudaStream_t s) {

@@ -137,10 +137,12 @@ struct WaveParams {
     T* ic;                   // kAdj: imaging accumulator (shot 0 base)
     int image;               // kAdj: accumulate this step
     int* err;                // device error word (PGB_ERR_* bits), may be NULL
-    // 2D persistent sweep: task counter shared by the launches of one run; this
-    // launch's tasks are the counter values task_base .. task_base + tasks - 1
+    // 2D persistent sweep: task counters (interior, PML shell) shared by the
+    // launches of one run; this launch's tasks of kind 0 are the counter values
+    // task_base .. task_base + tasks - 1 of task_ctr[0], those of kind 1 start at
+    // task_base2 on task_ctr[1]
     unsigned long long* task_ctr;
-    unsigned long long task_base;
+    unsigned long long task_base, task_base2;
 };
 
 // ---- helpers shared by the 2D kernels ---------------------------------------
@@ -178,16 +180,17 @@ __device__ __forceinline__ void record_block(const WaveParams<T>& p, int rb) {
 
 template <typename T, int R, int MODE>
 void launch_wave2d(const WaveParams<T>& p, int bz, cudaStream_t s);
-// persistent-warp 2D sweep fed by shared-memory row rings; tasks = [ntasks][5]
-// ints (x0, x1, zs, ze, kind) of one shot, shared by all shots; `blocks` task
-// blocks.  Returns the number of task-counter values the launch consumes.
-template <typename T, int R, int MODE>
+// persistent-warp 2D sweep fed by shared-memory row rings, one task kind per
+// kernel (0 interior, 1 PML shell); tasks = [ntasks][5] ints (x0, x1, zs, ze,
+// kind) of one shot, shared by all shots; `blocks` task blocks.  Returns the
+// number of task-counter values the launch consumes.
+template <typename T, int R, int MODE, int KIND>
 long long launch_wave2d_warp_tasks(const WaveParams<T>& p, const int* tasks, int ntasks, int blocks,
                                    cudaStream_t s);
 int wave2d_warp_threads();
 int wave2d_warp_seg(int dtype_bytes, int order, int pml);
-// resident task blocks of the whole GPU for one (dtype, order, mode), at most `tasks`/warps
-int wave2d_warp_blocks(int dtype_bytes, int order, int mode, long long tasks);
+// resident task blocks of the whole GPU for one (dtype, order, mode, kind)
+int wave2d_warp_blocks(int dtype_bytes, int order, int mode, int kind);
 void wave2d_warp_prepare();
 template <typename T, int R, int MODE>
 void launch_wave3d(const WaveParams<T>& p, int bz, cudaStream_t s);

@@ -18,7 +18,7 @@
 // takes the next (shot, task) from a global counter until the launch's tasks
 // are used up, so no wave of blocks runs half empty at the end.  A task owns the
 // cells z in [zs, ze) of the rows x0..x1-1; lane L holds the V consecutive cells
-// from zs + L*V.  Per row x, lane 0 has already asked (A rows ahead) for
+// from zs + L*V.  Per row x, the warp has already asked (A rows ahead) for
 //   * row x+R of u_k, with an R-cell z-halo each side, into the warp's x-ring
 //     of 2R+A rows (the x-derivatives read rows x-R..x+R from it);
 //   * the centre rows of u_{k-1}, C^2 (and dWaveOp, ic for the adjoint; Phi_z
@@ -28,11 +28,13 @@
 // is one row (no unrolling), which keeps the kernel small enough for the
 // instruction cache.  Warps never wait for each other.
 // Task kinds (warp-uniform branch):
-//   kind 0  interior: at least R cells away from the padding, 16-byte lane
-//           vectors, no PML state;
-//   kind 1  PML shell: the padding and its R-wide rim, 8-byte lane vectors (more
+//   kind 0  interior: at least R cells away from the padding and off the outer
+//           (Dirichlet) ring, 16-byte lane vectors, no PML state, no masks;
+//   kind 1  PML shell: the padding and its R-wide rim, 2-cell lane vectors (more
 //           busy lanes on the narrow z-bands), Phi_x / Phi_z carried where both
 //           sigmas vanish as in the reference.
+// Each lane issues at most one of a row's bulk copies (per-lane copy descriptors),
+// and the arithmetic runs on cell pairs (packed f32x2 instructions in FP32).
 // Waits are bounded: on expiry the kernel sets the plan's error word, waits (again
 // bounded) for the copies it issued, and carries on.
 #include "tma.cuh"
@@ -79,7 +81,7 @@ __device__ __forceinline__ void stg_cs(T* p, const Vec<T, N>& r) {
 template <typename T, int R, int MODE, int KIND>
 struct Ring {
     static constexpr int AL = 16 / (int)sizeof(T);              // elements per 16 bytes
-    static constexpr int V = KIND == 0 ? AL : (AL > 1 ? AL / 2 : 1);  // cells per lane
+    static constexpr int V = KIND == 0 ? AL : 2;                 // cells per lane (pairs)
     static constexpr int HZ = (R + AL - 1) / AL * AL;            // z-halo cells per side
     static constexpr int NB = HZ / V;                            // halo vectors per side
     static constexpr int SEG = 32 * V;                           // cells a task owns at most
@@ -89,16 +91,43 @@ struct Ring {
     static constexpr bool PML = KIND == 1;
     static constexpr int NPF = MODE == kAdj ? 4 : 2;             // centre rows per stage
     static constexpr int PST = NPF * SEG + (PML ? WS : 0);       // stage (elements)
-    static constexpr int ELEMS = NU * WS + (PML ? NU * SEG : 0) + A * PST;
+    // u ring, Phi_x ring (same slot stride, centre at +HZ, so one row offset serves both), stages
+    static constexpr int ELEMS = NU * WS * (PML ? 2 : 1) + A * PST;
+    static constexpr size_t per_warp = 128 + sizeof(T) * (size_t)ELEMS;  // barriers + rings
+    static constexpr size_t bytes = kWarps * per_warp;
     static_assert(A >= 1 && A <= 16, "the barrier block holds 16 mbarriers");
+    static_assert(V % 2 == 0 && HZ % V == 0, "lanes hold whole pairs; halo in whole vectors");
+    static_assert(per_warp % 16 == 0, "warp regions stay 16-byte aligned");
 };
 
-template <typename T, int R, int MODE>
-struct WarpSmem {
-    static constexpr int e0 = Ring<T, R, MODE, 0>::ELEMS, e1 = Ring<T, R, MODE, 1>::ELEMS;
-    static constexpr size_t per_warp = 128 + sizeof(T) * (size_t)(e0 > e1 ? e0 : e1);  // barriers + rings
-    static constexpr size_t bytes = kWarps * per_warp;
-    static_assert(per_warp % 16 == 0, "warp regions stay 16-byte aligned");
+// Pair arithmetic: two neighbouring cells per operation.  FP32 uses the packed
+// f32x2 instructions (one issue slot for two cells, each lane rounded exactly
+// like the scalar operation); FP64 spells the pair out.
+template <typename T> struct PairOps;
+template <> struct PairOps<float> {
+    using P = float2;
+    static __device__ __forceinline__ P mk(float a, float b) { return make_float2(a, b); }
+    static __device__ __forceinline__ P dup(float a) { return make_float2(a, a); }
+    static __device__ __forceinline__ P add(P a, P b) { return __fadd2_rn(a, b); }
+    static __device__ __forceinline__ P sub(P a, P b) {
+        unsigned long long d;
+        asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(*reinterpret_cast<unsigned long long*>(&a)),
+            "l"(*reinterpret_cast<unsigned long long*>(&b)));
+        return *reinterpret_cast<P*>(&d);
+    }
+    static __device__ __forceinline__ P mul(P a, P b) { return __fmul2_rn(a, b); }
+    static __device__ __forceinline__ P fma(P a, P b, P c) { return __ffma2_rn(a, b, c); }
+};
+template <> struct PairOps<double> {
+    using P = double2;
+    static __device__ __forceinline__ P mk(double a, double b) { return make_double2(a, b); }
+    static __device__ __forceinline__ P dup(double a) { return make_double2(a, a); }
+    static __device__ __forceinline__ P add(P a, P b) { return make_double2(a.x + b.x, a.y + b.y); }
+    static __device__ __forceinline__ P sub(P a, P b) { return make_double2(a.x - b.x, a.y - b.y); }
+    static __device__ __forceinline__ P mul(P a, P b) { return make_double2(a.x * b.x, a.y * b.y); }
+    static __device__ __forceinline__ P fma(P a, P b, P c) {
+        return make_double2(::fma(a.x, b.x, c.x), ::fma(a.y, b.y, c.y));
+    }
 };
 
 // Pipeline position of a warp, carried across its tasks: the stage the next row
@@ -108,62 +137,89 @@ struct Pipe {
     uint32_t ph;
 };
 
+template <typename T> __device__ __forceinline__ T rcp_(T x);
+template <> __device__ __forceinline__ float rcp_(float x) { return __frcp_rn(x); }
+template <> __device__ __forceinline__ double rcp_(double x) { return 1.0 / x; }
+
 template <typename T, int R, int MODE, int KIND>
 __device__ __forceinline__ void sweep(const WaveParams<T>& p, unsigned char* wsm, Pipe& pp, const int shot,
                                       const int x0, const int x1, const int zs, const int ze, bool& bad,
                                       bool& late) {
     using G = Ring<T, R, MODE, KIND>;
+    using O = PairOps<T>;
+    using P = typename O::P;
     constexpr int V = G::V, HZ = G::HZ, NB = G::NB, SEG = G::SEG, WS = G::WS, A = G::A, NU = G::NU;
     constexpr bool PML = G::PML;
     constexpr int NW = (2 * NB + 1) * V;  // z-window of a lane
     constexpr int C0 = NB * V;            // its centre
-    uint64_t* bar = reinterpret_cast<uint64_t*>(wsm);
-    T* uring = reinterpret_cast<T*>(wsm + 128);
-    T* xring = uring + NU * WS;           // Phi_x rows (PML tasks)
-    T* pring = xring + (PML ? NU * SEG : 0);
+    constexpr int TB = (int)sizeof(T);
+    // byte layout of the warp region: barriers | u ring | Phi_x ring (PML) | stages
+    constexpr int SLOT = WS * TB, STG = G::PST * TB;
+    constexpr int OFF_U = 128, OFF_X = OFF_U + NU * SLOT, OFF_P = OFF_X + (PML ? NU * SLOT : 0);
+    const uint32_t bar0 = smem_u32(wsm);
     const int lane = threadIdx.x & 31;
+    const unsigned char* lb = wsm + lane * V * TB;  // this lane's first cell in any slot
     const int niter = x1 - x0;
     const int zl = zs + lane * V;
     const bool own = zl < ze;
     const long long sh = (long long)shot * p.fstride;
-    const T* ucur = p.u_cur + sh;
     T* uprev = p.u_prev + sh;
     const bool img = MODE == kAdj && p.image;
     auto rowoff = [&](int x) { return (long long)(x + kHalo) * p.ldz + kOZ; };
     const int ncen = (ze - zs + G::AL - 1) / G::AL * G::AL;
-    const uint32_t bu = (uint32_t)(ncen + 2 * HZ) * sizeof(T);
-    const uint32_t bc = (uint32_t)ncen * sizeof(T);
+    const uint32_t bu = (uint32_t)(ncen + 2 * HZ) * TB;
+    const uint32_t bc = (uint32_t)ncen * TB;
     const uint32_t bstage = bu + 2 * bc + (img ? 2 * bc : 0) + (PML ? bc + bu : 0);
 
-    // copies for row x0 + i: u_k row x+R into x-ring slot `slot`, centre rows into stage s
-    auto issue = [&](int i, int s, int slot, uint32_t extra) {
-        const int x = x0 + i;
-        T* st = pring + s * G::PST;
-        mbar_arrive_expect_tx(&bar[s], bstage + extra);
-        bulk_g2s(uring + slot * WS, ucur + rowoff(x + R) + zs - HZ, bu, &bar[s]);
-        bulk_g2s(st, uprev + rowoff(x) + zs, bc, &bar[s]);
-        bulk_g2s(st + SEG, p.c2 + rowoff(x) + zs, bc, &bar[s]);
-        if (img) {
-            bulk_g2s(st + 2 * SEG, p.dw_in + sh + rowoff(x) + zs, bc, &bar[s]);
-            bulk_g2s(st + 3 * SEG, p.ic + sh + rowoff(x) + zs, bc, &bar[s]);
+    // One bulk copy per lane and row.  Lane c's copy: field, row offset (R for
+    // the x-ring fields), halo or centre, and destination (x-ring slot or stage).
+    //   0 u_k -> u ring; 1 u_{k-1}, 2 C^2 -> stage; [3 dWaveOp, 4 ic -> stage];
+    //   [PML: Phi_x -> Phi_x ring; Phi_z (halo) -> stage]
+    const int ncp = 3 + (img ? 2 : 0) + (PML ? 2 : 0);
+    const T* csrc = nullptr;  // element of row 0 (x-ring fields: row R)
+    uint32_t cdst = 0, cstep = 0, cbytes = 0;
+    bool cring = false;
+    {
+        const int c = lane;
+        const int cpml = 3 + (img ? 2 : 0);
+        const uint32_t w0 = smem_u32(wsm);
+        if (c == 0) {
+            csrc = p.u_cur + sh + rowoff(R) + zs - HZ; cdst = w0 + OFF_U; cstep = SLOT; cbytes = bu; cring = true;
+        } else if (c == 1 || c == 2 || (img && (c == 3 || c == 4))) {
+            const T* f = c == 1 ? (const T*)uprev : c == 2 ? p.c2 : c == 3 ? p.dw_in + sh : (const T*)p.ic + sh;
+            csrc = f + rowoff(0) + zs; cdst = w0 + OFF_P + (c - 1) * SEG * TB; cstep = STG; cbytes = bc;
+        } else if (PML && c == cpml) {
+            csrc = p.phx_in + sh + rowoff(R) + zs; cdst = w0 + OFF_X + HZ * TB; cstep = SLOT; cbytes = bc;
+            cring = true;
+        } else if (PML && c == cpml + 1) {
+            csrc = p.phz_in + sh + rowoff(0) + zs - HZ; cdst = w0 + OFF_P + G::NPF * SEG * TB; cstep = STG;
+            cbytes = bu;
         }
-        if (PML) {
-            bulk_g2s(xring + slot * SEG, p.phx_in + sh + rowoff(x + R) + zs, bc, &bar[s]);
-            bulk_g2s(st + G::NPF * SEG, p.phz_in + sh + rowoff(x) + zs - HZ, bu, &bar[s]);
-        }
+    }
+    // row x0 + i into x-ring slot `slot` and stage s (the stage's expect_tx comes first)
+    auto copy_row = [&](int i, int s, int slot) {
+        if (lane < ncp)
+            bulk_g2s_s(cdst + (uint32_t)(cring ? slot : s) * cstep, csrc + (long long)(x0 + i) * p.ldz, cbytes,
+                       bar0 + 8u * s);
     };
-    if (lane == 0) {
-        fence_proxy_async();  // earlier generic reads of the rings before the new copies
-        // rows x0-R .. x0+R-1 ride on the first row's stage
-        issue(0, pp.s, 2 * R, 2 * R * (bu + (PML ? bc : 0)));
-        for (int j = 0; j < 2 * R; ++j) {
-            bulk_g2s(uring + j * WS, ucur + rowoff(x0 - R + j) + zs - HZ, bu, &bar[pp.s]);
-            if (PML) bulk_g2s(xring + j * SEG, p.phx_in + sh + rowoff(x0 - R + j) + zs, bc, &bar[pp.s]);
+    fence_proxy_async();  // earlier generic reads of the rings before the new copies
+    {
+        // the 2R leading rows x0-R .. x0+R-1 of u_k (and Phi_x) ride on the first row's stage
+        const uint32_t pro = 2 * R * (bu + (PML ? bc : 0));
+        if (lane == 0) mbar_arrive_expect_tx_s(bar0 + 8u * pp.s, bstage + pro);
+        if (lane < (PML ? 4 * R : 2 * R)) {
+            const int j = lane < 2 * R ? lane : lane - 2 * R;
+            const bool u = lane < 2 * R;
+            const T* src = (u ? p.u_cur + sh - HZ : p.phx_in + sh) + rowoff(x0 - R + j) + zs;
+            const uint32_t dst = smem_u32(wsm) + (u ? OFF_U : OFF_X + HZ * TB) + j * SLOT;
+            bulk_g2s_s(dst, src, u ? bu : bc, bar0 + 8u * pp.s);
         }
+        copy_row(0, pp.s, 2 * R);
         int s = pp.s;
         for (int i = 1; i < min(A, niter); ++i) {
             if (++s == A) s = 0;
-            issue(i, s, 2 * R + i, 0);
+            if (lane == 0) mbar_arrive_expect_tx_s(bar0 + 8u * s, bstage);
+            copy_row(i, s, 2 * R + i);
         }
     }
 
@@ -177,139 +233,172 @@ __device__ __forceinline__ void sweep(const WaveParams<T>& p, unsigned char* wsm
         sgz[v] = (PML && z < p.nz) ? __ldg(p.sgz + z) : T(0);
         mgz[v] = (PML && MODE == kRecomp && z < p.nz) ? __ldg(p.mgz + z) : T(0);
     }
-    T cx[R + 1], cz[R + 1];  // second-derivative weights with the grid spacing folded in
-#pragma unroll
-    for (int m = 0; m <= R; ++m) {
-        cx[m] = T(d2w(R, m)) * p.idx2;
-        cz[m] = T(d2w(R, m)) * p.idz2;
-    }
     const int* bx = p.inj.box + shot * 6;
-    const bool inj_task = p.inj.on && bx[0] < x1 && bx[1] > x0 && bx[4] < ze && bx[5] > zs;
+    const int bx0 = __ldg(bx), bx1 = __ldg(bx + 1);
+    const bool inj_task = p.inj.on && bx0 < x1 && bx1 > x0 && __ldg(bx + 4) < ze && __ldg(bx + 5) > zs;
 
-    int b = 0;  // x-ring slot of row x - R
-    for (int i = 0; i < niter; ++i) {
+    // weight pairs, built once per task
+    P wx[R + 1], wz[R + 1], a1[R + 1];
+#pragma unroll
+    for (int m = 1; m <= R; ++m) {
+        wx[m] = O::dup(T(d2w(R, m)) * p.idx2);
+        wz[m] = O::dup(T(d2w(R, m)) * p.idz2);
+        a1[m] = O::dup(T(d1w(R, m)));
+    }
+
+    // byte offsets of the slots holding rows x-R .. x+R (rotated every row)
+    int ra[2 * R + 1];
+#pragma unroll
+    for (int j = 0; j <= 2 * R; ++j) ra[j] = j * SLOT;
+    int b = 0;               // x-ring slot of row x - R
+    int nx_slot = 2 * R + 1; // x-ring slot of row x + R + 1
+    if (nx_slot >= NU) nx_slot -= NU;
+    long long o = rowoff(x0) + zl;  // element of the lane's first cell in row x
+    // sigma_x (and the mesh sigma_x) of the row, loaded one row ahead
+    T sx_n = PML ? __ldg(p.sgx + x0) : T(0);
+    T mx_n = PML && MODE == kRecomp ? __ldg(p.mgx + x0) : T(0);
+    for (int i = 0; i < niter; ++i, o += p.ldz) {
         const int x = x0 + i;
         const int s = pp.s;
-        if (!mbar_wait_bounded(&bar[s], pp.ph, kPolls)) late = true;
-        const T* st = pring + s * G::PST;
-        auto slot = [&](int j) {  // x-ring slot of row x - R + j
-            const int t = b + j;
-            return t >= NU ? t - NU : t;
-        };
+        if (!mbar_wait_bounded(reinterpret_cast<uint64_t*>(wsm) + s, pp.ph, kPolls)) late = true;
+        const unsigned char* sb = lb + OFF_P + s * STG;  // this lane in stage s
 
-        // ---- every shared-memory read of this row --------------------------------
+        // ---- the shared-memory reads of this row --------------------------------------
         T w[NW];  // u_k row x around the lane's cells
-        {
-            const T* r = uring + slot(R) * WS + lane * V;
 #pragma unroll
-            for (int j = 0; j <= 2 * NB; ++j) {
-                const Vec<T, V> a = lds<T, V>(r + j * V);
+        for (int j = 0; j <= 2 * NB; ++j) {
+            const Vec<T, V> a = lds<T, V>(reinterpret_cast<const T*>(lb + OFF_U + ra[R] + j * V * TB));
 #pragma unroll
-                for (int v = 0; v < V; ++v) w[j * V + v] = a.v[v];
-            }
+            for (int v = 0; v < V; ++v) w[j * V + v] = a.v[v];
         }
         Vec<T, V> ux[2 * R];  // u_k rows x-R..x-1, x+1..x+R at the lane's cells
 #pragma unroll
         for (int m = 1; m <= R; ++m) {
-            ux[R - m] = lds<T, V>(uring + slot(R - m) * WS + HZ + lane * V);
-            ux[R + m - 1] = lds<T, V>(uring + slot(R + m) * WS + HZ + lane * V);
+            ux[R - m] = lds<T, V>(reinterpret_cast<const T*>(lb + OFF_U + ra[R - m] + HZ * TB));
+            ux[R + m - 1] = lds<T, V>(reinterpret_cast<const T*>(lb + OFF_U + ra[R + m] + HZ * TB));
         }
-        const Vec<T, V> um = lds<T, V>(st + lane * V);
-        const Vec<T, V> cc = lds<T, V>(st + SEG + lane * V);
+        const Vec<T, V> um = lds<T, V>(reinterpret_cast<const T*>(sb));
+        const Vec<T, V> cc = lds<T, V>(reinterpret_cast<const T*>(sb + SEG * TB));
         Vec<T, V> dwi, ici;
         if (MODE == kAdj && img) {
-            dwi = lds<T, V>(st + 2 * SEG + lane * V);
-            ici = lds<T, V>(st + 3 * SEG + lane * V);
+            dwi = lds<T, V>(reinterpret_cast<const T*>(sb + 2 * SEG * TB));
+            ici = lds<T, V>(reinterpret_cast<const T*>(sb + 3 * SEG * TB));
         }
         Vec<T, V> px[2 * R + 1];  // Phi_x rows x-R..x+R (PML tasks)
         T wp[NW];                 // Phi_z row x around the lane's cells (PML tasks)
         if (PML) {
 #pragma unroll
-            for (int j = 0; j <= 2 * R; ++j) px[j] = lds<T, V>(xring + slot(j) * SEG + lane * V);
-            const T* r = st + G::NPF * SEG + lane * V;
+            for (int j = 0; j <= 2 * R; ++j)
+                px[j] = lds<T, V>(reinterpret_cast<const T*>(lb + OFF_X + ra[j] + HZ * TB));
 #pragma unroll
             for (int j = 0; j <= 2 * NB; ++j) {
-                const Vec<T, V> a = lds<T, V>(r + j * V);
+                const Vec<T, V> a = lds<T, V>(reinterpret_cast<const T*>(sb + G::NPF * SEG * TB + j * V * TB));
 #pragma unroll
                 for (int v = 0; v < V; ++v) wp[j * V + v] = a.v[v];
             }
         }
-        __syncwarp();  // every lane has read stage s and row x-R: lane 0 may refill them
-        if (lane == 0 && i + A < niter) {
-            fence_proxy_async();
-            issue(i + A, s, b, 0);
-        }
-        if (++pp.s == A) { pp.s = 0; pp.ph ^= 1u; }
-        if (++b == NU) b = 0;
-
-        // ---- the update -------------------------------------------------------------
+        // ---- the update, two cells at a time ----------------------------------------
         const bool xok = x > 0 && x < p.nx - 1;
-        const bool inj_row = inj_task && own && x >= bx[0] && x < bx[1];
-        T sgx = T(0), mgx = T(0);
-        if (PML) {
-            sgx = __ldg(p.sgx + x);
-            if (MODE == kRecomp) mgx = __ldg(p.mgx + x);
+        const bool inj_row = inj_task && own && x >= bx0 && x < bx1;
+        const T sx = sx_n, mgx = mx_n;
+        if (PML && i + 1 < niter) {
+            sx_n = __ldg(p.sgx + x + 1);
+            if (MODE == kRecomp) mx_n = __ldg(p.mgx + x + 1);
         }
+        (void)sx; (void)mgx;
         Vec<T, V> un, dwo, pxo, pzo, ico;
 #pragma unroll
-        for (int v = 0; v < V; ++v) {
-            const int z = zl + v;
-            const T uc = w[C0 + v];
+        for (int k = 0; k < V / 2; ++k) {
+            const int v0 = 2 * k;
+            auto pr = [&](const Vec<T, V>& a) { return O::mk(a.v[v0], a.v[v0 + 1]); };
+            auto pw = [&](const T* a, int d) { return O::mk(a[C0 + v0 + d], a[C0 + v0 + 1 + d]); };
+            const P uc = pw(w, 0);
             // Laplacian in difference form: sum_m w_m ((u_+m - u_0) + (u_-m - u_0)),
             // equal to the central stencil because the weights sum to zero, and free
             // of the large cancellation of w_0 u_0 (the FP32 path depends on this)
-            T F = T(0);
+            // (x and z accumulate separately: two short dependency chains)
+            P Fx = O::dup(T(0)), Fz = Fx;
 #pragma unroll
             for (int m = 1; m <= R; ++m) {
-                F += cx[m] * ((ux[R + m - 1].v[v] - uc) + (ux[R - m].v[v] - uc));
-                F += cz[m] * ((w[C0 + v + m] - uc) + (w[C0 + v - m] - uc));
+                Fx = O::fma(wx[m], O::add(O::sub(pr(ux[R + m - 1]), uc), O::sub(pr(ux[R - m]), uc)), Fx);
+                Fz = O::fma(wz[m], O::add(O::sub(pw(w, m), uc), O::sub(pw(w, -m), uc)), Fz);
             }
-            if (inj_row && z < p.nz) F += inject_rhs(p.inj, bx, shot, x, z);
-            const T uo = um.v[v], c2 = cc.v[v];
-            const bool ok = xok && zok[v];
-            T unew;
+            P F = O::add(Fx, Fz);
+            if (inj_row) {
+                F.x += inject_rhs(p.inj, bx, shot, x, zl + v0);
+                F.y += inject_rhs(p.inj, bx, shot, x, zl + v0 + 1);
+            }
+            const P uo = pr(um), c2 = pr(cc);
+            // interior tasks never touch the outer (Dirichlet) ring: no masks there
+            const bool ok0 = !PML || (xok && zok[v0]), ok1 = !PML || (xok && zok[v0 + 1]);
+            P unew;
             if (PML) {
-                T dpx = T(0), dpz = T(0), dx1 = T(0), dz1 = T(0);
+                P dpx = O::dup(T(0)), dpz = dpx, dx1 = dpx, dz1 = dpx;
 #pragma unroll
                 for (int m = 1; m <= R; ++m) {
-                    const T a = T(d1w(R, m));
-                    dpx += a * (px[R + m].v[v] - px[R - m].v[v]);
-                    dpz += a * (wp[C0 + v + m] - wp[C0 + v - m]);
-                    dx1 += a * (ux[R + m - 1].v[v] - ux[R - m].v[v]);
-                    dz1 += a * (w[C0 + v + m] - w[C0 + v - m]);
+                    const P a = a1[m];
+                    dpx = O::fma(a, O::sub(pr(px[R + m]), pr(px[R - m])), dpx);
+                    dpz = O::fma(a, O::sub(pw(wp, m), pw(wp, -m)), dpz);
+                    dx1 = O::fma(a, O::sub(pr(ux[R + m - 1]), pr(ux[R - m])), dx1);
+                    dz1 = O::fma(a, O::sub(pw(w, m), pw(w, -m)), dz1);
                 }
-                F += dpx * p.idx + dpz * p.idz;
-                const T sx = sgx, sz = sgz[v];
-                const T phx = px[R].v[v], phz = wp[C0 + v];
-                T ph_x = phx, ph_z = phz;  // carried where both sigmas vanish (_2D.h:172-176)
-                if (sx != T(0) || sz != T(0)) {
-                    const T dudx = dx1 * p.idx, dudz = dz1 * p.idz;
-                    ph_x = phx - p.dt * sx * phx + p.dt * (sz - sx) * dudx;
-                    ph_z = phz - p.dt * sz * phz + p.dt * (sx - sz) * dudz;
-                    const T fac1 = T(2) * p.dt2 / (T(2) + p.dt * (sx + sz));
-                    const T fac2 = c2 * F - (uo - T(2) * uc) * p.idt2 + (sx + sz) * uo * p.i2dt - (sx * sz) * uc;
-                    unew = fac1 * fac2;
-                } else {
-                    unew = p.dt2 * c2 * F - (uo - T(2) * uc);
-                }
-                if (!ok) { unew = T(0); ph_x = T(0); ph_z = T(0); }
-                pxo.v[v] = ph_x;
-                pzo.v[v] = ph_z;
+                F = O::add(F, O::fma(dpx, O::dup(p.idx), O::mul(dpz, O::dup(p.idz))));
+                // split-field PML update (_2D.h:157-170), branch-free: with both sigmas
+                // zero it reduces to the plain leapfrog update and carries Phi unchanged
+                const P szp = O::mk(sgz[v0], sgz[v0 + 1]);
+                const P dsx = O::dup(p.dt * sx), dsz = O::mul(O::dup(p.dt), szp);
+                const P S = O::add(O::dup(sx), szp);                     // sx + sz
+                const P phx = pr(px[R]), phz = pw(wp, 0);
+                // Phi' = Phi - dt s Phi + dt (s_other - s) du/dn
+                P ph_x = O::fma(O::mul(O::sub(dsz, dsx), O::dup(p.idx)), dx1, O::fma(dsx, O::mul(phx, O::dup(T(-1))), phx));
+                P ph_z = O::fma(O::mul(O::sub(dsx, dsz), O::dup(p.idz)), dz1, O::fma(dsz, O::mul(phz, O::dup(T(-1))), phz));
+                // u' = 2 dt^2 / (2 + dt S) * (C^2 F - (u_{k-1} - 2u)/dt^2 + S u_{k-1}/(2dt) - sx sz u)
+                const P den = O::fma(O::dup(p.dt), S, O::dup(T(2)));
+                const P fac1 = O::mul(O::dup(T(2) * p.dt2), O::mk(rcp_(den.x), rcp_(den.y)));
+                const P c2F = O::mul(c2, F);
+                P fac2 = O::fma(O::fma(O::dup(T(-2)), uc, uo), O::dup(-p.idt2), c2F);
+                fac2 = O::fma(O::mul(S, O::dup(p.i2dt)), uo, fac2);
+                fac2 = O::fma(O::mul(O::dup(-sx), szp), uc, fac2);
+                unew = O::mul(fac1, fac2);
+                if (!ok0) { unew.x = T(0); ph_x.x = T(0); ph_z.x = T(0); }
+                if (!ok1) { unew.y = T(0); ph_x.y = T(0); ph_z.y = T(0); }
+                pxo.v[v0] = ph_x.x; pxo.v[v0 + 1] = ph_x.y;
+                pzo.v[v0] = ph_z.x; pzo.v[v0 + 1] = ph_z.y;
                 if (MODE == kRecomp) {
-                    const T mz = mgz[v];
-                    const T d = c2 * F + ((mgx + mz) - (sx + sz)) * (unew - uo) * p.i2dt + (mgx * mz - sx * sz) * uc;
-                    dwo.v[v] = ok ? d : T(0);
+                    // dWaveOp = C^2 F + (sm - s)(u' - u_{k-1})/(2dt) + (smx smz - sx sz) u
+                    const P mzp = O::mk(mgz[v0], mgz[v0 + 1]);
+                    const P dS = O::sub(O::add(O::dup(mgx), mzp), S);
+                    const P dP = O::sub(O::mul(O::dup(mgx), mzp), O::mul(O::dup(sx), szp));
+                    P d = O::fma(O::mul(dS, O::dup(p.i2dt)), O::sub(unew, uo), c2F);
+                    d = O::fma(dP, uc, d);
+                    dwo.v[v0] = ok0 ? d.x : T(0);
+                    dwo.v[v0 + 1] = ok1 ? d.y : T(0);
                 }
             } else {
-                unew = ok ? p.dt2 * c2 * F - (uo - T(2) * uc) : T(0);
-                if (MODE == kRecomp) dwo.v[v] = ok ? c2 * F : T(0);
+                // u_{k+1} = dt^2 C^2 F - (u_{k-1} - 2 u_k)
+                const P q = O::fma(O::dup(T(-2)), uc, uo);
+                unew = O::fma(O::mul(O::dup(p.dt2), c2), F, O::mul(q, O::dup(T(-1))));
+                if (MODE == kRecomp) {
+                    const P d = O::mul(c2, F);
+                    dwo.v[v0] = d.x;
+                    dwo.v[v0 + 1] = d.y;
+                }
             }
-            un.v[v] = unew;
-            if (MODE == kFwd) bad |= own && !isfinite(unew);
-            if (MODE == kAdj) ico.v[v] = ici.v[v] + uc * dwi.v[v];
+            un.v[v0] = unew.x;
+            un.v[v0 + 1] = unew.y;
+            if (MODE == kAdj) {
+                const P ic = O::fma(uc, pr(dwi), pr(ici));
+                ico.v[v0] = ic.x;
+                ico.v[v0 + 1] = ic.y;
+            }
+        }
+        if (MODE == kFwd) {  // a NaN or Inf anywhere in the lane's cells survives the sum
+            T sum = T(0);
+#pragma unroll
+            for (int v = 0; v < V; ++v) sum += un.v[v];
+            bad |= own && !isfinite(sum);
         }
         if (own) {
-            const long long o = rowoff(x) + zl;
             stg<T, V>(uprev + o, un);
             if (PML) {
                 stg<T, V>(p.phx_out + sh + o, pxo);
@@ -318,49 +407,66 @@ __device__ __forceinline__ void sweep(const WaveParams<T>& p, unsigned char* wsm
             if (MODE == kRecomp && p.dw_out) stg_cs<T, V>(p.dw_out + sh + o, dwo);
             if (MODE == kAdj && img) stg<T, V>(p.ic + sh + o, ico);
         }
+
+        // ---- refill: every lane is done with stage s and row x-R -------------------
+        __syncwarp();
+        if (i + A < niter) {
+            fence_proxy_async();
+            if (lane == 0) mbar_arrive_expect_tx_s(bar0 + 8u * s, bstage);
+            copy_row(i + A, s, b);
+        }
+        if (++pp.s == A) { pp.s = 0; pp.ph ^= 1u; }
+#pragma unroll
+        for (int j = 0; j < 2 * R; ++j) ra[j] = ra[j + 1];
+        ra[2 * R] = nx_slot * SLOT;
+        if (++b == NU) b = 0;
+        if (++nx_slot == NU) nx_slot = 0;
     }
 }
 
-template <typename T, int R, int MODE>
-__global__ void __launch_bounds__(kWarps * 32) wave2d_warp_kernel(const WaveParams<T> p, const int* __restrict__ tasks,
-                                                                  int ntasks, int rec_blocks) {
+// Resident blocks per SM the register budget aims at (FP32): the interior path
+// fits five 4-warp blocks without spills, the PML shell four.
+template <typename T, int KIND>
+struct MinBlocks {
+    static constexpr int value = sizeof(T) == 4 ? (KIND == 0 ? 5 : 4) : 1;
+};
+
+template <typename T, int R, int MODE, int KIND>
+__global__ void __launch_bounds__(kWarps * 32, (MinBlocks<T, KIND>::value))
+    wave2d_warp_kernel(const WaveParams<T> p, const int* __restrict__ tasks, int ntasks, int rec_blocks) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     if ((int)blockIdx.x < rec_blocks) {
         if (MODE == kFwd) record_block(p, blockIdx.x);
         return;
     }
+    using G = Ring<T, R, MODE, KIND>;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    unsigned char* wsm = smem_raw + warp * WarpSmem<T, R, MODE>::per_warp;
+    unsigned char* wsm = smem_raw + warp * G::per_warp;
     uint64_t* bar = reinterpret_cast<uint64_t*>(wsm);
-    constexpr int A = Ring<T, R, MODE, 0>::A;
-    static_assert(A == Ring<T, R, MODE, 1>::A, "both kinds share the stage barriers");
+    constexpr int A = G::A;
     if (lane == 0) {
         for (int s = 0; s < A; ++s) mbar_init(&bar[s], 1);
         fence_mbar_init();
     }
     __syncwarp();
+    unsigned long long* ctr = p.task_ctr + KIND;
+    const unsigned long long base = KIND == 0 ? p.task_base : p.task_base2;
     const unsigned long long total = (unsigned long long)ntasks * (unsigned)p.nshot;
     Pipe pp{0, 0u};
-    int issued[A];  // rows issued per stage (for the drain after an expired wait)
-    (void)issued;
     bool bad = false, late = false;
     for (;;) {
         unsigned long long t = 0;
-        if (lane == 0) t = atomicAdd(p.task_ctr, 1ull) - p.task_base;
+        if (lane == 0) t = atomicAdd(ctr, 1ull) - base;
         t = __shfl_sync(0xffffffffu, t, 0);
         if (t >= total) break;
         const int shot = (int)(t / (unsigned)ntasks);
         const int* tk = tasks + 5 * (int)(t - (unsigned long long)shot * ntasks);
-        const int x0 = __ldg(tk), x1 = __ldg(tk + 1), zs = __ldg(tk + 2), ze = __ldg(tk + 3), kind = __ldg(tk + 4);
-        if (kind == 0)
-            sweep<T, R, MODE, 0>(p, wsm, pp, shot, x0, x1, zs, ze, bad, late);
-        else
-            sweep<T, R, MODE, 1>(p, wsm, pp, shot, x0, x1, zs, ze, bad, late);
+        sweep<T, R, MODE, KIND>(p, wsm, pp, shot, __ldg(tk), __ldg(tk + 1), __ldg(tk + 2), __ldg(tk + 3), bad, late);
     }
     late = __any_sync(0xffffffffu, late);
     if (late) {
         // a stage whose wait expired may still have copies in flight: wait for the
-        // last phase of every stage (bounded) before the shared memory is released
+        // last phase of every stage (bounded) before the shared memory is released.
         // pp.s is the next stage to use; stage j's last armed phase has parity
         // pp.ph for j < pp.s and pp.ph ^ 1 otherwise
         for (int j = 0; j < A; ++j) mbar_wait_bounded(&bar[j], j < pp.s ? pp.ph : (pp.ph ^ 1u), kPolls);
@@ -371,33 +477,38 @@ __global__ void __launch_bounds__(kWarps * 32) wave2d_warp_kernel(const WavePara
     }
 }
 
+template <typename T, int R, int MODE, int KIND>
+void prep_one() {
+    using G = Ring<T, R, MODE, KIND>;
+    cudaFuncSetAttribute(wave2d_warp_kernel<T, R, MODE, KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)G::bytes);
+    // all of the unified L1 / shared storage as shared memory: the rings are the working set
+    cudaFuncSetAttribute(wave2d_warp_kernel<T, R, MODE, KIND>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         (int)cudaSharedmemCarveoutMaxShared);
+}
 template <typename T, int R>
 void prep_warp() {
-    cudaFuncSetAttribute(wave2d_warp_kernel<T, R, kFwd>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)WarpSmem<T, R, kFwd>::bytes);
-    cudaFuncSetAttribute(wave2d_warp_kernel<T, R, kRecomp>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)WarpSmem<T, R, kRecomp>::bytes);
-    cudaFuncSetAttribute(wave2d_warp_kernel<T, R, kAdj>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)WarpSmem<T, R, kAdj>::bytes);
+    prep_one<T, R, kFwd, 0>(); prep_one<T, R, kRecomp, 0>(); prep_one<T, R, kAdj, 0>();
+    prep_one<T, R, kFwd, 1>(); prep_one<T, R, kRecomp, 1>(); prep_one<T, R, kAdj, 1>();
 }
 
-template <typename T, int R, int MODE>
+template <typename T, int R, int MODE, int KIND>
 int occupancy() {
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, wave2d_warp_kernel<T, R, MODE>, kWarps * 32,
-                                                      WarpSmem<T, R, MODE>::bytes) != cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, wave2d_warp_kernel<T, R, MODE, KIND>, kWarps * 32,
+                                                      Ring<T, R, MODE, KIND>::bytes) != cudaSuccess)
         n = 1;
     return n > 0 ? n : 1;
 }
 
 }  // namespace
 
-template <typename T, int R, int MODE>
+template <typename T, int R, int MODE, int KIND>
 long long launch_wave2d_warp_tasks(const WaveParams<T>& p, const int* tasks, int ntasks, int blocks,
                                    cudaStream_t s) {
-    const int rec = MODE == kFwd ? p.rec.blocks : 0;
-    wave2d_warp_kernel<T, R, MODE><<<rec + blocks, kWarps * 32, WarpSmem<T, R, MODE>::bytes, s>>>(p, tasks, ntasks,
-                                                                                                 rec);
+    const int rec = MODE == kFwd && KIND == 0 ? p.rec.blocks : 0;
+    wave2d_warp_kernel<T, R, MODE, KIND>
+        <<<rec + blocks, kWarps * 32, Ring<T, R, MODE, KIND>::bytes, s>>>(p, tasks, ntasks, rec);
     // counter values the launch consumes: one per task plus one final fetch per warp
     return (long long)ntasks * p.nshot + (long long)blocks * kWarps;
 }
@@ -409,16 +520,18 @@ void wave2d_warp_prepare() {
 
 int wave2d_warp_threads() { return kWarps * 32; }
 
-// persistent blocks of one launch: resident blocks per SM x SMs, no more than the tasks need
-int wave2d_warp_blocks(int dtype_bytes, int order, int mode, long long tasks) {
+// persistent blocks of one launch: resident blocks per SM x SMs
+int wave2d_warp_blocks(int dtype_bytes, int order, int mode, int kind) {
     int dev = 0, sms = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int R = order / 2;
     int occ = 1;
-#define PGB_OCC(TT, RR)                                                  \
-    occ = mode == kFwd ? occupancy<TT, RR, kFwd>()                       \
-        : mode == kRecomp ? occupancy<TT, RR, kRecomp>() : occupancy<TT, RR, kAdj>()
+#define PGB_OCC(TT, RR)                                                                          \
+    occ = kind == 0 ? (mode == kFwd ? occupancy<TT, RR, kFwd, 0>()                               \
+                       : mode == kRecomp ? occupancy<TT, RR, kRecomp, 0>() : occupancy<TT, RR, kAdj, 0>()) \
+                    : (mode == kFwd ? occupancy<TT, RR, kFwd, 1>()                               \
+                       : mode == kRecomp ? occupancy<TT, RR, kRecomp, 1>() : occupancy<TT, RR, kAdj, 1>())
     if (dtype_bytes == 4) {
         switch (R) { case 1: PGB_OCC(float, 1); break; case 2: PGB_OCC(float, 2); break;
                      case 3: PGB_OCC(float, 3); break; default: PGB_OCC(float, 4); break; }
@@ -427,25 +540,24 @@ int wave2d_warp_blocks(int dtype_bytes, int order, int mode, long long tasks) {
                      case 3: PGB_OCC(double, 3); break; default: PGB_OCC(double, 4); break; }
     }
 #undef PGB_OCC
-    const long long need = (tasks + kWarps - 1) / kWarps;
-    const long long have = (long long)occ * sms;
-    return (int)(need < have ? need : have);
+    return occ * sms;
 }
 
 // widest z-range a task of each kind may own: 32 lanes x V cells (same rule as Ring)
 int wave2d_warp_seg(int dtype_bytes, int order, int pml) {
     (void)order;
-    const int AL = 16 / dtype_bytes;
-    const int V = pml ? (AL > 1 ? AL / 2 : 1) : AL;
+    const int V = pml ? 2 : 16 / dtype_bytes;
     return 32 * V;
 }
 
-#define PGB_INSTW(T, R)                                                                                          \
-    template long long launch_wave2d_warp_tasks<T, R, kFwd>(const WaveParams<T>&, const int*, int, int,          \
-                                                            cudaStream_t);                                       \
-    template long long launch_wave2d_warp_tasks<T, R, kRecomp>(const WaveParams<T>&, const int*, int, int,       \
+#define PGB_INSTW1(T, R, K)                                                                                     \
+    template long long launch_wave2d_warp_tasks<T, R, kFwd, K>(const WaveParams<T>&, const int*, int, int,       \
                                                                cudaStream_t);                                    \
-    template long long launch_wave2d_warp_tasks<T, R, kAdj>(const WaveParams<T>&, const int*, int, int, cudaStream_t);
+    template long long launch_wave2d_warp_tasks<T, R, kRecomp, K>(const WaveParams<T>&, const int*, int, int,    \
+                                                                  cudaStream_t);                                 \
+    template long long launch_wave2d_warp_tasks<T, R, kAdj, K>(const WaveParams<T>&, const int*, int, int,       \
+                                                               cudaStream_t);
+#define PGB_INSTW(T, R) PGB_INSTW1(T, R, 0) PGB_INSTW1(T, R, 1)
 PGB_INSTW(float, 1)
 PGB_INSTW(float, 2)
 PGB_INSTW(float, 3)
