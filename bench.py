@@ -34,6 +34,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "FWI gradient shots/s, batched adjoint vs plain, 1xGB300 at <=1e-3 rel err; Gcell/s"
+# DRAM bytes (read + write) per launch of each 2D step, from an ncu capture of the
+# same kernels (profiles/); None where no capture backs a number
+TRAFFIC = {"forward": None, "recompute": None, "adjoint": None}
 
 
 def _peaks():
@@ -229,6 +232,27 @@ def main():
     clocks = _clock_summary(clk, local) if rank == 0 else None
     launches = plan.launches() * args.steps
     rn = float(plan.rnorm2.item())
+
+    # ---- per-kernel roofline: each step kernel timed alone with CUDA events ------------
+    # (one launch = one 2D step of a shot group: interior + PML-shell kernels)
+    # algorithmic bytes per cell: forward 4w interior / 8w PML; recompute +w (dWaveOp
+    # out); adjoint +3w (dWaveOp in, imaging accumulator in and out)
+    extra = {"forward": 0, "recompute": 1, "adjoint": 3}
+    modes = {}
+    nrep = max(64, min(512, solver.nsteps))
+    for mode, name in enumerate(("forward", "recompute", "adjoint")):
+        plan.step_loop(mode, 16)
+        torch.cuda.synchronize()
+        e0.record()
+        plan.step_loop(mode, nrep)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / nrep
+        nb = w * ((4 + extra[name]) * n_int + (8 + extra[name]) * n_pml) * plan.shots_per_launch
+        modes[name] = {"launch_ms": ms, "bytes_per_launch": nb, "achieved_gbs": nb / (ms * 1e-3) / 1e9,
+                       "kernel_launches_per_step": plan.launches() // nrep}
+    if plan.status():
+        raise RuntimeError("device status flags set during the kernel timing")
     del plan
     torch.cuda.empty_cache()
     if world > 1:
@@ -258,6 +282,8 @@ def main():
 
     cells_per_grad = 3 * n_all * solver.nsteps * args.shots
     peak, peak_kind = _peaks()
+    dom_name = max(modes, key=lambda k: modes[k]["launch_ms"])  # each mode runs nsteps times per gradient
+    dom = modes[dom_name]
     line = {"metric": METRIC, "value": world * args.shots / t_grad, "unit": "shots/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_grad, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, no dataset)",
@@ -265,10 +291,14 @@ def main():
             "gcell_per_s": world * cells_per_grad / t_grad / 1e9,
             "e2e": {"value": world * args.shots / t_e2e, "unit": "shots/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
-                         "kernel": "wave2d forward step (kFwd)", "bytes_per_launch": bytes_per_launch,
-                         "launch_ms": fwd_launch_ms, "fwd_gcell_per_s": fwd_gcells},
+            "roofline": {"bound": "hbm", "achieved": dom["achieved_gbs"], "peak": peak, "unit": "GB/s",
+                         "frac": dom["achieved_gbs"] / peak, "traffic": TRAFFIC.get(dom_name), "peak_kind": peak_kind,
+                         "kernel": f"2D {dom_name} step (interior + PML-shell kernels)",
+                         "bytes_per_launch": dom["bytes_per_launch"], "launch_ms": dom["launch_ms"],
+                         "modes": {k: {"launch_ms": v["launch_ms"], "achieved_gbs": v["achieved_gbs"],
+                                       "frac": v["achieved_gbs"] / peak} for k, v in modes.items()},
+                         "forward_graph": {"launch_ms": fwd_launch_ms, "achieved_gbs": achieved,
+                                           "gcell_per_s": fwd_gcells}},
             "gpu_launches": launches, "misfit_rnorm2": rn, "clocks": clocks}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(nsample=args.cpu_sample, scale=args.scale, nsteps_full=args.nsteps)

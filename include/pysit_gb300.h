@@ -199,6 +199,14 @@ int pysit_misfit_per_shot_noalloc(int dtype, const void* dobs, const void* dsim,
 /* Number of kernel launches the last forward/gradient/misfit call issued. */
 int pysit_plan_last_launch_count(const pysit_plan* plan, int64_t* launches);
 
+/* Benchmarking aid, no counterpart in the reference: enqueues `nsteps` launches
+ * of one step kernel (mode 0 forward, 1 forward recompute writing dWaveOp,
+ * 2 adjoint with imaging) of the first shot group on the plan's own buffers, so
+ * that a caller can time one kernel with events on `stream`.  The wavefield
+ * buffers keep evolving from whatever the previous run left; nothing is
+ * returned and the next forward/gradient call starts from scratch. */
+int pysit_plan_step_loop(pysit_plan* plan, int mode, int nsteps, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

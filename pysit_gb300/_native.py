@@ -79,6 +79,7 @@ _PROTOS = {
     "pysit_plan_status": (_i, [_vp, C.POINTER(_i), _vp]),
     "pysit_misfit_per_shot_noalloc": (_i, [_i, _vp, _vp, _i, C.c_int64, _vp, _vp, _vp]),
     "pysit_plan_last_launch_count": (_i, [_vp, C.POINTER(C.c_int64)]),
+    "pysit_plan_step_loop": (_i, [_vp, _i, _i, _vp]),
 }
 
 _lib = None

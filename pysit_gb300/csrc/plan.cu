@@ -55,6 +55,38 @@ __global__ void set_c2_kernel(const double* __restrict__ C, int nx, int ny, int 
     }
 }
 
+// Injection term of one 2D step added after the stencil kernels:
+//     u_{k+1} += fac C^2 rhs,   fac = dt^2, or 2 dt^2 / (2 + dt (sx + sz)) where a sigma is nonzero,
+// the factor the reference's update applies to C^2 (rhs + ...) (_2D.h:157-179); the update is
+// linear in rhs, so adding it afterwards equals injecting it inside the stencil.  One thread per
+// (shot, cell of the shot's injection box); cells of the outer ring are left alone, as the
+// reference skips them.  Used for wide operators (the adjoint source at every receiver), whose
+// per-cell tap walk would stall the stencil's row loop.
+template <typename T>
+__global__ void inject_scatter2d_kernel(const WaveParams<T> p, int cells_max) {
+    const long long n = (long long)p.nshot * cells_max;
+    for (long long id = blockIdx.x * (long long)blockDim.x + threadIdx.x; id < n;
+         id += (long long)gridDim.x * blockDim.x) {
+        const int shot = (int)(id / cells_max), c = (int)(id - (long long)shot * cells_max);
+        const int* bx = p.inj.box + shot * 6;
+        const int bzw = bx[5] - bx[4];
+        if (bzw <= 0 || c >= (bx[1] - bx[0]) * bzw) continue;
+        const int x = bx[0] + c / bzw, z = bx[4] + c % bzw;
+        if (x <= 0 || x >= p.nx - 1 || z <= 0 || z >= p.nz - 1) continue;
+        const T rhs = inject_rhs(p.inj, bx, shot, x, z);
+        const T sx = p.sgx[x], sz = p.sgz[z];
+        const T fac = (sx != T(0) || sz != T(0)) ? T(2) * p.dt2 / (T(2) + p.dt * (sx + sz)) : p.dt2;
+        const long long o = foff2(p, x, z);
+        p.u_prev[(long long)shot * p.fstride + o] += fac * p.c2[o] * rhs;
+    }
+}
+
+// trace recorder as a kernel of its own (runs beside the stencil kernels: it only reads u_k)
+template <typename T>
+__global__ void record_kernel(const WaveParams<T> p) {
+    record_block(p, blockIdx.x);
+}
+
 constexpr int kRedBlocks = 1024;
 constexpr int kRedThreads = 256;
 
@@ -169,6 +201,7 @@ struct pysit_plan {
     virtual int gradient(const void* dobs, double* grad, double* rnorm2, void* traces,
                          cudaStream_t s, bool with_grad, bool migrate) = 0;
     virtual int status(int* flags, cudaStream_t s) = 0;
+    virtual int step_loop(int mode, int nsteps, cudaStream_t s) = 0;
     int64_t last_launches = 0;
 };
 
@@ -197,6 +230,7 @@ struct PlanT final : public pysit_plan {
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     // ---- acquisition (host) ----------------------------------------------------
     std::vector<CSRBox> src_inj, rec_inj;
+    int rec_box_max = 0;              // largest receiver injection box (cells) over the shots
     std::vector<int> rec_rows;        // [nshots*nrec+1]
     std::vector<long long> rec_off;   // internal offsets
     std::vector<double> rec_ws;       // sampling weights
@@ -295,6 +329,9 @@ struct PlanT final : public pysit_plan {
         rc = build_injection(d.rec_tap_ptr, d.rec_tap_cell, d.rec_tap_point, d.rec_tap_winject, nrec,
                              rec_inj, "receiver");
         if (rc) return rc;
+        rec_box_max = 0;
+        for (auto& b : rec_inj)
+            rec_box_max = std::max(rec_box_max, (b.box[1] - b.box[0]) * (b.box[3] - b.box[2]) * (b.box[5] - b.box[4]));
         rc = build_recording(d);
         if (rc) return rc;
         src_amp.assign(d.src_amp, d.src_amp + (size_t)nshots * nsteps * nsrc);
@@ -668,22 +705,38 @@ struct PlanT final : public pysit_plan {
             const long long need = ((long long)ntask2d[k] * p.nshot + wpb - 1) / wpb;
             nb[k] = (int)std::min<long long>(need, blocks2d[MODE][k]);
         }
+        // the adjoint source covers every receiver: added by a scatter kernel after the step
+        const bool scatter = MODE == kAdj && q.inj.on && rec_box_max > 0;
+        if (scatter) q.inj.on = 0;
+        const bool rec = MODE == kFwd && q.rec.blocks > 0;
+        const int recb = q.rec.blocks;
+        q.rec.blocks = 0;
         const bool fork = ntask2d[1] > 0 && ntask2d[0] > 0;
+        cudaStream_t side = fork ? aux : s;
         if (fork) {
             cudaEventRecord(ev_fork, s);
             cudaStreamWaitEvent(aux, ev_fork, 0);
-            ctr_next[1] += launch_wave2d_warp_tasks<T, RR, MODE, 1>(q, tk + 5 * ntask2d[0], ntask2d[1], nb[1], aux);
+        }
+        if (rec) {
+            record_kernel<T><<<recb, bz, 0, side>>>(q);
             ++launches;
         }
-        if (ntask2d[0] > 0 || (MODE == kFwd && p.rec.blocks > 0)) {
-            ctr_next[0] += launch_wave2d_warp_tasks<T, RR, MODE, 0>(q, tk, ntask2d[0], ntask2d[0] ? nb[0] : 0, s);
+        if (ntask2d[1] > 0) {
+            ctr_next[1] += launch_wave2d_warp_tasks<T, RR, MODE, 1>(q, tk + 5 * ntask2d[0], ntask2d[1], nb[1], side);
+            ++launches;
+        }
+        if (ntask2d[0] > 0) {
+            ctr_next[0] += launch_wave2d_warp_tasks<T, RR, MODE, 0>(q, tk, ntask2d[0], nb[0], s);
             ++launches;
         }
         if (fork) {
             cudaEventRecord(ev_join, aux);
             cudaStreamWaitEvent(s, ev_join, 0);
-        } else if (ntask2d[1] > 0) {
-            ctr_next[1] += launch_wave2d_warp_tasks<T, RR, MODE, 1>(q, tk + 5 * ntask2d[0], ntask2d[1], nb[1], s);
+        }
+        if (scatter) {
+            q.inj.on = 1;
+            const long long n = (long long)q.nshot * rec_box_max;
+            inject_scatter2d_kernel<T><<<(int)std::min<long long>((n + 255) / 256, 4096), 256, 0, s>>>(q, rec_box_max);
             ++launches;
         }
     }
@@ -786,13 +839,7 @@ struct PlanT final : public pysit_plan {
             }
             bind_state(p, st);
             set_inject(p, true, g0, k, nullptr);
-            p.rec.rowptr = at<int>(off.recrow) + (size_t)g0 * nrec;
-            p.rec.off = at<long long>(off.recoff);
-            p.rec.w = at<T>(off.recw);
-            p.rec.traces = tr + (long long)k * nrec;
-            p.rec.tr_sstride = (long long)nsteps * nrec;
-            p.rec.nrec = nrec;
-            p.rec.blocks = nrec > 0 ? ceil_div((long long)gn * nrec, bz) : 0;
+            set_recording(p, g0, gn, tr + (long long)k * nrec);
             launch(p, kFwd, s);
             advance(st);
         }
@@ -838,6 +885,50 @@ struct PlanT final : public pysit_plan {
     void reset_task_counter(cudaStream_t s) {
         cudaMemsetAsync(ws + off.ctr, 0, 2 * sizeof(unsigned long long), s);
         ctr_next[0] = ctr_next[1] = 0;
+    }
+
+    // n launches of one step kernel on the first shot group's buffers, for timing
+    // (the state keeps evolving from whatever the last run left; no output)
+    int step_loop(int mode, int n, cudaStream_t s) override {
+        PGB_REQUIRE(ws, "no workspace bound");
+        PGB_REQUIRE(model_set, "pysit_plan_set_model must be called first");
+        PGB_REQUIRE(mode >= kFwd && mode <= kAdj, "mode must be 0 (forward), 1 (recompute) or 2 (adjoint)");
+        PGB_REQUIRE(n >= 0, "nsteps must be >= 0");
+        launches = 0;
+        reset_task_counter(s);
+        const int gn = std::min(G, nshots);
+        WaveParams<T> p = base_params(0, gn);
+        State st = mode == kAdj ? make_state(off.A, off.AX, off.AY, off.AZ, off.AS)
+                                : make_state(off.U, off.PX, off.PY, off.PZ, off.PS);
+        for (int i = 0; i < n; ++i) {
+            const int k = i % nsteps;
+            bind_state(p, st);
+            if (mode == kAdj) {
+                set_inject(p, false, 0, k, at<T>(off.traces));
+                p.image = 1;
+                p.dw_in = fld(off.replay) + (size_t)(k % S) * fstride * G;
+                p.ic = fld(off.ic);
+            } else {
+                set_inject(p, true, 0, k, nullptr);
+                if (mode == kRecomp) p.dw_out = fld(off.replay) + (size_t)(k % S) * fstride * G;
+                else set_recording(p, 0, gn, at<T>(off.traces) + (long long)k * nrec);
+            }
+            launch(p, mode, s);
+            advance(st);
+        }
+        PGB_CHECK_CUDA(cudaGetLastError());
+        last_launches = launches;
+        return PYSIT_OK;
+    }
+
+    void set_recording(WaveParams<T>& p, int g0, int gn, T* tr_k) const {
+        p.rec.rowptr = at<int>(off.recrow) + (size_t)g0 * nrec;
+        p.rec.off = at<long long>(off.recoff);
+        p.rec.w = at<T>(off.recw);
+        p.rec.traces = tr_k;
+        p.rec.tr_sstride = (long long)nsteps * nrec;
+        p.rec.nrec = nrec;
+        p.rec.blocks = nrec > 0 ? ceil_div((long long)gn * nrec, bz) : 0;
     }
 
     void enqueue_forward(void* traces_out, cudaStream_t s) {
@@ -1041,4 +1132,9 @@ extern "C" int pysit_plan_last_launch_count(const pysit_plan* p, int64_t* n) {
     PGB_REQUIRE(p && n, "NULL argument");
     *n = p->last_launches;
     return PYSIT_OK;
+}
+
+extern "C" int pysit_plan_step_loop(pysit_plan* p, int mode, int nsteps, void* stream) {
+    PGB_REQUIRE(p, "NULL plan");
+    return p->step_loop(mode, nsteps, (cudaStream_t)stream);
 }

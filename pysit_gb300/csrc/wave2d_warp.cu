@@ -4,8 +4,7 @@
 // Same maths as the reference step cda_time_scalar_2D (pysit/solvers/
 // constant_density_acoustic/time/scalar/constant_density_acoustic_time_scalar_2D.h:88-179)
 // with the fusions of the batched pipeline:
-//   kFwd    trace recording of u_k (recorder blocks at the front of the grid,
-//           receivers.py:462-510);
+//   kFwd    (trace recording of u_k runs as a kernel of its own beside these);
 //   kRecomp the imaging operand dWaveOp_k (constant_density_acoustic_base.py:24-40)
 //           from the stencil's own bracket F: C^2 F where the step and mesh
 //           sigmas agree, plus the sigma differences elsewhere (the right PML,
@@ -33,6 +32,8 @@
 //   kind 1  PML shell: the padding and its R-wide rim, 2-cell lane vectors (more
 //           busy lanes on the narrow z-bands), Phi_x / Phi_z carried where both
 //           sigmas vanish as in the reference.
+// Injection (_2D.h:165): the source taps of the cells of a row, inline; the
+// caller may instead switch the injection off here and add it after the step.
 // Each lane issues at most one of a row's bulk copies (per-lane copy descriptors),
 // and the arithmetic runs on cell pairs (packed f32x2 instructions in FP32).
 // Waits are bounded: on expiry the kernel sets the plan's error word, waits (again

@@ -228,6 +228,12 @@ class WavePlan:
             C.c_void_p(self.rnorm2.data_ptr()), C.c_void_p(_native.stream_handle())))
         return self.grad
 
+    def step_loop(self, mode, nsteps):
+        """Enqueue `nsteps` launches of one step kernel (0 forward, 1 recompute, 2 adjoint) on the
+        plan's own buffers, for timing one kernel; returns nothing useful (benchmarking aid)."""
+        _native.check(_native.load().pysit_plan_step_loop(self._h, int(mode), int(nsteps),
+                                                           C.c_void_p(_native.stream_handle())))
+
     def status(self):
         """Device status flags (1: bulk-copy wait expired, 2: non-finite wavefield); clears them."""
         f = C.c_int()

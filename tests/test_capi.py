@@ -107,6 +107,8 @@ def test_plan_create_reports_workspace_and_destroys(lib):
     # running before binding a workspace is an error, not a crash
     rc = lib.pysit_plan_forward(h, None, None)
     assert rc == _native.PYSIT_EINVAL
+    assert lib.pysit_plan_step_loop(h, 0, 4, None) == _native.PYSIT_EINVAL
+    assert b"no workspace" in lib.pysit_cuda_last_error()
     _native.check(lib.pysit_plan_destroy(h))
 
 
