@@ -9,8 +9,12 @@ seeded synthetic model: pysit_gb300.workloads.cfg2).  Output: one JSON line.
   e2e    shots/s through the public torch.autograd API (FWIMisfit): every step
          copies the velocity and the observed traces from pinned host memory to
          the device and reads the gradient back
-  roofline  the forward step kernel: algorithmic bytes per launch / its mean
-         launch time (CUDA events), against the measured HBM copy peak
+  roofline  the dominant step kernel (forward, recompute or adjoint; each timed
+         alone with CUDA events): algorithmic bytes per launch / mean launch
+         time, against the measured HBM copy peak; all three under "modes"
+  plain_fp64  the plain path: PySIT's per-shot, per-step loop in FP64 over the
+         per-step CUDA kernels, one shot on a bounded sample of steps
+         (extrapolated), and the batched/plain speed-up
   cpu_baseline  the CPU oracle port of the same pipeline on the host cores, on
          a bounded sample of steps, extrapolated to a full gradient
 --impl reference times that CPU implementation alone (the reference arm).
@@ -66,6 +70,33 @@ def _cpu_worker(args):
     sim, dws = pipeline.forward(P, want_dwaveop=True)
     pipeline.adjoint_image(P, np.random.default_rng(0).standard_normal(sim.shape) * 1e-3, dws)
     return time.perf_counter() - t0
+
+
+def plain_fp64_baseline(scale=1.0, nsteps_full=4000, nsample=256, order=8):
+    """The plain path on the GPU: PySIT's per-shot, per-step control flow
+    (TemporalLeastSquares.compute_gradient, temporal_least_squares.py:141-198) in FP64 over the
+    per-step CUDA kernels, one shot of the same grid timed over `nsample` steps and extrapolated
+    to the full step count (its cost per step does not depend on the number of steps)."""
+    import torch
+    import pysit_gb300 as api
+    from pysit_gb300 import workloads
+
+    def run(ns):
+        m, shots, solver, C, C0 = workloads.cfg2(scale=scale, nshots=1, nsteps=ns, order=order, precision="double")
+        api.generate_seismic_data(shots, solver, solver.ModelParameters(m, {"C": C}))
+        obj = api.TemporalLeastSquares(solver, batched=False)
+        m0 = solver.ModelParameters(m, {"C": C0})
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        obj.compute_gradient(shots, m0)
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0, solver.nsteps
+
+    run(32)  # warm-up (kernels, allocator)
+    t, ns = run(nsample)
+    per_shot = t / ns * nsteps_full
+    return {"value": 1.0 / per_shot, "unit": "shots/s", "dtype": "f64",
+            "sample": f"1 shot x {ns} steps of the same grid, extrapolated to {nsteps_full} steps; wall {t:.2f}s"}
 
 
 def cpu_baseline(nsample=40, procs=None, scale=1.0, nsteps_full=4000, order=8):
@@ -136,6 +167,7 @@ def main():
     ap.add_argument("--shots-per-launch", type=int, default=None)
     ap.add_argument("--cpu-sample", type=int, default=40)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain per-shot FP64 GPU path")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -300,6 +332,10 @@ def main():
                          "forward_graph": {"launch_ms": fwd_launch_ms, "achieved_gbs": achieved,
                                            "gcell_per_s": fwd_gcells}},
             "gpu_launches": launches, "misfit_rnorm2": rn, "clocks": clocks}
+    if rank == 0 and not args.no_plain:
+        plain = plain_fp64_baseline(scale=args.scale, nsteps_full=args.nsteps)
+        plain["batched_over_plain"] = line["value"] / world / plain["value"]
+        line["plain_fp64"] = plain
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(nsample=args.cpu_sample, scale=args.scale, nsteps_full=args.nsteps)
     if rank == 0:

@@ -49,6 +49,9 @@ constexpr uint32_t kPolls = 1u << 22;
 #ifndef PGB_RING_AHEAD
 #define PGB_RING_AHEAD 4   // rows whose copies are in flight ahead of the computation
 #endif
+#ifndef PGB_RING_RB
+#define PGB_RING_RB 2      // rows per iteration of the FP32 interior sweep
+#endif
 
 template <typename T, int N> struct VecT;
 template <> struct VecT<float, 4> { using type = float4; };
@@ -87,18 +90,23 @@ struct Ring {
     static constexpr int NB = HZ / V;                            // halo vectors per side
     static constexpr int SEG = 32 * V;                           // cells a task owns at most
     static constexpr int WS = SEG + 2 * HZ;                      // slot with halo (elements)
-    static constexpr int A = MODE == kAdj && PGB_RING_AHEAD > 2 ? PGB_RING_AHEAD - 1 : PGB_RING_AHEAD;
-    static constexpr int NU = 2 * R + A;                         // x-ring slots
+    // rows per iteration: the FP32 interior sweeps two rows at a time (the per-row
+    // bookkeeping is shared, and the 2R+2 rows of the window are read once)
+    static constexpr int RB = sizeof(T) == 4 && KIND == 0 ? PGB_RING_RB : 1;
+    static constexpr int AR = MODE == kAdj && PGB_RING_AHEAD > 2 ? PGB_RING_AHEAD - 1 : PGB_RING_AHEAD;
+    static constexpr int A = (AR + RB - 1) / RB < 2 ? 2 : (AR + RB - 1) / RB;  // iterations in flight
+    static constexpr int NU = 2 * R + RB * A;                    // x-ring slots
     static constexpr bool PML = KIND == 1;
-    static constexpr int NPF = MODE == kAdj ? 4 : 2;             // centre rows per stage
-    static constexpr int PST = NPF * SEG + (PML ? WS : 0);       // stage (elements)
+    static constexpr int NPF = MODE == kAdj ? 4 : 2;             // centre fields per row
+    static constexpr int PST = RB * (NPF * SEG + (PML ? WS : 0));  // stage (elements)
     // u ring, Phi_x ring (same slot stride, centre at +HZ, so one row offset serves both), stages
     static constexpr int ELEMS = NU * WS * (PML ? 2 : 1) + A * PST;
     static constexpr size_t per_warp = 128 + sizeof(T) * (size_t)ELEMS;  // barriers + rings
     static constexpr size_t bytes = kWarps * per_warp;
-    static_assert(A >= 1 && A <= 16, "the barrier block holds 16 mbarriers");
+    static_assert(A >= 2 && A <= 16, "the barrier block holds 16 mbarriers");
     static_assert(V % 2 == 0 && HZ % V == 0, "lanes hold whole pairs; halo in whole vectors");
     static_assert(per_warp % 16 == 0, "warp regions stay 16-byte aligned");
+    static_assert(RB == 1 || RB == 2, "one or two rows per iteration");
 };
 
 // Pair arithmetic: two neighbouring cells per operation.  FP32 uses the packed
@@ -150,17 +158,21 @@ __device__ __forceinline__ void sweep(const WaveParams<T>& p, unsigned char* wsm
     using O = PairOps<T>;
     using P = typename O::P;
     constexpr int V = G::V, HZ = G::HZ, NB = G::NB, SEG = G::SEG, WS = G::WS, A = G::A, NU = G::NU;
+    constexpr int RB = G::RB, NPF = G::NPF;
     constexpr bool PML = G::PML;
     constexpr int NW = (2 * NB + 1) * V;  // z-window of a lane
     constexpr int C0 = NB * V;            // its centre
+    constexpr int NR = 2 * R + RB;        // rows an iteration reads: x-R .. x+RB-1+R
     constexpr int TB = (int)sizeof(T);
     // byte layout of the warp region: barriers | u ring | Phi_x ring (PML) | stages
     constexpr int SLOT = WS * TB, STG = G::PST * TB;
     constexpr int OFF_U = 128, OFF_X = OFF_U + NU * SLOT, OFF_P = OFF_X + (PML ? NU * SLOT : 0);
+    constexpr int OFF_PZ = NPF * RB * SEG * TB;  // Phi_z rows inside a stage
     const uint32_t bar0 = smem_u32(wsm);
     const int lane = threadIdx.x & 31;
     const unsigned char* lb = wsm + lane * V * TB;  // this lane's first cell in any slot
-    const int niter = x1 - x0;
+    const int niter = x1 - x0;                      // rows
+    const int nit = (niter + RB - 1) / RB;          // iterations
     const int zl = zs + lane * V;
     const bool own = zl < ze;
     const long long sh = (long long)shot * p.fstride;
@@ -170,44 +182,51 @@ __device__ __forceinline__ void sweep(const WaveParams<T>& p, unsigned char* wsm
     const int ncen = (ze - zs + G::AL - 1) / G::AL * G::AL;
     const uint32_t bu = (uint32_t)(ncen + 2 * HZ) * TB;
     const uint32_t bc = (uint32_t)ncen * TB;
-    const uint32_t bstage = bu + 2 * bc + (img ? 2 * bc : 0) + (PML ? bc + bu : 0);
+    const uint32_t brow = bu + 2 * bc + (img ? 2 * bc : 0) + (PML ? bc + bu : 0);  // bytes per row
+    auto bytes_it = [&](int it) { return (uint32_t)min(RB, niter - RB * it) * brow; };
 
-    // One bulk copy per lane and row.  Lane c's copy: field, row offset (R for
-    // the x-ring fields), halo or centre, and destination (x-ring slot or stage).
+    // One bulk copy per lane and iteration: lane c copies row r = c % RB of field
+    // f = c / RB (field, row offset R for the x-ring fields, halo or centre, and
+    // destination: x-ring slot or stage).
     //   0 u_k -> u ring; 1 u_{k-1}, 2 C^2 -> stage; [3 dWaveOp, 4 ic -> stage];
     //   [PML: Phi_x -> Phi_x ring; Phi_z (halo) -> stage]
-    const int ncp = 3 + (img ? 2 : 0) + (PML ? 2 : 0);
-    const T* csrc = nullptr;  // element of row 0 (x-ring fields: row R)
+    const int nfield = 3 + (img ? 2 : 0) + (PML ? 2 : 0);
+    const int ncp = nfield * RB;
+    const int cf = lane / RB, cr = lane - cf * RB;
+    const T* csrc = nullptr;  // element of row cr (x-ring fields: row cr + R)
     uint32_t cdst = 0, cstep = 0, cbytes = 0;
     bool cring = false;
     {
-        const int c = lane;
         const int cpml = 3 + (img ? 2 : 0);
         const uint32_t w0 = smem_u32(wsm);
-        if (c == 0) {
-            csrc = p.u_cur + sh + rowoff(R) + zs - HZ; cdst = w0 + OFF_U; cstep = SLOT; cbytes = bu; cring = true;
-        } else if (c == 1 || c == 2 || (img && (c == 3 || c == 4))) {
-            const T* f = c == 1 ? (const T*)uprev : c == 2 ? p.c2 : c == 3 ? p.dw_in + sh : (const T*)p.ic + sh;
-            csrc = f + rowoff(0) + zs; cdst = w0 + OFF_P + (c - 1) * SEG * TB; cstep = STG; cbytes = bc;
-        } else if (PML && c == cpml) {
-            csrc = p.phx_in + sh + rowoff(R) + zs; cdst = w0 + OFF_X + HZ * TB; cstep = SLOT; cbytes = bc;
+        if (cf == 0) {
+            csrc = p.u_cur + sh + rowoff(cr + R) + zs - HZ; cdst = w0 + OFF_U; cstep = SLOT; cbytes = bu; cring = true;
+        } else if (cf == 1 || cf == 2 || (img && (cf == 3 || cf == 4))) {
+            const T* f = cf == 1 ? (const T*)uprev : cf == 2 ? p.c2 : cf == 3 ? p.dw_in + sh : (const T*)p.ic + sh;
+            csrc = f + rowoff(cr) + zs;
+            cdst = w0 + OFF_P + ((cf - 1) * RB + cr) * SEG * TB; cstep = STG; cbytes = bc;
+        } else if (PML && cf == cpml) {
+            csrc = p.phx_in + sh + rowoff(cr + R) + zs; cdst = w0 + OFF_X + HZ * TB; cstep = SLOT; cbytes = bc;
             cring = true;
-        } else if (PML && c == cpml + 1) {
-            csrc = p.phz_in + sh + rowoff(0) + zs - HZ; cdst = w0 + OFF_P + G::NPF * SEG * TB; cstep = STG;
+        } else if (PML && cf == cpml + 1) {
+            csrc = p.phz_in + sh + rowoff(cr) + zs - HZ; cdst = w0 + OFF_P + OFF_PZ + cr * SLOT; cstep = STG;
             cbytes = bu;
         }
     }
-    // row x0 + i into x-ring slot `slot` and stage s (the stage's expect_tx comes first)
-    auto copy_row = [&](int i, int s, int slot) {
-        if (lane < ncp)
-            bulk_g2s_s(cdst + (uint32_t)(cring ? slot : s) * cstep, csrc + (long long)(x0 + i) * p.ldz, cbytes,
-                       bar0 + 8u * s);
+    // the rows of iteration `it` into stage s; their x-ring slots follow the rows
+    auto copy_iter = [&](int it, int s) {
+        if (lane < ncp && RB * it + cr < niter) {
+            int slot = RB * it + 2 * R + cr;
+            slot -= slot / NU * NU;
+            bulk_g2s_s(cdst + (uint32_t)(cring ? slot : s) * cstep, csrc + (long long)(x0 + RB * it) * p.ldz,
+                       cbytes, bar0 + 8u * s);
+        }
     };
     fence_proxy_async();  // earlier generic reads of the rings before the new copies
     {
-        // the 2R leading rows x0-R .. x0+R-1 of u_k (and Phi_x) ride on the first row's stage
+        // the 2R leading rows x0-R .. x0+R-1 of u_k (and Phi_x) ride on the first stage
         const uint32_t pro = 2 * R * (bu + (PML ? bc : 0));
-        if (lane == 0) mbar_arrive_expect_tx_s(bar0 + 8u * pp.s, bstage + pro);
+        if (lane == 0) mbar_arrive_expect_tx_s(bar0 + 8u * pp.s, bytes_it(0) + pro);
         if (lane < (PML ? 4 * R : 2 * R)) {
             const int j = lane < 2 * R ? lane : lane - 2 * R;
             const bool u = lane < 2 * R;
@@ -215,12 +234,12 @@ __device__ __forceinline__ void sweep(const WaveParams<T>& p, unsigned char* wsm
             const uint32_t dst = smem_u32(wsm) + (u ? OFF_U : OFF_X + HZ * TB) + j * SLOT;
             bulk_g2s_s(dst, src, u ? bu : bc, bar0 + 8u * pp.s);
         }
-        copy_row(0, pp.s, 2 * R);
+        copy_iter(0, pp.s);
         int s = pp.s;
-        for (int i = 1; i < min(A, niter); ++i) {
+        for (int it = 1; it < min(A, nit); ++it) {
             if (++s == A) s = 0;
-            if (lane == 0) mbar_arrive_expect_tx_s(bar0 + 8u * s, bstage);
-            copy_row(i, s, 2 * R + i);
+            if (lane == 0) mbar_arrive_expect_tx_s(bar0 + 8u * s, bytes_it(it));
+            copy_iter(it, s);
         }
     }
 
@@ -237,7 +256,6 @@ __device__ __forceinline__ void sweep(const WaveParams<T>& p, unsigned char* wsm
     const int* bx = p.inj.box + shot * 6;
     const int bx0 = __ldg(bx), bx1 = __ldg(bx + 1);
     const bool inj_task = p.inj.on && bx0 < x1 && bx1 > x0 && __ldg(bx + 4) < ze && __ldg(bx + 5) > zs;
-
     // weight pairs, built once per task
     P wx[R + 1], wz[R + 1], a1[R + 1];
 #pragma unroll
@@ -247,189 +265,197 @@ __device__ __forceinline__ void sweep(const WaveParams<T>& p, unsigned char* wsm
         a1[m] = O::dup(T(d1w(R, m)));
     }
 
-    // byte offsets of the slots holding rows x-R .. x+R (rotated every row)
-    int ra[2 * R + 1];
+    // byte offsets of the slots holding rows x-R .. x+RB-1+R (shifted by RB every iteration)
+    int ra[NR];
 #pragma unroll
-    for (int j = 0; j <= 2 * R; ++j) ra[j] = j * SLOT;
-    int b = 0;               // x-ring slot of row x - R
-    int nx_slot = 2 * R + 1; // x-ring slot of row x + R + 1
-    if (nx_slot >= NU) nx_slot -= NU;
-    long long o = rowoff(x0) + zl;  // element of the lane's first cell in row x
-    // sigma_x (and the mesh sigma_x) of the row, loaded one row ahead
+    for (int j = 0; j < NR; ++j) ra[j] = j * SLOT;
+    int nxs = (NR) % NU;             // x-ring slot of the first row entering next
+    long long o = rowoff(x0) + zl;   // element of the lane's first cell in row x
+    // sigma_x (and the mesh sigma_x) of the shell rows, loaded one iteration ahead
     T sx_n = PML ? __ldg(p.sgx + x0) : T(0);
     T mx_n = PML && MODE == kRecomp ? __ldg(p.mgx + x0) : T(0);
-    for (int i = 0; i < niter; ++i, o += p.ldz) {
-        const int x = x0 + i;
+    for (int it = 0; it < nit; ++it, o += (long long)RB * p.ldz) {
+        const int x = x0 + RB * it;
         const int s = pp.s;
         if (!mbar_wait_bounded(reinterpret_cast<uint64_t*>(wsm) + s, pp.ph, kPolls)) late = true;
         const unsigned char* sb = lb + OFF_P + s * STG;  // this lane in stage s
 
-        // ---- the shared-memory reads of this row --------------------------------------
-        T w[NW];  // u_k row x around the lane's cells
+        // ---- the shared-memory reads of this iteration ---------------------------------
+        Vec<T, V> cv[NR];  // u_k rows x-R .. x+RB-1+R at the lane's cells
 #pragma unroll
-        for (int j = 0; j <= 2 * NB; ++j) {
-            const Vec<T, V> a = lds<T, V>(reinterpret_cast<const T*>(lb + OFF_U + ra[R] + j * V * TB));
-#pragma unroll
-            for (int v = 0; v < V; ++v) w[j * V + v] = a.v[v];
-        }
-        Vec<T, V> ux[2 * R];  // u_k rows x-R..x-1, x+1..x+R at the lane's cells
-#pragma unroll
-        for (int m = 1; m <= R; ++m) {
-            ux[R - m] = lds<T, V>(reinterpret_cast<const T*>(lb + OFF_U + ra[R - m] + HZ * TB));
-            ux[R + m - 1] = lds<T, V>(reinterpret_cast<const T*>(lb + OFF_U + ra[R + m] + HZ * TB));
-        }
-        const Vec<T, V> um = lds<T, V>(reinterpret_cast<const T*>(sb));
-        const Vec<T, V> cc = lds<T, V>(reinterpret_cast<const T*>(sb + SEG * TB));
-        Vec<T, V> dwi, ici;
-        if (MODE == kAdj && img) {
-            dwi = lds<T, V>(reinterpret_cast<const T*>(sb + 2 * SEG * TB));
-            ici = lds<T, V>(reinterpret_cast<const T*>(sb + 3 * SEG * TB));
-        }
-        Vec<T, V> px[2 * R + 1];  // Phi_x rows x-R..x+R (PML tasks)
-        T wp[NW];                 // Phi_z row x around the lane's cells (PML tasks)
-        if (PML) {
-#pragma unroll
-            for (int j = 0; j <= 2 * R; ++j)
-                px[j] = lds<T, V>(reinterpret_cast<const T*>(lb + OFF_X + ra[j] + HZ * TB));
-#pragma unroll
-            for (int j = 0; j <= 2 * NB; ++j) {
-                const Vec<T, V> a = lds<T, V>(reinterpret_cast<const T*>(sb + G::NPF * SEG * TB + j * V * TB));
-#pragma unroll
-                for (int v = 0; v < V; ++v) wp[j * V + v] = a.v[v];
-            }
-        }
-        // ---- the update, two cells at a time ----------------------------------------
-        const bool xok = x > 0 && x < p.nx - 1;
-        const bool inj_row = inj_task && own && x >= bx0 && x < bx1;
+        for (int j = 0; j < NR; ++j) cv[j] = lds<T, V>(reinterpret_cast<const T*>(lb + OFF_U + ra[j] + HZ * TB));
         const T sx = sx_n, mgx = mx_n;
-        if (PML && i + 1 < niter) {
+        if (PML && it + 1 < nit) {
             sx_n = __ldg(p.sgx + x + 1);
             if (MODE == kRecomp) mx_n = __ldg(p.mgx + x + 1);
         }
         (void)sx; (void)mgx;
-        Vec<T, V> un, dwo, pxo, pzo, ico;
+
 #pragma unroll
-        for (int k = 0; k < V / 2; ++k) {
-            const int v0 = 2 * k;
-            auto pr = [&](const Vec<T, V>& a) { return O::mk(a.v[v0], a.v[v0 + 1]); };
-            auto pw = [&](const T* a, int d) { return O::mk(a[C0 + v0 + d], a[C0 + v0 + 1 + d]); };
-            const P uc = pw(w, 0);
-            // Laplacian in difference form: sum_m w_m ((u_+m - u_0) + (u_-m - u_0)),
-            // equal to the central stencil because the weights sum to zero, and free
-            // of the large cancellation of w_0 u_0 (the FP32 path depends on this)
-            // (x and z accumulate separately: two short dependency chains)
-            P Fx = O::dup(T(0)), Fz = Fx;
+        for (int r = 0; r < RB; ++r) {
+            const int xr = x + r;
+            const bool valid = RB == 1 || RB * it + r < niter;  // an odd last row has no partner
+            T w[NW];  // u_k row xr around the lane's cells
 #pragma unroll
-            for (int m = 1; m <= R; ++m) {
-                Fx = O::fma(wx[m], O::add(O::sub(pr(ux[R + m - 1]), uc), O::sub(pr(ux[R - m]), uc)), Fx);
-                Fz = O::fma(wz[m], O::add(O::sub(pw(w, m), uc), O::sub(pw(w, -m), uc)), Fz);
+            for (int j = 0; j <= 2 * NB; ++j) {
+                const Vec<T, V> a = j == NB ? cv[R + r]
+                                            : lds<T, V>(reinterpret_cast<const T*>(lb + OFF_U + ra[R + r] + j * V * TB));
+#pragma unroll
+                for (int v = 0; v < V; ++v) w[j * V + v] = a.v[v];
             }
-            P F = O::add(Fx, Fz);
-            if (inj_row) {
-                F.x += inject_rhs(p.inj, bx, shot, x, zl + v0);
-                F.y += inject_rhs(p.inj, bx, shot, x, zl + v0 + 1);
+            const Vec<T, V> um = lds<T, V>(reinterpret_cast<const T*>(sb + (0 * RB + r) * SEG * TB));
+            const Vec<T, V> cc = lds<T, V>(reinterpret_cast<const T*>(sb + (1 * RB + r) * SEG * TB));
+            Vec<T, V> dwi, ici;
+            if (MODE == kAdj && img) {
+                dwi = lds<T, V>(reinterpret_cast<const T*>(sb + (2 * RB + r) * SEG * TB));
+                ici = lds<T, V>(reinterpret_cast<const T*>(sb + (3 * RB + r) * SEG * TB));
             }
-            const P uo = pr(um), c2 = pr(cc);
-            // interior tasks never touch the outer (Dirichlet) ring: no masks there
-            const bool ok0 = !PML || (xok && zok[v0]), ok1 = !PML || (xok && zok[v0 + 1]);
-            P unew;
+            Vec<T, V> px[2 * R + 1];  // Phi_x rows xr-R..xr+R (PML tasks)
+            T wp[NW];                 // Phi_z row xr around the lane's cells (PML tasks)
             if (PML) {
-                P dpx = O::dup(T(0)), dpz = dpx, dx1 = dpx, dz1 = dpx;
+#pragma unroll
+                for (int j = 0; j <= 2 * R; ++j)
+                    px[j] = lds<T, V>(reinterpret_cast<const T*>(lb + OFF_X + ra[r + j] + HZ * TB));
+#pragma unroll
+                for (int j = 0; j <= 2 * NB; ++j) {
+                    const Vec<T, V> a = lds<T, V>(reinterpret_cast<const T*>(sb + OFF_PZ + r * SLOT + j * V * TB));
+#pragma unroll
+                    for (int v = 0; v < V; ++v) wp[j * V + v] = a.v[v];
+                }
+            }
+
+            // ---- the update of row xr, two cells at a time ----------------------------------
+            const bool xok = xr > 0 && xr < p.nx - 1;
+            const bool inj_row = inj_task && own && xr >= bx0 && xr < bx1;
+            Vec<T, V> un, dwo, pxo, pzo, ico;
+#pragma unroll
+            for (int k = 0; k < V / 2; ++k) {
+                const int v0 = 2 * k;
+                auto pr = [&](const Vec<T, V>& a) { return O::mk(a.v[v0], a.v[v0 + 1]); };
+                auto pw = [&](const T* a, int d) { return O::mk(a[C0 + v0 + d], a[C0 + v0 + 1 + d]); };
+                const P uc = pw(w, 0);
+                // Laplacian in difference form: sum_m w_m ((u_+m - u_0) + (u_-m - u_0)),
+                // equal to the central stencil because the weights sum to zero, and free
+                // of the large cancellation of w_0 u_0 (the FP32 path depends on this)
+                // (x and z accumulate separately: two short dependency chains)
+                P Fx = O::dup(T(0)), Fz = Fx;
 #pragma unroll
                 for (int m = 1; m <= R; ++m) {
-                    const P a = a1[m];
-                    dpx = O::fma(a, O::sub(pr(px[R + m]), pr(px[R - m])), dpx);
-                    dpz = O::fma(a, O::sub(pw(wp, m), pw(wp, -m)), dpz);
-                    dx1 = O::fma(a, O::sub(pr(ux[R + m - 1]), pr(ux[R - m])), dx1);
-                    dz1 = O::fma(a, O::sub(pw(w, m), pw(w, -m)), dz1);
+                    Fx = O::fma(wx[m], O::add(O::sub(pr(cv[R + r + m]), uc), O::sub(pr(cv[R + r - m]), uc)), Fx);
+                    Fz = O::fma(wz[m], O::add(O::sub(pw(w, m), uc), O::sub(pw(w, -m), uc)), Fz);
                 }
-                F = O::add(F, O::fma(dpx, O::dup(p.idx), O::mul(dpz, O::dup(p.idz))));
-                // split-field PML update (_2D.h:157-170), branch-free: with both sigmas
-                // zero it reduces to the plain leapfrog update and carries Phi unchanged
-                const P szp = O::mk(sgz[v0], sgz[v0 + 1]);
-                const P dsx = O::dup(p.dt * sx), dsz = O::mul(O::dup(p.dt), szp);
-                const P S = O::add(O::dup(sx), szp);                     // sx + sz
-                const P phx = pr(px[R]), phz = pw(wp, 0);
-                // Phi' = Phi - dt s Phi + dt (s_other - s) du/dn
-                P ph_x = O::fma(O::mul(O::sub(dsz, dsx), O::dup(p.idx)), dx1, O::fma(dsx, O::mul(phx, O::dup(T(-1))), phx));
-                P ph_z = O::fma(O::mul(O::sub(dsx, dsz), O::dup(p.idz)), dz1, O::fma(dsz, O::mul(phz, O::dup(T(-1))), phz));
-                // u' = 2 dt^2 / (2 + dt S) * (C^2 F - (u_{k-1} - 2u)/dt^2 + S u_{k-1}/(2dt) - sx sz u)
-                const P den = O::fma(O::dup(p.dt), S, O::dup(T(2)));
-                const P fac1 = O::mul(O::dup(T(2) * p.dt2), O::mk(rcp_(den.x), rcp_(den.y)));
-                const P c2F = O::mul(c2, F);
-                P fac2 = O::fma(O::fma(O::dup(T(-2)), uc, uo), O::dup(-p.idt2), c2F);
-                fac2 = O::fma(O::mul(S, O::dup(p.i2dt)), uo, fac2);
-                fac2 = O::fma(O::mul(O::dup(-sx), szp), uc, fac2);
-                unew = O::mul(fac1, fac2);
-                if (!ok0) { unew.x = T(0); ph_x.x = T(0); ph_z.x = T(0); }
-                if (!ok1) { unew.y = T(0); ph_x.y = T(0); ph_z.y = T(0); }
-                pxo.v[v0] = ph_x.x; pxo.v[v0 + 1] = ph_x.y;
-                pzo.v[v0] = ph_z.x; pzo.v[v0 + 1] = ph_z.y;
-                if (MODE == kRecomp) {
-                    // dWaveOp = C^2 F + (sm - s)(u' - u_{k-1})/(2dt) + (smx smz - sx sz) u
-                    const P mzp = O::mk(mgz[v0], mgz[v0 + 1]);
-                    const P dS = O::sub(O::add(O::dup(mgx), mzp), S);
-                    const P dP = O::sub(O::mul(O::dup(mgx), mzp), O::mul(O::dup(sx), szp));
-                    P d = O::fma(O::mul(dS, O::dup(p.i2dt)), O::sub(unew, uo), c2F);
-                    d = O::fma(dP, uc, d);
-                    dwo.v[v0] = ok0 ? d.x : T(0);
-                    dwo.v[v0 + 1] = ok1 ? d.y : T(0);
+                P F = O::add(Fx, Fz);
+                if (inj_row) {
+                    F.x += inject_rhs(p.inj, bx, shot, xr, zl + v0);
+                    F.y += inject_rhs(p.inj, bx, shot, xr, zl + v0 + 1);
                 }
-            } else {
-                // u_{k+1} = dt^2 C^2 F - (u_{k-1} - 2 u_k)
-                const P q = O::fma(O::dup(T(-2)), uc, uo);
-                unew = O::fma(O::mul(O::dup(p.dt2), c2), F, O::mul(q, O::dup(T(-1))));
-                if (MODE == kRecomp) {
-                    const P d = O::mul(c2, F);
-                    dwo.v[v0] = d.x;
-                    dwo.v[v0 + 1] = d.y;
-                }
-            }
-            un.v[v0] = unew.x;
-            un.v[v0 + 1] = unew.y;
-            if (MODE == kAdj) {
-                const P ic = O::fma(uc, pr(dwi), pr(ici));
-                ico.v[v0] = ic.x;
-                ico.v[v0 + 1] = ic.y;
-            }
-        }
-        if (MODE == kFwd) {  // a NaN or Inf anywhere in the lane's cells survives the sum
-            T sum = T(0);
+                const P uo = pr(um), c2 = pr(cc);
+                // interior tasks never touch the outer (Dirichlet) ring: no masks there
+                const bool ok0 = !PML || (xok && zok[v0]), ok1 = !PML || (xok && zok[v0 + 1]);
+                P unew;
+                if (PML) {
+                    P dpx = O::dup(T(0)), dpz = dpx, dx1 = dpx, dz1 = dpx;
 #pragma unroll
-            for (int v = 0; v < V; ++v) sum += un.v[v];
-            bad |= own && !isfinite(sum);
-        }
-        if (own) {
-            stg<T, V>(uprev + o, un);
-            if (PML) {
-                stg<T, V>(p.phx_out + sh + o, pxo);
-                stg<T, V>(p.phz_out + sh + o, pzo);
+                    for (int m = 1; m <= R; ++m) {
+                        const P a = a1[m];
+                        dpx = O::fma(a, O::sub(pr(px[R + m]), pr(px[R - m])), dpx);
+                        dpz = O::fma(a, O::sub(pw(wp, m), pw(wp, -m)), dpz);
+                        dx1 = O::fma(a, O::sub(pr(cv[R + r + m]), pr(cv[R + r - m])), dx1);
+                        dz1 = O::fma(a, O::sub(pw(w, m), pw(w, -m)), dz1);
+                    }
+                    F = O::add(F, O::fma(dpx, O::dup(p.idx), O::mul(dpz, O::dup(p.idz))));
+                    // split-field PML update (_2D.h:157-170), branch-free: with both sigmas
+                    // zero it reduces to the plain leapfrog update and carries Phi unchanged
+                    const P szp = O::mk(sgz[v0], sgz[v0 + 1]);
+                    const P dsx = O::dup(p.dt * sx), dsz = O::mul(O::dup(p.dt), szp);
+                    const P S = O::add(O::dup(sx), szp);  // sx + sz
+                    const P phx = pr(px[R]), phz = pw(wp, 0);
+                    // Phi' = Phi - dt s Phi + dt (s_other - s) du/dn
+                    P ph_x = O::fma(O::mul(O::sub(dsz, dsx), O::dup(p.idx)), dx1, O::fma(dsx, O::mul(phx, O::dup(T(-1))), phx));
+                    P ph_z = O::fma(O::mul(O::sub(dsx, dsz), O::dup(p.idz)), dz1, O::fma(dsz, O::mul(phz, O::dup(T(-1))), phz));
+                    // u' = 2 dt^2 / (2 + dt S) * (C^2 F - (u_{k-1} - 2u)/dt^2 + S u_{k-1}/(2dt) - sx sz u)
+                    const P den = O::fma(O::dup(p.dt), S, O::dup(T(2)));
+                    const P fac1 = O::mul(O::dup(T(2) * p.dt2), O::mk(rcp_(den.x), rcp_(den.y)));
+                    const P c2F = O::mul(c2, F);
+                    P fac2 = O::fma(O::fma(O::dup(T(-2)), uc, uo), O::dup(-p.idt2), c2F);
+                    fac2 = O::fma(O::mul(S, O::dup(p.i2dt)), uo, fac2);
+                    fac2 = O::fma(O::mul(O::dup(-sx), szp), uc, fac2);
+                    unew = O::mul(fac1, fac2);
+                    if (!ok0) { unew.x = T(0); ph_x.x = T(0); ph_z.x = T(0); }
+                    if (!ok1) { unew.y = T(0); ph_x.y = T(0); ph_z.y = T(0); }
+                    pxo.v[v0] = ph_x.x; pxo.v[v0 + 1] = ph_x.y;
+                    pzo.v[v0] = ph_z.x; pzo.v[v0 + 1] = ph_z.y;
+                    if (MODE == kRecomp) {
+                        // dWaveOp = C^2 F + (sm - s)(u' - u_{k-1})/(2dt) + (smx smz - sx sz) u
+                        const P mzp = O::mk(mgz[v0], mgz[v0 + 1]);
+                        const P dS = O::sub(O::add(O::dup(mgx), mzp), S);
+                        const P dP = O::sub(O::mul(O::dup(mgx), mzp), O::mul(O::dup(sx), szp));
+                        P d = O::fma(O::mul(dS, O::dup(p.i2dt)), O::sub(unew, uo), c2F);
+                        d = O::fma(dP, uc, d);
+                        dwo.v[v0] = ok0 ? d.x : T(0);
+                        dwo.v[v0 + 1] = ok1 ? d.y : T(0);
+                    }
+                } else {
+                    // u_{k+1} = dt^2 C^2 F - (u_{k-1} - 2 u_k)
+                    const P q = O::fma(O::dup(T(-2)), uc, uo);
+                    unew = O::fma(O::mul(O::dup(p.dt2), c2), F, O::mul(q, O::dup(T(-1))));
+                    if (MODE == kRecomp) {
+                        const P d = O::mul(c2, F);
+                        dwo.v[v0] = d.x;
+                        dwo.v[v0 + 1] = d.y;
+                    }
+                }
+                un.v[v0] = unew.x;
+                un.v[v0 + 1] = unew.y;
+                if (MODE == kAdj) {
+                    const P ic = O::fma(uc, pr(dwi), pr(ici));
+                    ico.v[v0] = ic.x;
+                    ico.v[v0 + 1] = ic.y;
+                }
             }
-            if (MODE == kRecomp && p.dw_out) stg_cs<T, V>(p.dw_out + sh + o, dwo);
-            if (MODE == kAdj && img) stg<T, V>(p.ic + sh + o, ico);
+            if (MODE == kFwd) {  // a NaN or Inf anywhere in the lane's cells survives the sum
+                T sum = T(0);
+#pragma unroll
+                for (int v = 0; v < V; ++v) sum += un.v[v];
+                bad |= own && valid && !isfinite(sum);
+            }
+            if (own && valid) {
+                const long long orow = o + (long long)r * p.ldz;
+                stg<T, V>(uprev + orow, un);
+                if (PML) {
+                    stg<T, V>(p.phx_out + sh + orow, pxo);
+                    stg<T, V>(p.phz_out + sh + orow, pzo);
+                }
+                if (MODE == kRecomp && p.dw_out) stg_cs<T, V>(p.dw_out + sh + orow, dwo);
+                if (MODE == kAdj && img) stg<T, V>(p.ic + sh + orow, ico);
+            }
         }
 
-        // ---- refill: every lane is done with stage s and row x-R -------------------
+        // ---- refill: every lane is done with stage s and rows x-R .. x-R+RB-1 ---------------
         __syncwarp();
-        if (i + A < niter) {
+        if (it + A < nit) {
             fence_proxy_async();
-            if (lane == 0) mbar_arrive_expect_tx_s(bar0 + 8u * s, bstage);
-            copy_row(i + A, s, b);
+            if (lane == 0) mbar_arrive_expect_tx_s(bar0 + 8u * s, bytes_it(it + A));
+            copy_iter(it + A, s);
         }
         if (++pp.s == A) { pp.s = 0; pp.ph ^= 1u; }
 #pragma unroll
-        for (int j = 0; j < 2 * R; ++j) ra[j] = ra[j + 1];
-        ra[2 * R] = nx_slot * SLOT;
-        if (++b == NU) b = 0;
-        if (++nx_slot == NU) nx_slot = 0;
+        for (int j = 0; j < 2 * R; ++j) ra[j] = ra[j + RB];
+#pragma unroll
+        for (int q = 0; q < RB; ++q) {
+            const int t = nxs + q;
+            ra[2 * R + q] = (t >= NU ? t - NU : t) * SLOT;
+        }
+        nxs += RB;
+        if (nxs >= NU) nxs -= NU;
     }
 }
 
-// Resident blocks per SM the register budget aims at (FP32): the interior path
-// fits five 4-warp blocks without spills, the PML shell four.
+// Resident blocks per SM the register budget aims at (FP32): four 4-warp blocks
+// (128 registers); a one-row interior sweep fits five (96 registers).
 template <typename T, int KIND>
 struct MinBlocks {
-    static constexpr int value = sizeof(T) == 4 ? (KIND == 0 ? 5 : 4) : 1;
+    static constexpr int value = sizeof(T) == 4 ? (KIND == 0 && PGB_RING_RB == 1 ? 5 : 4) : 1;
 };
 
 template <typename T, int R, int MODE, int KIND>
