@@ -4,6 +4,7 @@ Run in a container that has the reference tree (default /root/reference) after
 ``make -C oracle`` built its SWIG module into oracle/_ref:
 
     python tests/golden/make_golden.py            # all problems of tests/problems.py
+    python tests/golden/make_golden.py lbfgs:o2   # the reference's LBFGS run on problem o2
 
 For every problem it stores (compressed .npz): the traces of every shot
 modelled on the true model by the reference's own ``generate_seismic_data``
@@ -71,7 +72,47 @@ def run(name):
           f"|grad|={np.linalg.norm(out['grad']):.6e} objective={out['objective']:.6e}")
 
 
+LBFGS_ITERS = 5
+
+
+def run_lbfgs(name):
+    """PySIT's own LBFGS (memory 10, backtracking line search) for LBFGS_ITERS
+    iterations on the problem's data, with the cpp FP64 solver: objective and
+    alpha histories, the function/gradient call counts and the final model."""
+    pysit = pysit_live.import_pysit()
+    m, shots, solver, C, C0 = problems.build(pysit, name, kernel="cpp")
+    pysit.generate_seismic_data(shots, solver, solver.ModelParameters(m, {"C": C}))
+    obj = pysit.TemporalLeastSquares(solver)
+    calls = {"evaluate": 0, "gradient": 0}
+    ev, gr = obj.evaluate, obj.compute_gradient
+
+    def evaluate(*a, **k):
+        calls["evaluate"] += 1
+        return ev(*a, **k)
+
+    def compute_gradient(*a, **k):
+        calls["gradient"] += 1
+        return gr(*a, **k)
+
+    obj.evaluate, obj.compute_gradient = evaluate, compute_gradient
+    opt = pysit.LBFGS(obj, memory_length=10)
+    final = opt(shots, solver.ModelParameters(m, {"C": C0}), LBFGS_ITERS, line_search="backtrack",
+                status_configuration={"objective_frequency": 1, "gradient_length_frequency": 1})
+    _, objective = opt.retrieve_history("objective")
+    _, alpha = opt.retrieve_history("alpha")
+    _, gnorm = opt.retrieve_history("gradient_length")
+    out = dict(objective=np.array(objective), alpha=np.array(alpha), gradient_length=np.array(gnorm),
+               final_C=np.asarray(final.C).reshape(-1), n_evaluate=calls["evaluate"],
+               n_gradient=calls["gradient"], iterations=LBFGS_ITERS)
+    np.savez_compressed(os.path.join(HERE, f"lbfgs_{name}.npz"), **out)
+    print(f"lbfgs_{name}: objective {out['objective']} alpha {out['alpha']} "
+          f"evaluate {calls['evaluate']} gradient {calls['gradient']}")
+
+
 if __name__ == "__main__":
     names = sys.argv[1:] or list(problems.SPECS)
     for n in names:
-        run(n)
+        if n.startswith("lbfgs:"):
+            run_lbfgs(n.split(":", 1)[1])
+        else:
+            run(n)
