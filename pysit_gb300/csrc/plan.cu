@@ -81,6 +81,34 @@ __global__ void inject_scatter2d_kernel(const WaveParams<T> p, int cells_max) {
     }
 }
 
+// The same for a 3D step: fac = 2 dt^2 / (2 + dt (sx + sy + sz)) where a sigma is
+// nonzero (_3D.h:220-226).
+template <typename T>
+__global__ void inject_scatter3d_kernel(const WaveParams<T> p, int cells_max) {
+    const long long n = (long long)p.nshot * cells_max;
+    for (long long id = blockIdx.x * (long long)blockDim.x + threadIdx.x; id < n;
+         id += (long long)gridDim.x * blockDim.x) {
+        const int shot = (int)(id / cells_max), c = (int)(id - (long long)shot * cells_max);
+        const int* bx = p.inj.box + shot * 6;
+        const int byw = bx[3] - bx[2], bzw = bx[5] - bx[4];
+        if (byw <= 0 || bzw <= 0 || c >= (bx[1] - bx[0]) * byw * bzw) continue;
+        const int x = bx[0] + c / (byw * bzw), r = c % (byw * bzw);
+        const int y = bx[2] + r / bzw, z = bx[4] + r % bzw;
+        if (x <= 0 || x >= p.nx - 1 || y <= 0 || y >= p.ny - 1 || z <= 0 || z >= p.nz - 1) continue;
+        // the tap sum of the cell, as inject_rhs does in 2D
+        const long long cell = ((long long)(x - bx[0]) * byw + (y - bx[2])) * bzw + (z - bx[4]);
+        const int* rp = p.inj.rowptr + p.inj.rpbase[shot];
+        const T* amp = p.inj.amp + shot * p.inj.amp_sstride;
+        T rhs = T(0);
+        for (int e = rp[cell]; e < rp[cell + 1]; ++e) rhs += p.inj.w[e] * amp[p.inj.pt[e]];
+        const T sx = p.sgx[x], sy = p.sgy[y], sz = p.sgz[z];
+        const T fac = (sx != T(0) || sy != T(0) || sz != T(0)) ? T(2) * p.dt2 / (T(2) + p.dt * (sx + sy + sz))
+                                                               : p.dt2;
+        const long long o = ((long long)(x + p.hx) * p.rows_y + (y + p.hy)) * p.ldz + kOZ + z;
+        p.u_prev[(long long)shot * p.fstride + o] += fac * p.c2[o] * rhs;
+    }
+}
+
 // trace recorder as a kernel of its own (runs beside the stencil kernels: it only reads u_k)
 template <typename T>
 __global__ void record_kernel(const WaveParams<T> p) {
@@ -224,6 +252,8 @@ struct PlanT final : public pysit_plan {
     bool warp2d = true;          // 2D: warp-task sweep (true) or bulk-copy row pipeline (false)
     std::vector<int> tasks2d;    // [ntasks][5] warp tasks of the 2D sweep: interior first, then shell
     int ntask2d[2] = {0, 0};     // tasks of each kind
+    std::vector<int> tasks3d;    // [ntasks][6] block tasks of the 3D sweep: interior first, then shell
+    int ntask3d[2] = {0, 0};
     int blocks2d[3][2] = {{1, 1}, {1, 1}, {1, 1}};  // resident task blocks per mode and kind (whole GPU)
     unsigned long long ctr_next[2] = {0, 0};  // task-counter values the next 2D launch starts at
     cudaStream_t aux = nullptr;  // second stream of the 2D step (shell kernel beside the interior one)
@@ -362,6 +392,13 @@ struct PlanT final : public pysit_plan {
             ntx = (nx + tx - 1) / tx;
             return;
         }
+        if (dim == 3) {
+            bz = 128;  // threads of the recorder blocks
+            tx = have ? etx : 64;
+            build_tasks3d();
+            ntz = ntx = 1;
+            return;
+        }
         if (have) {
             bz = ebz; tx = etx;
         } else {
@@ -420,6 +457,45 @@ struct PlanT final : public pysit_plan {
         add_tasks(xb, nx, 0, nz, 1);    // high-x band
         add_tasks(xa, xb, 0, za, 1);    // low-z band
         add_tasks(xa, xb, zb, nz, 1);   // high-z band
+    }
+
+    // 3D block tasks: the interior box (R cells clear of the padding, off the outer
+    // ring, z-bounds multiples of 4) and the six slabs of the shell around it; x in
+    // chunks of about tx rows, y in groups of one row per warp, z in segments.
+    // Consecutive tasks are neighbouring y-groups (their halo rows meet in L2).
+    void add_tasks3d(int xa, int xb, int ya, int yb, int za, int zb, int kind) {
+        if (xb <= xa || yb <= ya || zb <= za) return;
+        std::vector<std::pair<int, int>> zs;
+        split(za, zb, wave3d_seg((int)sizeof(T), kind), zs);
+        const int rows = wave3d_rows_per_block();
+        const int nxc = (xb - xa + tx - 1) / tx, wx = (xb - xa + nxc - 1) / nxc;
+        for (int x = xa; x < xb; x += wx)
+            for (auto& z : zs)
+                for (int y = ya; y < yb; y += rows) {
+                    int t[6] = {x, std::min(xb, x + wx), y, std::min(yb, y + rows), z.first, z.second};
+                    tasks3d.insert(tasks3d.end(), t, t + 6);
+                }
+    }
+    void build_tasks3d() {
+        tasks3d.clear();
+        const int xa = pl[0] > 0 ? pl[0] + R : 1, xb = pr[0] > 0 ? nx - pr[0] - R : nx - 1;
+        const int ya = pl[1] > 0 ? pl[1] + R : 1, yb = pr[1] > 0 ? ny - pr[1] - R : ny - 1;
+        const int za = ((pl[2] > 0 ? pl[2] + R : 1) + 3) / 4 * 4;
+        const int zb = (pr[2] > 0 ? nz - pr[2] - R : nz - 1) / 4 * 4;
+        ntask3d[0] = ntask3d[1] = 0;
+        if (xa >= xb || ya >= yb || za >= zb) {
+            add_tasks3d(0, nx, 0, ny, 0, nz, 1);
+        } else {
+            add_tasks3d(xa, xb, ya, yb, za, zb, 0);
+            ntask3d[0] = (int)(tasks3d.size() / 6);
+            add_tasks3d(0, xa, 0, ny, 0, nz, 1);    // low-x slab
+            add_tasks3d(xb, nx, 0, ny, 0, nz, 1);   // high-x slab
+            add_tasks3d(xa, xb, 0, ya, 0, nz, 1);   // low-y slab
+            add_tasks3d(xa, xb, yb, ny, 0, nz, 1);  // high-y slab
+            add_tasks3d(xa, xb, ya, yb, 0, za, 1);  // low-z slab
+            add_tasks3d(xa, xb, ya, yb, zb, nz, 1); // high-z slab
+        }
+        ntask3d[1] = (int)(tasks3d.size() / 6) - ntask3d[0];
     }
 
     long long internal_offset(long long cell) const {
@@ -544,7 +620,7 @@ struct PlanT final : public pysit_plan {
         off.gpad = take((size_t)nx * ny * nz * sizeof(double));
         off.err = take(sizeof(int));
         off.ctr = take(2 * sizeof(unsigned long long));
-        off.tasks = take(std::max<size_t>(tasks2d.size(), 1) * sizeof(int));
+        off.tasks = take(std::max<size_t>(std::max(tasks2d.size(), tasks3d.size()), 1) * sizeof(int));
         off.partial = take(kRedBlocks * sizeof(double));
         off.rnorm = take(sizeof(double));
         ws_need = tot;
@@ -606,7 +682,7 @@ struct PlanT final : public pysit_plan {
         if ((rc = upload_inj(rec_inj, off.rbox, off.rrpb, off.rrow, off.rpt, off.rw, s))) return rc;
         if ((rc = upload(off.recrow, rec_rows, s)) || (rc = upload(off.recoff, rec_off, s))) return rc;
         if ((rc = upload(off.recw, tmp = toT(rec_ws), s))) return rc;
-        if ((rc = upload(off.tasks, tasks2d, s))) return rc;
+        if ((rc = upload(off.tasks, dim == 3 ? tasks3d : tasks2d, s))) return rc;
         PGB_CHECK_CUDA(cudaStreamSynchronize(s));
         if (!cap) PGB_CHECK_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
         if (dim == 2) {
@@ -614,6 +690,8 @@ struct PlanT final : public pysit_plan {
             wave2d_warp_prepare();
             for (int m = 0; m < 3; ++m)
                 for (int k = 0; k < 2; ++k) blocks2d[m][k] = wave2d_warp_blocks((int)sizeof(T), order, m, k);
+        }
+        if (dim >= 2) {
             if (!aux) PGB_CHECK_CUDA(cudaStreamCreateWithFlags(&aux, cudaStreamNonBlocking));
             if (!ev_fork) PGB_CHECK_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
             if (!ev_join) PGB_CHECK_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
@@ -741,8 +819,48 @@ struct PlanT final : public pysit_plan {
         }
     }
 
+    // One 3D step: interior kernel on s, PML-shell kernel (and the trace recorder)
+    // on the auxiliary stream, forked and joined as in 2D; the adjoint source is
+    // added after the step by a scatter kernel.
+    template <int RR, int MODE>
+    void launch3d(const WaveParams<T>& p, cudaStream_t s) {
+        const int* tk = at<int>(off.tasks);
+        WaveParams<T> q = p;
+        const bool scatter = MODE == kAdj && q.inj.on && rec_box_max > 0;
+        if (scatter) q.inj.on = 0;
+        const bool rec = MODE == kFwd && q.rec.blocks > 0;
+        const bool fork = ntask3d[0] > 0 && (ntask3d[1] > 0 || rec);
+        cudaStream_t side = fork ? aux : s;
+        if (fork) {
+            cudaEventRecord(ev_fork, s);
+            cudaStreamWaitEvent(aux, ev_fork, 0);
+        }
+        if (rec) {
+            record_kernel<T><<<q.rec.blocks, bz, 0, side>>>(q);
+            ++launches;
+        }
+        if (ntask3d[1] > 0) {
+            launch_wave3d_tasks<T, RR, MODE, 1>(q, tk + 6 * ntask3d[0], ntask3d[1], side);
+            ++launches;
+        }
+        if (ntask3d[0] > 0) {
+            launch_wave3d_tasks<T, RR, MODE, 0>(q, tk, ntask3d[0], s);
+            ++launches;
+        }
+        if (fork) {
+            cudaEventRecord(ev_join, aux);
+            cudaStreamWaitEvent(s, ev_join, 0);
+        }
+        if (scatter) {
+            q.inj.on = 1;
+            const long long n = (long long)q.nshot * rec_box_max;
+            inject_scatter3d_kernel<T><<<(int)std::min<long long>((n + 255) / 256, 4096), 256, 0, s>>>(q, rec_box_max);
+            ++launches;
+        }
+    }
+
     void launch(const WaveParams<T>& p, int mode, cudaStream_t s) {
-        if (!(dim == 2 && warp2d)) ++launches;
+        if (!(dim == 2 && warp2d) && dim != 3) ++launches;
 #define PGB_L(RR)                                                              \
     do {                                                                       \
         if (dim == 2 && warp2d) {                                              \
@@ -754,9 +872,9 @@ struct PlanT final : public pysit_plan {
             else if (mode == kRecomp) launch_wave2d<T, RR, kRecomp>(p, bz, s); \
             else launch_wave2d<T, RR, kAdj>(p, bz, s);                         \
         } else if (dim == 3) {                                                 \
-            if (mode == kFwd) launch_wave3d<T, RR, kFwd>(p, bz, s);            \
-            else if (mode == kRecomp) launch_wave3d<T, RR, kRecomp>(p, bz, s); \
-            else launch_wave3d<T, RR, kAdj>(p, bz, s);                         \
+            if (mode == kFwd) launch3d<RR, kFwd>(p, s);                        \
+            else if (mode == kRecomp) launch3d<RR, kRecomp>(p, s);             \
+            else launch3d<RR, kAdj>(p, s);                                     \
         } else {                                                               \
             if (mode == kFwd) launch_wave1d<T, RR, kFwd>(p, bz, s);            \
             else if (mode == kRecomp) launch_wave1d<T, RR, kRecomp>(p, bz, s); \

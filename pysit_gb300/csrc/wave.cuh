@@ -192,8 +192,12 @@ int wave2d_warp_seg(int dtype_bytes, int order, int pml);
 // resident task blocks of the whole GPU for one (dtype, order, mode, kind)
 int wave2d_warp_blocks(int dtype_bytes, int order, int mode, int kind);
 void wave2d_warp_prepare();
-template <typename T, int R, int MODE>
-void launch_wave3d(const WaveParams<T>& p, int bz, cudaStream_t s);
+// 3D block tasks (x0, x1, y0, y1, zs, ze): one block of wave3d_rows_per_block()
+// warps (one y-row each) per task and shot; KIND 0 interior, 1 PML shell
+template <typename T, int R, int MODE, int KIND>
+void launch_wave3d_tasks(const WaveParams<T>& p, const int* tasks, int ntasks, cudaStream_t s);
+int wave3d_rows_per_block();
+int wave3d_seg(int dtype_bytes, int kind);  // widest z-range of a task of each kind
 template <typename T, int R, int MODE>
 void launch_wave1d(const WaveParams<T>& p, int bz, cudaStream_t s);
 // one-time kernel attributes (large dynamic shared memory); call outside graph capture

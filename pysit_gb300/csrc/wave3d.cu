@@ -1,8 +1,12 @@
 // Batched 1D and 3D leapfrog steps (forward, recompute, adjoint modes) on the
-// internal zero-halo layout of wave.cuh.  Same maths as wave2d.cu for
-// cda_time_scalar_1D (pysit/solvers/constant_density_acoustic/time/scalar/
-// constant_density_acoustic_time_scalar_1D.h:78-130) and cda_time_scalar_3D
-// (..._3D.h:107-235), one thread per cell, z on threadIdx.x.
+// internal zero-halo layout of wave.cuh, for cda_time_scalar_1D (pysit/solvers/
+// constant_density_acoustic/time/scalar/constant_density_acoustic_time_scalar_1D.h:78-130)
+// and cda_time_scalar_3D (..._3D.h:107-235).
+//
+// 3D: a table of block tasks covers the padded grid once (interior: R cells
+// clear of the padding and off the outer ring; PML shell: the rest).  Each kind
+// is its own kernel; both sweep along x with the neighbour planes in L1.
+// 1D: one thread per cell.
 //
 // 3D auxiliary state: Phi_x/y/z is non-zero only inside the padding; psi
 // (integrated on every cell by the reference, _3D.h:216,230) only influences
@@ -57,24 +61,11 @@ __device__ __forceinline__ T dd2(const T* __restrict__ v, long long o, long long
     return a;
 }
 
-// grid: x = cells along z (blockDim.x), y = y index, z = x index * nshot;
-// recorder blocks use blockIdx.y == gridDim.y - 1 beyond the tile range.
+// One cell of the reference's 3D step (_3D.h:107-235) with the batched fusions:
+// the general path, PML included.  Cells of the outer ring get zero.
 template <typename T, int R, int MODE>
-__global__ void __launch_bounds__(256) wave3d_cell_kernel(const WaveParams<T> p, int nrecblk) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y;
-    int xi = blockIdx.z;
-    if (xi >= p.nx * p.nshot) {
-        if (MODE == kFwd) {
-            long long id = ((long long)(xi - p.nx * p.nshot) * gridDim.y + j) * gridDim.x * blockDim.x +
-                           (long long)blockIdx.x * blockDim.x + threadIdx.x;
-            record3(p, id);
-        }
-        return;
-    }
-    const int shot = xi / p.nx;
-    const int i = xi - shot * p.nx;
-    if (k >= p.nz || j >= p.ny) return;
+__device__ __forceinline__ void cell3d(const WaveParams<T>& p, const int shot, const int i, const int j,
+                                       const int k) {
     const long long sh = (long long)shot * p.fstride;
     const long long ys = p.ldz, xs = (long long)p.rows_y * p.ldz;
     const long long o = ((long long)(i + p.hx) * p.rows_y + (j + p.hy)) * p.ldz + kOZ + k;
@@ -132,6 +123,181 @@ __global__ void __launch_bounds__(256) wave3d_cell_kernel(const WaveParams<T> p,
         __stcs(p.dw_out + sh + o, ok ? d : T(0));
     }
     if (MODE == kAdj && p.image) p.ic[sh + o] += uc * __ldcs(p.dw_in + sh + o);
+    if (MODE == kFwd && p.err && !isfinite(unew)) atomicOr(p.err, PGB_ERR_NONFINITE);
+}
+
+// ---- task sweeps ---------------------------------------------------------------
+// A task (x0, x1, y0, y1, zs, ze) is handled by one block: warp w owns y-row
+// y0 + w and sweeps x0..x1-1 over the z-range [zs, ze).  The block's rows of the
+// 2R+1 planes around x stay in L1 while it marches, so u_k comes from DRAM
+// about once; the x- and y-neighbours are constant offsets from the centre row.
+constexpr int kW3 = 8;  // warps (y-rows) per block
+
+// PML shell: one cell per lane, the general per-cell update
+template <typename T, int R, int MODE>
+__global__ void __launch_bounds__(kW3 * 32) wave3d_shell_kernel(const WaveParams<T> p, const int* __restrict__ tasks,
+                                                               int ntasks) {
+    const int shot = blockIdx.x / ntasks;
+    const int* tk = tasks + 6 * (blockIdx.x - shot * ntasks);
+    const int j = __ldg(tk + 2) + (threadIdx.x >> 5);
+    const int k = __ldg(tk + 4) + (threadIdx.x & 31);
+    if (j >= __ldg(tk + 3) || k >= __ldg(tk + 5)) return;
+    const int x1 = __ldg(tk + 1);
+    for (int i = __ldg(tk); i < x1; ++i) cell3d<T, R, MODE>(p, shot, i, j, k);
+}
+
+template <typename T> struct Vec3;
+template <> struct Vec3<float> { using type = float4; static constexpr int N = 4; };
+template <> struct Vec3<double> { using type = double2; static constexpr int N = 2; };
+
+template <typename T> struct Pair3;
+template <> struct Pair3<float> {
+    using P = float2;
+    static __device__ __forceinline__ P mk(float a, float b) { return make_float2(a, b); }
+    static __device__ __forceinline__ P dup(float a) { return make_float2(a, a); }
+    static __device__ __forceinline__ P add(P a, P b) { return __fadd2_rn(a, b); }
+    static __device__ __forceinline__ P sub(P a, P b) {
+        unsigned long long d;
+        asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(*reinterpret_cast<unsigned long long*>(&a)),
+            "l"(*reinterpret_cast<unsigned long long*>(&b)));
+        return *reinterpret_cast<P*>(&d);
+    }
+    static __device__ __forceinline__ P mul(P a, P b) { return __fmul2_rn(a, b); }
+    static __device__ __forceinline__ P fma(P a, P b, P c) { return __ffma2_rn(a, b, c); }
+};
+template <> struct Pair3<double> {
+    using P = double2;
+    static __device__ __forceinline__ P mk(double a, double b) { return make_double2(a, b); }
+    static __device__ __forceinline__ P dup(double a) { return make_double2(a, a); }
+    static __device__ __forceinline__ P add(P a, P b) { return make_double2(a.x + b.x, a.y + b.y); }
+    static __device__ __forceinline__ P sub(P a, P b) { return make_double2(a.x - b.x, a.y - b.y); }
+    static __device__ __forceinline__ P mul(P a, P b) { return make_double2(a.x * b.x, a.y * b.y); }
+    static __device__ __forceinline__ P fma(P a, P b, P c) {
+        return make_double2(::fma(a.x, b.x, c.x), ::fma(a.y, b.y, c.y));
+    }
+};
+
+template <typename T>
+__device__ __forceinline__ typename Vec3<T>::type ldv(const T* q) {
+    return __ldg(reinterpret_cast<const typename Vec3<T>::type*>(q));
+}
+template <typename T>
+__device__ __forceinline__ typename Vec3<T>::type ldv_plain(const T* q) {
+    return *reinterpret_cast<const typename Vec3<T>::type*>(q);
+}
+
+// Interior: 16-byte vectors (V cells per lane), arithmetic on cell pairs, no PML
+// state (every tap is off the padding), no masks (off the outer ring).  Task
+// z-bounds are multiples of 4 cells, so every vector load is aligned.
+template <typename T, int R, int MODE>
+__global__ void __launch_bounds__(kW3 * 32, (sizeof(T) == 4 ? 2 : 1))
+    wave3d_interior_kernel(const WaveParams<T> p, const int* __restrict__ tasks, int ntasks) {
+    using O = Pair3<T>;
+    using P = typename O::P;
+    using VT = typename Vec3<T>::type;
+    constexpr int V = Vec3<T>::N;
+    constexpr int AL = 16 / (int)sizeof(T);
+    constexpr int HZ = (R + AL - 1) / AL * AL;
+    constexpr int NB = HZ / V;
+    constexpr int NW = (2 * NB + 1) * V;
+    constexpr int C0 = NB * V;
+    const int shot = blockIdx.x / ntasks;
+    const int* tk = tasks + 6 * (blockIdx.x - shot * ntasks);
+    const int j = __ldg(tk + 2) + (threadIdx.x >> 5);
+    const int zl = __ldg(tk + 4) + (threadIdx.x & 31) * V;
+    if (j >= __ldg(tk + 3) || zl >= __ldg(tk + 5)) return;
+    const int x0 = __ldg(tk), x1 = __ldg(tk + 1);
+    const long long sh = (long long)shot * p.fstride;
+    const long long ys = p.ldz, xs = (long long)p.rows_y * p.ldz;
+    P wx[R + 1], wy[R + 1], wz[R + 1];
+#pragma unroll
+    for (int m = 1; m <= R; ++m) {
+        wx[m] = O::dup(T(d2w(R, m)) * p.idx2);
+        wy[m] = O::dup(T(d2w(R, m)) * p.idy2);
+        wz[m] = O::dup(T(d2w(R, m)) * p.idz2);
+    }
+    const int* bx = p.inj.box + shot * 6;
+    const bool inj_col = p.inj.on && j >= bx[2] && j < bx[3] && zl + V > bx[4] && zl < bx[5];
+    bool bad = false;
+    long long o = ((long long)(x0 + p.hx) * p.rows_y + (j + p.hy)) * p.ldz + kOZ + zl;
+    for (int i = x0; i < x1; ++i, o += xs) {
+        const T* u = p.u_cur + sh + o;
+        T w[NW];
+#pragma unroll
+        for (int q = 0; q <= 2 * NB; ++q) {
+            const VT a = ldv(u + (q - NB) * V);
+            const T* av = reinterpret_cast<const T*>(&a);
+#pragma unroll
+            for (int v = 0; v < V; ++v) w[q * V + v] = av[v];
+        }
+        VT xa[2 * R], ya[2 * R];
+#pragma unroll
+        for (int m = 1; m <= R; ++m) {
+            xa[R - m] = ldv(u - m * xs);
+            xa[R + m - 1] = ldv(u + m * xs);
+            ya[R - m] = ldv(u - m * ys);
+            ya[R + m - 1] = ldv(u + m * ys);
+        }
+        const VT uo_v = ldv_plain(p.u_prev + sh + o);
+        const VT c2_v = ldv(p.c2 + o);
+        VT dw_v, ic_v;
+        if (MODE == kAdj && p.image) {
+            dw_v = __ldcs(reinterpret_cast<const VT*>(p.dw_in + sh + o));
+            ic_v = ldv_plain(p.ic + sh + o);
+        }
+        const T* uov = reinterpret_cast<const T*>(&uo_v);
+        const T* c2v = reinterpret_cast<const T*>(&c2_v);
+        const T* dwv = reinterpret_cast<const T*>(&dw_v);
+        const T* icv = reinterpret_cast<const T*>(&ic_v);
+        T un[V], dwo[V], ico[V];
+#pragma unroll
+        for (int k2 = 0; k2 < V / 2; ++k2) {
+            const int v0 = 2 * k2;
+            auto pv = [&](const VT& a) {
+                const T* t = reinterpret_cast<const T*>(&a);
+                return O::mk(t[v0], t[v0 + 1]);
+            };
+            const P uc = O::mk(w[C0 + v0], w[C0 + v0 + 1]);
+            // Laplacian in difference form (the FP32 path depends on it), one chain per axis
+            P Fx = O::dup(T(0)), Fy = Fx, Fz = Fx;
+#pragma unroll
+            for (int m = 1; m <= R; ++m) {
+                Fx = O::fma(wx[m], O::add(O::sub(pv(xa[R + m - 1]), uc), O::sub(pv(xa[R - m]), uc)), Fx);
+                Fy = O::fma(wy[m], O::add(O::sub(pv(ya[R + m - 1]), uc), O::sub(pv(ya[R - m]), uc)), Fy);
+                const P zp = O::mk(w[C0 + v0 + m], w[C0 + v0 + 1 + m]);
+                const P zm = O::mk(w[C0 + v0 - m], w[C0 + v0 + 1 - m]);
+                Fz = O::fma(wz[m], O::add(O::sub(zp, uc), O::sub(zm, uc)), Fz);
+            }
+            P F = O::add(O::add(Fx, Fy), Fz);
+            if (inj_col) {
+                F.x += inject_rhs3(p.inj, bx, shot, i, j, zl + v0);
+                F.y += inject_rhs3(p.inj, bx, shot, i, j, zl + v0 + 1);
+            }
+            const P uo = O::mk(uov[v0], uov[v0 + 1]), c2 = O::mk(c2v[v0], c2v[v0 + 1]);
+            // u_{k+1} = dt^2 C^2 F - (u_{k-1} - 2 u_k)
+            const P q = O::fma(O::dup(T(-2)), uc, uo);
+            const P unew = O::fma(O::mul(O::dup(p.dt2), c2), F, O::mul(q, O::dup(T(-1))));
+            un[v0] = unew.x; un[v0 + 1] = unew.y;
+            if (MODE == kRecomp) {
+                const P d = O::mul(c2, F);
+                dwo[v0] = d.x; dwo[v0 + 1] = d.y;
+            }
+            if (MODE == kAdj) {
+                const P ic = O::fma(uc, O::mk(dwv[v0], dwv[v0 + 1]), O::mk(icv[v0], icv[v0 + 1]));
+                ico[v0] = ic.x; ico[v0 + 1] = ic.y;
+            }
+        }
+        *reinterpret_cast<VT*>(p.u_prev + sh + o) = *reinterpret_cast<const VT*>(un);
+        if (MODE == kRecomp && p.dw_out) __stcs(reinterpret_cast<VT*>(p.dw_out + sh + o), *reinterpret_cast<const VT*>(dwo));
+        if (MODE == kAdj && p.image) *reinterpret_cast<VT*>(p.ic + sh + o) = *reinterpret_cast<const VT*>(ico);
+        if (MODE == kFwd) {
+            T sum = T(0);
+#pragma unroll
+            for (int v = 0; v < V; ++v) sum += un[v];
+            bad |= !isfinite(sum);
+        }
+    }
+    if (MODE == kFwd && bad && p.err) atomicOr(p.err, PGB_ERR_NONFINITE);
 }
 
 // 1D: one axis (z), Phi_z only (_1D.h:117-129).
@@ -179,19 +345,18 @@ __global__ void __launch_bounds__(256) wave1d_kernel(const WaveParams<T> p, int 
 
 }  // namespace
 
-template <typename T, int R, int MODE>
-void launch_wave3d(const WaveParams<T>& p, int bz, cudaStream_t s) {
-    (void)bz;
-    const int tb = 64;
-    dim3 grd(ceil_div(p.nz, tb), p.ny, p.nx * p.nshot);
-    int recblk = 0;
-    if (MODE == kFwd && p.rec.nrec > 0) {
-        long long per = (long long)grd.x * tb * grd.y;
-        recblk = ceil_div((long long)p.nshot * p.rec.nrec, per);
-        grd.z += recblk;
-    }
-    wave3d_cell_kernel<T, R, MODE><<<grd, tb, 0, s>>>(p, recblk);
+template <typename T, int R, int MODE, int KIND>
+void launch_wave3d_tasks(const WaveParams<T>& p, const int* tasks, int ntasks, cudaStream_t s) {
+    if (ntasks <= 0) return;
+    const int grid = ntasks * p.nshot;
+    if (KIND == 0)
+        wave3d_interior_kernel<T, R, MODE><<<grid, kW3 * 32, 0, s>>>(p, tasks, ntasks);
+    else
+        wave3d_shell_kernel<T, R, MODE><<<grid, kW3 * 32, 0, s>>>(p, tasks, ntasks);
 }
+
+int wave3d_rows_per_block() { return kW3; }
+int wave3d_seg(int dtype_bytes, int kind) { return kind == 0 ? 32 * (16 / dtype_bytes) : 32; }
 
 template <typename T, int R, int MODE>
 void launch_wave1d(const WaveParams<T>& p, int bz, cudaStream_t s) {
@@ -203,10 +368,11 @@ void launch_wave1d(const WaveParams<T>& p, int bz, cudaStream_t s) {
     wave1d_kernel<T, R, MODE><<<grid, tb, 0, s>>>(p, ntile);
 }
 
+#define PGB_INST3K(T, R, M)                                                                            \
+    template void launch_wave3d_tasks<T, R, M, 0>(const WaveParams<T>&, const int*, int, cudaStream_t); \
+    template void launch_wave3d_tasks<T, R, M, 1>(const WaveParams<T>&, const int*, int, cudaStream_t);
 #define PGB_INST13(T, R)                                                                    \
-    template void launch_wave3d<T, R, kFwd>(const WaveParams<T>&, int, cudaStream_t);    \
-    template void launch_wave3d<T, R, kRecomp>(const WaveParams<T>&, int, cudaStream_t); \
-    template void launch_wave3d<T, R, kAdj>(const WaveParams<T>&, int, cudaStream_t);    \
+    PGB_INST3K(T, R, kFwd) PGB_INST3K(T, R, kRecomp) PGB_INST3K(T, R, kAdj)                 \
     template void launch_wave1d<T, R, kFwd>(const WaveParams<T>&, int, cudaStream_t);    \
     template void launch_wave1d<T, R, kRecomp>(const WaveParams<T>&, int, cudaStream_t); \
     template void launch_wave1d<T, R, kAdj>(const WaveParams<T>&, int, cudaStream_t);
