@@ -144,6 +144,9 @@ typedef struct {
     const double* rec_tap_wsample; /* host */
     const double* rec_tap_winject; /* host */
     int use_graph;                 /* capture the time loops in CUDA graphs (1) or launch eagerly (0) */
+    int psi_consistent;            /* 3D PML: 0 = the reference's step, which multiplies sigma_x sigma_y
+                                      sigma_z psi by C^2 (_3D.h:219; unstable at realistic PML amplitudes);
+                                      1 = that term without C^2, as in the reference's matrix operator */
 } pysit_plan_desc;
 
 int pysit_plan_create(const pysit_plan_desc* desc, pysit_plan** out);

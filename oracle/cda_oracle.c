@@ -223,8 +223,12 @@ int oracle_cda3d_step_##SUF(int order, const T* km1_u, const T* k_phix,         
             kp1_phiz[idx] = k_phiz[idx] - dt * sz * k_phiz[idx]                        \
                             + dt * (sx + sy - sz) * dudz + dt * (sx * sy * dpsidz);    \
             T fac1 = (T)(2.0 * dt2 / (2.0 + dt * (sx + sy + sz)));                     \
-            T fac2 = c2 * (rhs[idx] + lap + dphixdx + dphiydy + dphizdz                \
-                           - (sx * sy * sz) * k_psi[idx])                              \
+            T src = g_psi_consistent                                                   \
+                ? c2 * (rhs[idx] + lap + dphixdx + dphiydy + dphizdz)                  \
+                      - (sx * sy * sz) * k_psi[idx]                                    \
+                : c2 * (rhs[idx] + lap + dphixdx + dphiydy + dphizdz                   \
+                        - (sx * sy * sz) * k_psi[idx]);                                \
+            T fac2 = src                                                               \
                      - (um - 2.0 * uc) / dt2 + (sx + sy + sz) * um / (2.0 * dt)        \
                      - (sx * sy + sy * sz + sz * sx) * uc;                             \
             kp1_u[idx] = fac1 * fac2;                                                  \
@@ -238,6 +242,11 @@ int oracle_cda3d_step_##SUF(int order, const T* km1_u, const T* k_phix,         
     }                                                                                  \
     return 0;                                                                          \
 }
+
+/* 3D: 0 (default) = the reference's step (_3D.h:219, C^2 on sigma_x sigma_y sigma_z psi);
+ * 1 = that term without C^2, the form of the reference's matrix operator */
+int g_psi_consistent = 0;
+void oracle_set_psi_consistent(int on) { g_psi_consistent = on ? 1 : 0; }
 
 DEFINE_ORACLE(double, f64)
 DEFINE_ORACLE(float, f32)

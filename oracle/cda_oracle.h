@@ -38,6 +38,10 @@ int oracle_cda3d_step_##SUF(int order, const T* km1_u, const T* k_phix,         
 ORACLE_DECL(double, f64)
 ORACLE_DECL(float, f32)
 
+/* 3D psi term: 0 (default) = C^2 multiplies sigma_x sigma_y sigma_z psi, as the
+ * reference's step does (_3D.h:219); 1 = it does not (the matrix operator's form). */
+void oracle_set_psi_consistent(int on);
+
 #ifdef __cplusplus
 }
 #endif

@@ -99,6 +99,12 @@ def step(kind, dim, order, km1_u, k_aux, k_u, Cpad, rhs, profiles, dt, deltas, s
 AUX = {1: ("Phiz",), 2: ("Phix", "Phiz"), 3: ("Phix", "Phiy", "Phiz", "psi")}
 
 
+def set_psi_consistent(on):
+    """3D oracle step: False (default) multiplies sigma_x sigma_y sigma_z psi by C^2 as the
+    reference's _3D.h:219 does; True leaves C^2 out (the reference's matrix operator)."""
+    lib("oracle").oracle_set_psi_consistent(C.c_int(1 if on else 0))
+
+
 def dwaveop(P, um, uc, up, psi):
     """(u+ - 2u + u-)/dt^2 + S1 (u+ - u-)/(2dt) + S2 u (+ S3 psi in 3D), mesh sigma maps."""
     dim, dt = P["dim"], P["dt"]

@@ -52,6 +52,7 @@ class PlanDesc(C.Structure):
         ("rec_tap_point", C.POINTER(C.c_int32)), ("rec_tap_wsample", C.POINTER(_d)),
         ("rec_tap_winject", C.POINTER(_d)),
         ("use_graph", _i),
+        ("psi_consistent", _i),
     ]
 
 

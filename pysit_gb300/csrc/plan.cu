@@ -239,7 +239,7 @@ namespace {
 template <typename T>
 struct PlanT final : public pysit_plan {
     // ---- description -------------------------------------------------------
-    int dim, order, R, nx, ny, nz, nsteps, p_img, S, G, nshots, nsrc, nrec, use_graph;
+    int dim, order, R, nx, ny, nz, nsteps, p_img, S, G, nshots, nsrc, nrec, use_graph, psi_consistent;
     double dx, dy, dz, dt;
     int pad_lo[3], pad_hi[3];
     int pl[3], pr[3];  // PML-state widths (kernel profile lengths)
@@ -324,6 +324,7 @@ struct PlanT final : public pysit_plan {
         dt = d.dt; nsteps = d.nsteps; p_img = d.imaging_period; S = d.checkpoint_every;
         nshots = d.nshots; G = std::min(d.shots_per_launch, d.nshots); nsrc = d.nsrc; nrec = d.nrec;
         use_graph = d.use_graph;
+        psi_consistent = d.psi_consistent ? 1 : 0;
         for (int a = 0; a < 3; ++a) { pad_lo[a] = d.pad_lo[a]; pad_hi[a] = d.pad_hi[a]; }
         const int na[3] = {nx, ny, nz};
         for (int a = 0; a < 3; ++a) {
@@ -740,6 +741,7 @@ struct PlanT final : public pysit_plan {
         p.idy = T(1.0 / dy); p.idy2 = T(1.0 / (T(dy) * T(dy)));
         p.idz = T(1.0 / dz); p.idz2 = T(1.0 / (T(dz) * T(dz)));
         p.err = ws ? at<int>(off.err) : nullptr;
+        p.psi_c2 = psi_consistent ? 0 : 1;
         p.task_ctr = ws ? at<unsigned long long>(off.ctr) : nullptr;
         (void)g0;
         return p;

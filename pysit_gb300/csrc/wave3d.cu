@@ -102,8 +102,11 @@ __device__ __forceinline__ void cell3d(const WaveParams<T>& p, const int shot, c
         T ny_ = phy - p.dt * sy * phy + p.dt * (sz + sx - sy) * dudy + p.dt * (sz * sx * dpsy);
         T nz_ = phz - p.dt * sz * phz + p.dt * (sx + sy - sz) * dudz + p.dt * (sx * sy * dpsz);
         const T fac1 = T(2) * p.dt2 / (T(2) + p.dt * (sx + sy + sz));
-        const T fac2 = c2 * (F - (sx * sy * sz) * ps) - (uo - T(2) * uc) * p.idt2 +
-                       (sx + sy + sz) * uo * p.i2dt - (sx * sy + sy * sz + sz * sx) * uc;
+        // the reference multiplies sigma_x sigma_y sigma_z psi by C^2 (_3D.h:219); the
+        // consistent form (psi_c2 = 0) leaves it out, as the matrix operator does
+        const T src = p.psi_c2 ? c2 * (F - (sx * sy * sz) * ps) : c2 * F - (sx * sy * sz) * ps;
+        const T fac2 = src - (uo - T(2) * uc) * p.idt2 + (sx + sy + sz) * uo * p.i2dt -
+                       (sx * sy + sy * sz + sz * sx) * uc;
         unew = fac1 * fac2;
         if (!ok) { nx_ = ny_ = nz_ = unew = T(0); }
         p.phx_out[sh + o] = nx_;
@@ -116,7 +119,7 @@ __device__ __forceinline__ void cell3d(const WaveParams<T>& p, const int shot, c
     if (psireg) p.psi_out[sh + o] = ok ? ps + p.dt * uc : T(0);
     p.u_prev[sh + o] = unew;
     if (MODE == kRecomp && p.dw_out) {
-        T d = c2 * (F - (sx * sy * sz) * ps);
+        T d = p.psi_c2 ? c2 * (F - (sx * sy * sz) * ps) : c2 * F - (sx * sy * sz) * ps;
         const T mx = __ldg(p.mgx + i), my = __ldg(p.mgy + j), mz = __ldg(p.mgz + k);
         d += ((mx + my + mz) - (sx + sy + sz)) * (unew - uo) * p.i2dt +
              ((mx * my + my * mz + mz * mx) - (sx * sy + sy * sz + sz * sx)) * uc + (mx * my * mz) * ps;
@@ -132,10 +135,48 @@ __device__ __forceinline__ void cell3d(const WaveParams<T>& p, const int shot, c
 // 2R+1 planes around x stay in L1 while it marches, so u_k comes from DRAM
 // about once; the x- and y-neighbours are constant offsets from the centre row.
 constexpr int kW3 = 8;  // warps (y-rows) per block
+#ifndef PGB_3D_AHEAD
+#define PGB_3D_AHEAD 2     // rows ahead whose operands are prefetched into L1
+#endif
+
+// L1 prefetch of the line holding q (the addresses used are rows the task reads)
+__device__ __forceinline__ void pf_l1(const void* q) { asm volatile("prefetch.global.L1 [%0];" ::"l"(q)); }
+
+// the operands of row (i, j) that are not in L1 yet when the sweep gets there:
+// the new x-neighbour plane, the y-neighbour rows, u_{k-1}, C^2 (and the PML
+// state / adjoint operands); o is the element offset of the row's first cell
+template <typename T, int R, int MODE, bool PML>
+__device__ __forceinline__ void prefetch_row(const WaveParams<T>& p, long long sh, long long o) {
+    const long long ys = p.ldz, xs = (long long)p.rows_y * p.ldz;
+    pf_l1(p.u_cur + sh + o + R * xs);
+#pragma unroll
+    for (int m = 1; m <= R; ++m) {
+        pf_l1(p.u_cur + sh + o - m * ys);
+        pf_l1(p.u_cur + sh + o + m * ys);
+    }
+    pf_l1(p.u_prev + sh + o);
+    pf_l1(p.c2 + o);
+    if (MODE == kAdj && p.image) {
+        pf_l1(p.dw_in + sh + o);
+        pf_l1(p.ic + sh + o);
+    }
+    if (PML) {
+        pf_l1(p.phx_in + sh + o + R * xs);
+        pf_l1(p.phz_in + sh + o);
+#pragma unroll
+        for (int m = 1; m <= R; ++m) {
+            pf_l1(p.phy_in + sh + o - m * ys);
+            pf_l1(p.phy_in + sh + o + m * ys);
+        }
+    }
+}
 
 // PML shell: one cell per lane, the general per-cell update
+#ifndef PGB_3D_SHELL_MINB
+#define PGB_3D_SHELL_MINB 4  // resident shell blocks per SM the register budget aims at (64 registers)
+#endif
 template <typename T, int R, int MODE>
-__global__ void __launch_bounds__(kW3 * 32) wave3d_shell_kernel(const WaveParams<T> p, const int* __restrict__ tasks,
+__global__ void __launch_bounds__(kW3 * 32, PGB_3D_SHELL_MINB) wave3d_shell_kernel(const WaveParams<T> p, const int* __restrict__ tasks,
                                                                int ntasks) {
     const int shot = blockIdx.x / ntasks;
     const int* tk = tasks + 6 * (blockIdx.x - shot * ntasks);
@@ -143,7 +184,13 @@ __global__ void __launch_bounds__(kW3 * 32) wave3d_shell_kernel(const WaveParams
     const int k = __ldg(tk + 4) + (threadIdx.x & 31);
     if (j >= __ldg(tk + 3) || k >= __ldg(tk + 5)) return;
     const int x1 = __ldg(tk + 1);
-    for (int i = __ldg(tk); i < x1; ++i) cell3d<T, R, MODE>(p, shot, i, j, k);
+    const long long sh = (long long)shot * p.fstride;
+    const long long xs = (long long)p.rows_y * p.ldz;
+    const long long o0 = ((long long)(p.hx) * p.rows_y + (j + p.hy)) * p.ldz + kOZ + k;  // row x = 0
+    for (int i = __ldg(tk); i < x1; ++i) {
+        prefetch_row<T, R, MODE, true>(p, sh, o0 + (long long)min(i + PGB_3D_AHEAD, x1 - 1) * xs);
+        cell3d<T, R, MODE>(p, shot, i, j, k);
+    }
 }
 
 template <typename T> struct Vec3;
@@ -189,8 +236,11 @@ __device__ __forceinline__ typename Vec3<T>::type ldv_plain(const T* q) {
 // Interior: 16-byte vectors (V cells per lane), arithmetic on cell pairs, no PML
 // state (every tap is off the padding), no masks (off the outer ring).  Task
 // z-bounds are multiples of 4 cells, so every vector load is aligned.
+#ifndef PGB_3D_INT_MINB
+#define PGB_3D_INT_MINB 2  // resident interior blocks per SM the register budget aims at (FP32)
+#endif
 template <typename T, int R, int MODE>
-__global__ void __launch_bounds__(kW3 * 32, (sizeof(T) == 4 ? 2 : 1))
+__global__ void __launch_bounds__(kW3 * 32, (sizeof(T) == 4 ? PGB_3D_INT_MINB : 1))
     wave3d_interior_kernel(const WaveParams<T> p, const int* __restrict__ tasks, int ntasks) {
     using O = Pair3<T>;
     using P = typename O::P;
@@ -221,6 +271,7 @@ __global__ void __launch_bounds__(kW3 * 32, (sizeof(T) == 4 ? 2 : 1))
     bool bad = false;
     long long o = ((long long)(x0 + p.hx) * p.rows_y + (j + p.hy)) * p.ldz + kOZ + zl;
     for (int i = x0; i < x1; ++i, o += xs) {
+        prefetch_row<T, R, MODE, false>(p, sh, o + (long long)(min(i + PGB_3D_AHEAD, x1 - 1) - i) * xs);
         const T* u = p.u_cur + sh + o;
         T w[NW];
 #pragma unroll

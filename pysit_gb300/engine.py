@@ -98,6 +98,7 @@ class WavePlan:
         d.shots_per_launch = self.shots_per_launch
         d.nshots = self.nshots
         d.use_graph = 1 if use_graph else 0
+        d.psi_consistent = 1 if getattr(solver, "pml_psi", "reference") == "consistent" else 0
 
         ts = np.arange(self.nsteps) * self.dt
         # sources
@@ -251,7 +252,8 @@ class WavePlan:
 def plan_for(solver, shots, imaging_period=1, **kw):
     """Cached WavePlan of a solver for a shot list (rebuilt when dt/nsteps change)."""
     key = (tuple(id(s) for s in shots), solver.dt, solver.nsteps, solver.precision,
-           solver.spatial_accuracy_order, int(imaging_period), tuple(sorted(kw.items())))
+           solver.spatial_accuracy_order, getattr(solver, "pml_psi", "reference"), int(imaging_period),
+           tuple(sorted(kw.items())))
     cache = solver._plans
     p = cache.get(key)
     if p is None:

@@ -170,13 +170,15 @@ class _CDATimeScalarCuda:
 
     def __init__(self, mesh, spatial_accuracy_order=4, trange=(0.0, 1.0), cfl_safety=1 / 6,
                  precision="double", checkpoint_every=None, shots_per_launch=None, use_graph=True,
-                 **kwargs):
+                 pml_psi="reference", **kwargs):
         if mesh.dim != self._dim:
             raise ValueError(f"{type(self).__name__} needs a {self._dim}D mesh")
         if spatial_accuracy_order not in (2, 4, 6, 8):
             raise ValueError("spatial_accuracy_order must be one of 2, 4, 6, 8")
         if precision not in ("single", "double"):
             raise ValueError("precision must be 'single' or 'double'")
+        if pml_psi not in ("reference", "consistent"):
+            raise ValueError("pml_psi must be 'reference' or 'consistent'")
         for i in range(mesh.dim):
             for bc in (mesh.parameters[i].lbc, mesh.parameters[i].rbc):
                 if bc.type == "pml" and getattr(bc.domain_bc, "compact", False):
@@ -194,6 +196,10 @@ class _CDATimeScalarCuda:
         self.checkpoint_every = checkpoint_every
         self.shots_per_launch = shots_per_launch
         self.use_graph = use_graph
+        # 3D batched path: 'reference' reproduces the reference's step, whose C^2 on
+        # sigma_x sigma_y sigma_z psi (_3D.h:219) makes the PML unstable at realistic
+        # amplitudes; 'consistent' drops that C^2 (the matrix operator's form)
+        self.pml_psi = pml_psi
         self._mp = None
         self._model_change_count = 0
         self._C_dev = None

@@ -64,8 +64,13 @@ def cfg2(scale=1.0, nshots=64, nsteps=4000, order=8, precision="single", cfl=0.4
 
 
 def cfg3(scale=1.0, nshots=8, nsteps=3000, order=8, precision="single", cfl=0.35, checkpoint_every=None,
-         shots_per_launch=1, seed=2027):
-    """(mesh, shots, solver, C_true, C_start) of the 3D gradient workload."""
+         shots_per_launch=1, seed=2027, pml_psi="consistent"):
+    """(mesh, shots, solver, C_true, C_start) of the 3D gradient workload.
+
+    Its PML amplitude (1e-3 reflection over 20 cells) makes the reference's 3D
+    step diverge (C^2 on sigma_x sigma_y sigma_z psi, _3D.h:219), so the workload
+    uses the consistent form by default; ``pml_psi="reference"`` reproduces the
+    reference's step."""
     nx, ny, nz = (max(12, int(round(n * scale))) for n in (400, 400, 300))
     npml = max(4, int(round(20 * scale)))
     dx = 15.0
@@ -82,12 +87,13 @@ def cfg3(scale=1.0, nshots=8, nsteps=3000, order=8, precision="single", cfl=0.35
     C = np.where(salt.reshape(C.shape), 4500.0, C)
     C0 = gaussian_filter(C, sigma=10 * max(scale, 0.1), mode="nearest")
     T = _steps_T(C0, m.deltas, cfl, nsteps)
-    nsx = max(1, int(round(math.sqrt(nshots))))
-    shots = core.equispaced_acquisition(m, core.RickerWavelet(6.0), sources=(nsx, max(1, nshots // nsx)),
+    # a source grid of exactly nshots points, as square as the divisors allow
+    nsx = max(d for d in range(1, int(math.isqrt(nshots)) + 1) if nshots % d == 0)
+    shots = core.equispaced_acquisition(m, core.RickerWavelet(6.0), sources=(nshots // nsx, nsx),
                                         receivers=(min(100, nx), min(100, ny)), source_depth=0.0,
                                         receiver_depth=0.0)
     solver = solvers.ConstantDensityAcousticWave(m, spatial_accuracy_order=order, trange=(0.0, T),
                                                  kernel_implementation="cuda", precision=precision,
                                                  cfl_safety=cfl, checkpoint_every=checkpoint_every,
-                                                 shots_per_launch=shots_per_launch)
+                                                 shots_per_launch=shots_per_launch, pml_psi=pml_psi)
     return m, shots, solver, C, C0

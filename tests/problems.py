@@ -56,8 +56,10 @@ def _models(mesh, spec):
     return C, C0
 
 
-def build(api, name, kernel="cuda", precision="double"):
-    spec = SPECS[name]
+def build(api, name, kernel="cuda", precision="double", spec_overrides=None, **solver_kw):
+    """(mesh, shots, solver, C_true, C_start) of problem `name`; spec_overrides replaces
+    entries of its spec (e.g. the PML), solver_kw go to the solver."""
+    spec = dict(SPECS[name], **(spec_overrides or {}))
     cells, amp = spec["pml"]
     dim = spec["dim"]
     deltas = [L / (n - 1) for L, n in zip(spec["L"], spec["n"])]
@@ -83,6 +85,7 @@ def build(api, name, kernel="cuda", precision="double"):
               cfl_safety=spec["cfl"])
     if precision != "double":
         kw["precision"] = precision
+    kw.update(solver_kw)
     solver = api.ConstantDensityAcousticWave(m, **kw)
     return m, shots, solver, C, C0
 
