@@ -214,6 +214,7 @@ def main():
     ts_obs = solver.ts()
     fplan = WavePlan(solver, shots, checkpoint_every=solver.checkpoint_every,
                      shots_per_launch=args.shots_per_launch)
+    tuned = fplan.autotune()  # task length along x (untimed setup; later plans reuse it)
     obs_dev = fplan.forward().clone()
     # kernel roofline: the forward step kernel, graph of nsteps launches
     torch.cuda.synchronize()
@@ -331,7 +332,8 @@ def main():
                                        "frac": v["achieved_gbs"] / peak} for k, v in modes.items()},
                          "forward_graph": {"launch_ms": fwd_launch_ms, "achieved_gbs": achieved,
                                            "gcell_per_s": fwd_gcells}},
-            "gpu_launches": launches, "misfit_rnorm2": rn, "clocks": clocks}
+            "gpu_launches": launches, "misfit_rnorm2": rn, "clocks": clocks,
+            "autotune": {"tile_x": tuned["chosen"], "ms": {str(k): v for k, v in tuned["ms"].items()}}}
     if rank == 0 and not args.no_plain:
         plain = plain_fp64_baseline(scale=args.scale, nsteps_full=args.nsteps)
         plain["batched_over_plain"] = line["value"] / world / plain["value"]

@@ -147,6 +147,8 @@ typedef struct {
     int psi_consistent;            /* 3D PML: 0 = the reference's step, which multiplies sigma_x sigma_y
                                       sigma_z psi by C^2 (_3D.h:219; unstable at realistic PML amplitudes);
                                       1 = that term without C^2, as in the reference's matrix operator */
+    int tile_x;                    /* 2D/3D task length along x in rows; 0 = the default (32 in 2D, 64 in 3D);
+                                      pysit_plan_autotune chooses it by timing */
 } pysit_plan_desc;
 
 int pysit_plan_create(const pysit_plan_desc* desc, pysit_plan** out);
@@ -209,6 +211,16 @@ int pysit_plan_last_launch_count(const pysit_plan* plan, int64_t* launches);
  * buffers keep evolving from whatever the previous run left; nothing is
  * returned and the next forward/gradient call starts from scratch. */
 int pysit_plan_step_loop(pysit_plan* plan, int mode, int nsteps, void* stream);
+
+/* Autotuner, no counterpart in the reference (its kernels have no tiles): times
+ * `nsteps` forward and `nsteps` adjoint steps (as pysit_plan_step_loop does) for
+ * each of the `ncand` task lengths along x in `candidates` (8..4096 rows), keeps
+ * the fastest, writes it to *chosen and the measured milliseconds per candidate to
+ * ms[ncand] (may be NULL).  Needs a bound workspace and a model; 2D and 3D plans.
+ * It drops the plan's captured graphs (they hold the old task tables); the
+ * wavefield buffers are left in an arbitrary state, as after step_loop. */
+int pysit_plan_autotune(pysit_plan* plan, const int* candidates, int ncand, int nsteps, int* chosen,
+                        double* ms, void* stream);
 
 #ifdef __cplusplus
 }

@@ -53,6 +53,7 @@ class PlanDesc(C.Structure):
         ("rec_tap_winject", C.POINTER(_d)),
         ("use_graph", _i),
         ("psi_consistent", _i),
+        ("tile_x", _i),
     ]
 
 
@@ -81,6 +82,7 @@ _PROTOS = {
     "pysit_misfit_per_shot_noalloc": (_i, [_i, _vp, _vp, _i, C.c_int64, _vp, _vp, _vp]),
     "pysit_plan_last_launch_count": (_i, [_vp, C.POINTER(C.c_int64)]),
     "pysit_plan_step_loop": (_i, [_vp, _i, _i, _vp]),
+    "pysit_plan_autotune": (_i, [_vp, C.POINTER(_i), _i, _i, C.POINTER(_i), C.POINTER(C.c_double), _vp]),
 }
 
 _lib = None

@@ -230,6 +230,7 @@ struct pysit_plan {
                          cudaStream_t s, bool with_grad, bool migrate) = 0;
     virtual int status(int* flags, cudaStream_t s) = 0;
     virtual int step_loop(int mode, int nsteps, cudaStream_t s) = 0;
+    virtual int autotune(const int* cand, int ncand, int nsteps, int* chosen, double* ms, cudaStream_t s) = 0;
     int64_t last_launches = 0;
 };
 
@@ -240,6 +241,8 @@ template <typename T>
 struct PlanT final : public pysit_plan {
     // ---- description -------------------------------------------------------
     int dim, order, R, nx, ny, nz, nsteps, p_img, S, G, nshots, nsrc, nrec, use_graph, psi_consistent;
+    int tile_req = 0;            // requested task length along x (0: default)
+    size_t task_cap = 0;         // ints the task buffer holds (enough for the shortest x-chunk)
     double dx, dy, dz, dt;
     int pad_lo[3], pad_hi[3];
     int pl[3], pr[3];  // PML-state widths (kernel profile lengths)
@@ -325,6 +328,7 @@ struct PlanT final : public pysit_plan {
         nshots = d.nshots; G = std::min(d.shots_per_launch, d.nshots); nsrc = d.nsrc; nrec = d.nrec;
         use_graph = d.use_graph;
         psi_consistent = d.psi_consistent ? 1 : 0;
+        tile_req = d.tile_x > 0 ? d.tile_x : 0;
         for (int a = 0; a < 3; ++a) { pad_lo[a] = d.pad_lo[a]; pad_hi[a] = d.pad_hi[a]; }
         const int na[3] = {nx, ny, nz};
         for (int a = 0; a < 3; ++a) {
@@ -381,7 +385,7 @@ struct PlanT final : public pysit_plan {
             warp2d = !(k && strcmp(k, "tma") == 0);
             if (warp2d) {
                 bz = wave2d_warp_threads();
-                tx = have ? etx : 32;
+                tx = have ? etx : tile_req ? tile_req : 32;
                 build_tasks2d();
                 ntz = ntx = 1;
                 return;
@@ -395,7 +399,7 @@ struct PlanT final : public pysit_plan {
         }
         if (dim == 3) {
             bz = 128;  // threads of the recorder blocks
-            tx = have ? etx : 64;
+            tx = have ? etx : tile_req ? tile_req : 64;
             build_tasks3d();
             ntz = ntx = 1;
             return;
@@ -497,6 +501,19 @@ struct PlanT final : public pysit_plan {
             add_tasks3d(xa, xb, ya, yb, zb, nz, 1); // high-z slab
         }
         ntask3d[1] = (int)(tasks3d.size() / 6) - ntask3d[0];
+    }
+
+    // ints of the task table for a task length tx_try (the current table is kept)
+    static constexpr int kMinTileX = 8;
+    size_t task_ints(int tx_try) {
+        if (!((dim == 2 && warp2d) || dim == 3)) return 0;
+        const int keep = tx;
+        tx = tx_try;
+        size_t n;
+        if (dim == 2) { build_tasks2d(); n = tasks2d.size(); } else { build_tasks3d(); n = tasks3d.size(); }
+        tx = keep;
+        if (dim == 2) build_tasks2d(); else build_tasks3d();
+        return n;
     }
 
     long long internal_offset(long long cell) const {
@@ -621,7 +638,8 @@ struct PlanT final : public pysit_plan {
         off.gpad = take((size_t)nx * ny * nz * sizeof(double));
         off.err = take(sizeof(int));
         off.ctr = take(2 * sizeof(unsigned long long));
-        off.tasks = take(std::max<size_t>(std::max(tasks2d.size(), tasks3d.size()), 1) * sizeof(int));
+        task_cap = std::max<size_t>(task_ints(kMinTileX), std::max(tasks2d.size(), tasks3d.size()));
+        off.tasks = take(std::max<size_t>(task_cap, 1) * sizeof(int));
         off.partial = take(kRedBlocks * sizeof(double));
         off.rnorm = take(sizeof(double));
         ws_need = tot;
@@ -1041,6 +1059,55 @@ struct PlanT final : public pysit_plan {
         return PYSIT_OK;
     }
 
+    int autotune(const int* cand, int ncand, int n, int* chosen, double* ms_out, cudaStream_t s) override {
+        PGB_REQUIRE(ws, "no workspace bound");
+        PGB_REQUIRE(model_set, "pysit_plan_set_model must be called first");
+        PGB_REQUIRE((dim == 2 && warp2d) || dim == 3, "autotuning applies to the 2D and 3D task sweeps");
+        PGB_REQUIRE(cand && ncand >= 1 && chosen, "need at least one candidate and an output");
+        PGB_REQUIRE(n >= 1, "nsteps must be >= 1");
+        for (int c = 0; c < ncand; ++c)
+            PGB_REQUIRE(cand[c] >= kMinTileX && cand[c] <= 4096, "candidate task length %d outside [%d, 4096]",
+                        cand[c], kMinTileX);
+        cudaEvent_t e0, e1;
+        PGB_CHECK_CUDA(cudaEventCreate(&e0));
+        PGB_CHECK_CUDA(cudaEventCreate(&e1));
+        int best = cand[0];
+        float best_ms = 1e30f;
+        int rc = PYSIT_OK;
+        for (int c = 0; c < ncand && rc == PYSIT_OK; ++c) {
+            if ((rc = use_tile(cand[c], s))) break;
+            if ((rc = step_loop(kFwd, 2, s))) break;  // warm-up
+            cudaEventRecord(e0, s);
+            if ((rc = step_loop(kFwd, n, s)) || (rc = step_loop(kAdj, n, s))) break;
+            cudaEventRecord(e1, s);
+            if (cudaEventSynchronize(e1) != cudaSuccess) { rc = cuda_status(cudaGetLastError(), "autotune"); break; }
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (ms_out) ms_out[c] = ms;
+            if (ms < best_ms) { best_ms = ms; best = cand[c]; }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        if (rc) return rc;
+        if ((rc = use_tile(best, s))) return rc;
+        *chosen = best;
+        return PYSIT_OK;
+    }
+
+    // rebuild and upload the task table for task length t; captured graphs hold the
+    // old table's counts, so they are dropped
+    int use_tile(int t, cudaStream_t s) {
+        tx = t;
+        std::vector<int>& tab = dim == 3 ? (build_tasks3d(), tasks3d) : (build_tasks2d(), tasks2d);
+        PGB_REQUIRE(tab.size() <= task_cap, "task table of %zu ints exceeds its buffer (%zu)", tab.size(), task_cap);
+        PGB_CHECK_CUDA(cudaMemcpyAsync(ws + off.tasks, tab.data(), tab.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+        PGB_CHECK_CUDA(cudaStreamSynchronize(s));
+        for (auto& kv : graphs)
+            if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+        graphs.clear();
+        return PYSIT_OK;
+    }
+
     void set_recording(WaveParams<T>& p, int g0, int gn, T* tr_k) const {
         p.rec.rowptr = at<int>(off.recrow) + (size_t)g0 * nrec;
         p.rec.off = at<long long>(off.recoff);
@@ -1257,4 +1324,10 @@ extern "C" int pysit_plan_last_launch_count(const pysit_plan* p, int64_t* n) {
 extern "C" int pysit_plan_step_loop(pysit_plan* p, int mode, int nsteps, void* stream) {
     PGB_REQUIRE(p, "NULL plan");
     return p->step_loop(mode, nsteps, (cudaStream_t)stream);
+}
+
+extern "C" int pysit_plan_autotune(pysit_plan* p, const int* candidates, int ncand, int nsteps, int* chosen,
+                                   double* ms, void* stream) {
+    PGB_REQUIRE(p, "NULL plan");
+    return p->autotune(candidates, ncand, nsteps, chosen, ms, (cudaStream_t)stream);
 }

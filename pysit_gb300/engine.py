@@ -23,6 +23,11 @@ __all__ = ["WavePlan", "padded_cells", "default_checkpoint_every"]
 
 _DESC_AXIS = {1: [2], 2: [0, 2], 3: [0, 1, 2]}  # mesh axis -> (x, y, z) slot of the descriptor
 
+# task lengths along x chosen by WavePlan.autotune, per (dim, order, padded grid, dtype,
+# shots per launch, psi form); later plans of the same configuration start from them
+_TUNED = {}
+TILE_CANDIDATES = {2: (16, 32, 64), 3: (16, 32, 64, 128)}
+
 
 def padded_cells(mesh, cells):
     """Map flat indices of the unpadded grid to flat indices of the padded grid."""
@@ -99,6 +104,10 @@ class WavePlan:
         d.nshots = self.nshots
         d.use_graph = 1 if use_graph else 0
         d.psi_consistent = 1 if getattr(solver, "pml_psi", "reference") == "consistent" else 0
+        self._tune_key = (self.dim, solver.spatial_accuracy_order, tuple(full), str(solver.dtype),
+                          self.shots_per_launch, d.psi_consistent)
+        d.tile_x = _TUNED.get(self._tune_key, 0)
+        self.tile_x = d.tile_x
 
         ts = np.arange(self.nsteps) * self.dt
         # sources
@@ -229,6 +238,23 @@ class WavePlan:
             C.c_void_p(self.rnorm2.data_ptr()), C.c_void_p(_native.stream_handle())))
         return self.grad
 
+    def autotune(self, candidates=None, nsteps=16):
+        """Time the task lengths along x in `candidates` (forward + adjoint steps on this plan's
+        buffers), keep the fastest for this plan and for later plans of the same configuration.
+        Returns {"chosen": rows, "ms": {candidate: milliseconds}}.  1D plans have no tiles."""
+        if self.dim == 1:
+            return {"chosen": 0, "ms": {}}
+        cand = list(candidates or TILE_CANDIDATES[self.dim])
+        self.set_model()
+        arr = (C.c_int * len(cand))(*cand)
+        ms = (C.c_double * len(cand))()
+        chosen = C.c_int()
+        _native.check(_native.load().pysit_plan_autotune(self._h, arr, len(cand), int(nsteps), C.byref(chosen), ms,
+                                                         C.c_void_p(_native.stream_handle())))
+        self.tile_x = int(chosen.value)
+        _TUNED[self._tune_key] = self.tile_x
+        return {"chosen": self.tile_x, "ms": dict(zip(cand, list(ms)))}
+
     def step_loop(self, mode, nsteps):
         """Enqueue `nsteps` launches of one step kernel (0 forward, 1 recompute, 2 adjoint) on the
         plan's own buffers, for timing one kernel; returns nothing useful (benchmarking aid)."""
@@ -261,5 +287,7 @@ def plan_for(solver, shots, imaging_period=1, **kw):
         while len(cache) >= 2:
             cache.pop(next(iter(cache)))
         p = WavePlan(solver, shots, imaging_period=imaging_period, **kw)
+        if getattr(solver, "autotune", False) and p._tune_key not in _TUNED:
+            p.autotune()
         cache[key] = p
     return p

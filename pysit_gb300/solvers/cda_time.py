@@ -170,7 +170,7 @@ class _CDATimeScalarCuda:
 
     def __init__(self, mesh, spatial_accuracy_order=4, trange=(0.0, 1.0), cfl_safety=1 / 6,
                  precision="double", checkpoint_every=None, shots_per_launch=None, use_graph=True,
-                 pml_psi="reference", **kwargs):
+                 pml_psi="reference", autotune=False, **kwargs):
         if mesh.dim != self._dim:
             raise ValueError(f"{type(self).__name__} needs a {self._dim}D mesh")
         if spatial_accuracy_order not in (2, 4, 6, 8):
@@ -200,6 +200,8 @@ class _CDATimeScalarCuda:
         # sigma_x sigma_y sigma_z psi (_3D.h:219) makes the PML unstable at realistic
         # amplitudes; 'consistent' drops that C^2 (the matrix operator's form)
         self.pml_psi = pml_psi
+        # choose the 2D/3D task length along x by timing when a batched plan is first built
+        self.autotune = autotune
         self._mp = None
         self._model_change_count = 0
         self._C_dev = None

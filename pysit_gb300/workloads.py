@@ -59,7 +59,7 @@ def cfg2(scale=1.0, nshots=64, nsteps=4000, order=8, precision="single", cfl=0.4
     solver = solvers.ConstantDensityAcousticWave(m, spatial_accuracy_order=order, trange=(0.0, T),
                                                  kernel_implementation="cuda", precision=precision,
                                                  cfl_safety=cfl, checkpoint_every=checkpoint_every,
-                                                 shots_per_launch=shots_per_launch)
+                                                 shots_per_launch=shots_per_launch, autotune=True)
     return m, shots, solver, C, C0
 
 
@@ -95,5 +95,6 @@ def cfg3(scale=1.0, nshots=8, nsteps=3000, order=8, precision="single", cfl=0.35
     solver = solvers.ConstantDensityAcousticWave(m, spatial_accuracy_order=order, trange=(0.0, T),
                                                  kernel_implementation="cuda", precision=precision,
                                                  cfl_safety=cfl, checkpoint_every=checkpoint_every,
-                                                 shots_per_launch=shots_per_launch, pml_psi=pml_psi)
+                                                 shots_per_launch=shots_per_launch, pml_psi=pml_psi,
+                                                 autotune=True)
     return m, shots, solver, C, C0

@@ -109,6 +109,10 @@ def test_plan_create_reports_workspace_and_destroys(lib):
     assert rc == _native.PYSIT_EINVAL
     assert lib.pysit_plan_step_loop(h, 0, 4, None) == _native.PYSIT_EINVAL
     assert b"no workspace" in lib.pysit_cuda_last_error()
+    cand = (C.c_int * 2)(16, 32)
+    chosen = C.c_int()
+    assert lib.pysit_plan_autotune(h, cand, 2, 4, C.byref(chosen), None, None) == _native.PYSIT_EINVAL
+    assert b"no workspace" in lib.pysit_cuda_last_error()
     _native.check(lib.pysit_plan_destroy(h))
 
 

@@ -181,3 +181,19 @@ def test_status_word_clear_after_stable_run_and_flags_instability():
     plan.forward()
     assert plan.status() & 2
     assert plan.status() == 0  # reading clears the word
+
+
+@pytest.mark.parametrize("name", ["o8", "3d"])
+def test_autotuned_tiles_keep_the_gradient(name, golden):
+    """The autotuner rebuilds the task table with the fastest x-length; the gradient is unchanged."""
+    from pysit_gb300.engine import WavePlan
+    g = golden(name)
+    m, shots, solver, C, C0 = _setup(name, g)
+    solver.model_parameters = solver.ModelParameters(m, {"C": C0})
+    plan = WavePlan(solver, shots)
+    plan.load_observed()
+    res = plan.autotune(candidates=(8, 16, 48), nsteps=4)
+    assert res["chosen"] in (8, 16, 48) and len(res["ms"]) == 3 and all(v > 0 for v in res["ms"].values())
+    grad, rn = plan.gradient()
+    assert plan.status() == 0
+    assert _rel(grad.cpu().numpy(), g["grad"]) < 1e-9
