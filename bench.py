@@ -72,7 +72,7 @@ def _cpu_worker(args):
     return time.perf_counter() - t0
 
 
-def plain_fp64_baseline(scale=1.0, nsteps_full=4000, nsample=256, order=8):
+def plain_fp64_baseline(scale=1.0, nsteps_full=4000, nsample=1024, order=8):
     """The plain path on the GPU: PySIT's per-shot, per-step control flow
     (TemporalLeastSquares.compute_gradient, temporal_least_squares.py:141-198) in FP64 over the
     per-step CUDA kernels, one shot of the same grid timed over `nsample` steps and extrapolated

@@ -9,7 +9,13 @@ No public dataset is involved: each model is generated from a named seed.
   cfg3  3D FWI gradient: 400 x 400 x 300 cells at 15 m + 20-cell PML, order 8,
         layered + smoothed perturbation + Gaussian salt body at 4500 m/s,
         8 shots, 100 x 100 receivers, 6 Hz, 3000 steps.
+  cfg5  end-to-end FWI: PySIT's LBFGS (memory 10, backtracking) for 20 iterations
+        on the cfg2 model with 128 shots, from the sigma = 30 smoothed model.
 ``scale`` shrinks a workload uniformly (cells per axis, shots, steps) for tests.
+
+``python -m pysit_gb300.workloads cfg5 [--iterations N] [--shots N] [--scale s]
+[--nsteps N] [--plain]`` runs the FWI and prints one JSON line (objective history,
+relative L2 error of the final model, wall time).
 """
 from __future__ import annotations
 
@@ -20,7 +26,7 @@ from scipy.ndimage import gaussian_filter
 
 from . import core, solvers
 
-__all__ = ["layered_model", "cfg2", "cfg3"]
+__all__ = ["layered_model", "cfg2", "cfg3", "cfg5", "run_lbfgs"]
 
 
 def layered_model(shape, nlayers, vmin, vmax, sigma_cells, amp, seed, clip=(1500.0, 5500.0)):
@@ -98,3 +104,63 @@ def cfg3(scale=1.0, nshots=8, nsteps=3000, order=8, precision="single", cfl=0.35
                                                  shots_per_launch=shots_per_launch, pml_psi=pml_psi,
                                                  autotune=True)
     return m, shots, solver, C, C0
+
+
+def cfg5(scale=1.0, nshots=128, nsteps=4000, precision="single", shots_per_launch=64, **kw):
+    """(mesh, shots, solver, C_true, C_start) of the end-to-end FWI workload: the cfg2 model
+    and start model with 128 shots (64 per launch keeps two plans within HBM)."""
+    return cfg2(scale=scale, nshots=nshots, nsteps=nsteps, precision=precision,
+                shots_per_launch=shots_per_launch, **kw)
+
+
+def run_lbfgs(m, shots, solver, C, C0, iterations=20, memory_length=10, batched=True, verbose=False):
+    """PySIT's LBFGS on data modelled at C, started from C0, with the GPU objective.
+    Returns the objective history, the relative L2 error of the final model to C,
+    and the wall time of the optimisation (the data modelling excluded)."""
+    import time
+
+    from .modeling import generate_seismic_data
+    from .objective_functions import TemporalLeastSquares
+    from .optimization import LBFGS
+
+    generate_seismic_data(shots, solver, solver.ModelParameters(m, {"C": C}))
+    objective = TemporalLeastSquares(solver, batched=batched)
+    opt = LBFGS(objective, memory_length=memory_length)
+    t0 = time.perf_counter()
+    final = opt(shots, solver.ModelParameters(m, {"C": C0}), iterations, line_search="backtrack",
+                status_configuration={"objective_frequency": 1, "gradient_length_frequency": 1},
+                verbose=verbose)
+    seconds = time.perf_counter() - t0
+    _, hist = opt.retrieve_history("objective")
+    _, alpha = opt.retrieve_history("alpha")
+    Cf = np.asarray(final.C).reshape(-1)
+    Ct = np.asarray(C).reshape(-1)
+    C0f = np.asarray(C0).reshape(-1)
+    return {"objective": [float(v) for v in hist], "alpha": [float(a) for a in alpha],
+            "rel_model_error": float(np.linalg.norm(Cf - Ct) / np.linalg.norm(Ct)),
+            "rel_model_error_start": float(np.linalg.norm(C0f - Ct) / np.linalg.norm(Ct)),
+            "seconds": seconds, "iterations": iterations, "shots": len(shots), "nsteps": solver.nsteps}
+
+
+def _main(argv=None):
+    import argparse
+    import json
+
+    ap = argparse.ArgumentParser(prog="python -m pysit_gb300.workloads")
+    ap.add_argument("workload", choices=["cfg5"])
+    ap.add_argument("--iterations", type=int, default=20)
+    ap.add_argument("--shots", type=int, default=128)
+    ap.add_argument("--nsteps", type=int, default=4000)
+    ap.add_argument("--scale", type=float, default=1.0)
+    ap.add_argument("--plain", action="store_true", help="per-shot FP64 objective instead of the batched FP32 one")
+    ap.add_argument("--verbose", action="store_true")
+    a = ap.parse_args(argv)
+    prec = "double" if a.plain else "single"
+    m, shots, solver, C, C0 = cfg5(scale=a.scale, nshots=a.shots, nsteps=a.nsteps, precision=prec)
+    out = run_lbfgs(m, shots, solver, C, C0, iterations=a.iterations, batched=not a.plain, verbose=a.verbose)
+    out.update(workload=a.workload, path="plain FP64" if a.plain else "batched FP32", scale=a.scale)
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    _main()
