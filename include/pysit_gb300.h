@@ -149,6 +149,9 @@ typedef struct {
                                       1 = that term without C^2, as in the reference's matrix operator */
     int tile_x;                    /* 2D/3D task length along x in rows; 0 = the default (32 in 2D, 64 in 3D);
                                       pysit_plan_autotune chooses it by timing */
+    const int32_t* shot_nsteps;    /* host [nshots] or NULL: the record length of each shot in steps
+                                      (1..nsteps); the residual of a shot is zero from its length on, so
+                                      its misfit and gradient are those of a run of that many steps */
 } pysit_plan_desc;
 
 int pysit_plan_create(const pysit_plan_desc* desc, pysit_plan** out);
@@ -221,6 +224,21 @@ int pysit_plan_step_loop(pysit_plan* plan, int mode, int nsteps, void* stream);
  * wavefield buffers are left in an arbitrary state, as after step_loop. */
 int pysit_plan_autotune(pysit_plan* plan, const int* candidates, int ncand, int nsteps, int* chosen,
                         double* ms, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Plan groups, no counterpart in the reference (it runs shots one after the
+ * other): several plans (different grids, orders or record lengths) whose
+ * gradients run concurrently, captured together in one CUDA graph - each plan
+ * on a stream of its own forked from the caller's stream and joined back.
+ * The plans stay owned by the caller and must outlive the group.
+ * ------------------------------------------------------------------------ */
+typedef struct pysit_group pysit_group;
+int pysit_group_create(pysit_plan* const* plans, int nplans, pysit_group** out);
+int pysit_group_destroy(pysit_group* group);
+/* Misfit and gradient of every plan: dobs[i], grad[i], rnorm2[i] as for
+ * pysit_plan_gradient of plan i.  The graph is cached per set of pointers. */
+int pysit_group_gradient(pysit_group* group, const void* const* dobs, double* const* grad,
+                         double* const* rnorm2, void* stream);
 
 #ifdef __cplusplus
 }

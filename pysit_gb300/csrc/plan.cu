@@ -124,11 +124,18 @@ template <typename T>
 __global__ void __launch_bounds__(kRedThreads) residual_kernel(const T* __restrict__ dobs,
                                                                T* __restrict__ tr, long long n,
                                                                double* __restrict__ partial,
-                                                               int operand) {
+                                                               int operand, const int* __restrict__ shot_steps,
+                                                               int nsteps, int nrec) {
     double acc = 0.0;
+    const long long per_shot = (long long)nsteps * nrec;
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
          c += (long long)gridDim.x * blockDim.x) {
         T r = operand ? dobs[c] : dobs[c] - tr[c];
+        // a shot's record ends at its own length: no residual after it
+        if (shot_steps) {
+            const long long sh = c / per_shot;
+            if ((c - sh * per_shot) / nrec >= shot_steps[sh]) r = T(0);
+        }
         tr[c] = r;
         acc += (double)r * (double)r;
     }
@@ -231,6 +238,8 @@ struct pysit_plan {
     virtual int status(int* flags, cudaStream_t s) = 0;
     virtual int step_loop(int mode, int nsteps, cudaStream_t s) = 0;
     virtual int autotune(const int* cand, int ncand, int nsteps, int* chosen, double* ms, cudaStream_t s) = 0;
+    // enqueue misfit + gradient on s without graph handling (for a group's capture)
+    virtual int enqueue_grad_raw(const void* dobs, double* grad, double* rnorm2, cudaStream_t s) = 0;
     int64_t last_launches = 0;
 };
 
@@ -242,6 +251,7 @@ struct PlanT final : public pysit_plan {
     // ---- description -------------------------------------------------------
     int dim, order, R, nx, ny, nz, nsteps, p_img, S, G, nshots, nsrc, nrec, use_graph, psi_consistent;
     int tile_req = 0;            // requested task length along x (0: default)
+    std::vector<int> shot_steps; // record length of each shot in steps (empty: all nsteps)
     size_t task_cap = 0;         // ints the task buffer holds (enough for the shortest x-chunk)
     double dx, dy, dz, dt;
     int pad_lo[3], pad_hi[3];
@@ -279,7 +289,7 @@ struct PlanT final : public pysit_plan {
         size_t sbox, srpb, srow, spt, sw;          // source injection
         size_t rbox, rrpb, rrow, rpt, rw;          // receiver injection
         size_t recrow, recoff, recw;               // recording
-        size_t gpad, partial, rnorm, err, tasks, ctr;
+        size_t gpad, partial, rnorm, err, tasks, ctr, shsteps;
     } off{};
     size_t field_bytes = 0;      // one field for G shots
     int ckpt_fields = 0;         // fields per checkpoint
@@ -329,6 +339,15 @@ struct PlanT final : public pysit_plan {
         use_graph = d.use_graph;
         psi_consistent = d.psi_consistent ? 1 : 0;
         tile_req = d.tile_x > 0 ? d.tile_x : 0;
+        shot_steps.clear();
+        if (d.shot_nsteps) {
+            for (int s2 = 0; s2 < d.nshots; ++s2) {
+                PGB_REQUIRE(d.shot_nsteps[s2] >= 1 && d.shot_nsteps[s2] <= d.nsteps,
+                            "record length of shot %d (%d steps) outside [1, nsteps = %d]", s2, d.shot_nsteps[s2],
+                            d.nsteps);
+                shot_steps.push_back(d.shot_nsteps[s2]);
+            }
+        }
         for (int a = 0; a < 3; ++a) { pad_lo[a] = d.pad_lo[a]; pad_hi[a] = d.pad_hi[a]; }
         const int na[3] = {nx, ny, nz};
         for (int a = 0; a < 3; ++a) {
@@ -638,6 +657,7 @@ struct PlanT final : public pysit_plan {
         off.gpad = take((size_t)nx * ny * nz * sizeof(double));
         off.err = take(sizeof(int));
         off.ctr = take(2 * sizeof(unsigned long long));
+        off.shsteps = take(std::max<size_t>(shot_steps.size(), 1) * sizeof(int));
         task_cap = std::max<size_t>(task_ints(kMinTileX), std::max(tasks2d.size(), tasks3d.size()));
         off.tasks = take(std::max<size_t>(task_cap, 1) * sizeof(int));
         off.partial = take(kRedBlocks * sizeof(double));
@@ -702,6 +722,7 @@ struct PlanT final : public pysit_plan {
         if ((rc = upload(off.recrow, rec_rows, s)) || (rc = upload(off.recoff, rec_off, s))) return rc;
         if ((rc = upload(off.recw, tmp = toT(rec_ws), s))) return rc;
         if ((rc = upload(off.tasks, dim == 3 ? tasks3d : tasks2d, s))) return rc;
+        if ((rc = upload(off.shsteps, shot_steps, s))) return rc;
         PGB_CHECK_CUDA(cudaStreamSynchronize(s));
         if (!cap) PGB_CHECK_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
         if (dim == 2) {
@@ -1146,7 +1167,8 @@ struct PlanT final : public pysit_plan {
             if (n > 0) {
                 residual_kernel<T><<<kRedBlocks, kRedThreads, 0, s>>>(
                     static_cast<const T*>(dobs) + (size_t)g0 * nsteps * nrec, at<T>(off.traces), n,
-                    at<double>(off.partial), migrate ? 1 : 0);
+                    at<double>(off.partial), migrate ? 1 : 0, shot_steps.empty() ? nullptr : at<int>(off.shsteps) + g0,
+                    nsteps, nrec);
                 sum_partials_kernel<<<1, kRedThreads, 0, s>>>(at<double>(off.partial), kRedBlocks,
                                                               at<double>(off.rnorm), 1);
                 launches += 2;
@@ -1221,6 +1243,16 @@ struct PlanT final : public pysit_plan {
         return run(migrate ? 3 : with_grad ? 1 : 2, dobs, grad, rnorm2, traces, s, [&](cudaStream_t st) {
             enqueue_gradient(dobs, grad, rnorm2, traces, with_grad, migrate, st);
         });
+    }
+
+    int enqueue_grad_raw(const void* dobs, double* grad, double* rnorm2, cudaStream_t s) override {
+        PGB_REQUIRE(ws, "no workspace bound");
+        PGB_REQUIRE(model_set, "pysit_plan_set_model must be called first");
+        PGB_REQUIRE((dobs || nrec == 0) && grad && rnorm2, "NULL argument");
+        launches = 0;
+        enqueue_gradient(dobs, grad, rnorm2, nullptr, true, false, s);
+        last_launches = launches;
+        return PYSIT_OK;
     }
 };
 
@@ -1330,4 +1362,80 @@ extern "C" int pysit_plan_autotune(pysit_plan* p, const int* candidates, int nca
                                    double* ms, void* stream) {
     PGB_REQUIRE(p, "NULL plan");
     return p->autotune(candidates, ncand, nsteps, chosen, ms, (cudaStream_t)stream);
+}
+
+// ---- plan groups ------------------------------------------------------------------------
+struct pysit_group {
+    std::vector<pysit_plan*> plans;
+    std::vector<cudaStream_t> streams;  // one per plan
+    std::vector<cudaEvent_t> done;      // one per plan
+    cudaStream_t cap = nullptr;
+    cudaEvent_t root = nullptr;
+    std::map<std::vector<const void*>, cudaGraphExec_t> graphs;
+    ~pysit_group() {
+        for (auto& kv : graphs)
+            if (kv.second) cudaGraphExecDestroy(kv.second);
+        for (auto s : streams) cudaStreamDestroy(s);
+        for (auto e : done) cudaEventDestroy(e);
+        if (cap) cudaStreamDestroy(cap);
+        if (root) cudaEventDestroy(root);
+    }
+};
+
+extern "C" int pysit_group_create(pysit_plan* const* plans, int nplans, pysit_group** out) {
+    PGB_REQUIRE(plans && out && nplans >= 1, "need at least one plan and an output");
+    for (int i = 0; i < nplans; ++i) PGB_REQUIRE(plans[i], "NULL plan %d", i);
+    std::unique_ptr<pysit_group> g(new pysit_group());
+    g->plans.assign(plans, plans + nplans);
+    PGB_CHECK_CUDA(cudaStreamCreateWithFlags(&g->cap, cudaStreamNonBlocking));
+    PGB_CHECK_CUDA(cudaEventCreateWithFlags(&g->root, cudaEventDisableTiming));
+    for (int i = 0; i < nplans; ++i) {
+        cudaStream_t s;
+        cudaEvent_t e;
+        PGB_CHECK_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+        g->streams.push_back(s);
+        PGB_CHECK_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        g->done.push_back(e);
+    }
+    *out = g.release();
+    return PYSIT_OK;
+}
+
+extern "C" int pysit_group_destroy(pysit_group* g) {
+    delete g;
+    return PYSIT_OK;
+}
+
+extern "C" int pysit_group_gradient(pysit_group* g, const void* const* dobs, double* const* grad,
+                                    double* const* rnorm2, void* stream) {
+    PGB_REQUIRE(g && dobs && grad && rnorm2, "NULL argument");
+    const int n = (int)g->plans.size();
+    std::vector<const void*> key;
+    for (int i = 0; i < n; ++i) { key.push_back(dobs[i]); key.push_back(grad[i]); key.push_back(rnorm2[i]); }
+    auto it = g->graphs.find(key);
+    if (it == g->graphs.end()) {
+        PGB_CHECK_CUDA(cudaStreamBeginCapture(g->cap, cudaStreamCaptureModeThreadLocal));
+        cudaEventRecord(g->root, g->cap);
+        int rc = PYSIT_OK;
+        for (int i = 0; i < n && rc == PYSIT_OK; ++i) {
+            cudaStreamWaitEvent(g->streams[i], g->root, 0);
+            rc = g->plans[i]->enqueue_grad_raw(dobs[i], grad[i], rnorm2[i], g->streams[i]);
+            cudaEventRecord(g->done[i], g->streams[i]);
+            cudaStreamWaitEvent(g->cap, g->done[i], 0);
+        }
+        cudaGraph_t graph = nullptr;
+        cudaError_t e = cudaStreamEndCapture(g->cap, &graph);
+        if (rc) {
+            if (graph) cudaGraphDestroy(graph);
+            return rc;
+        }
+        if (e != cudaSuccess) return cuda_status(e, "cudaStreamEndCapture (group)");
+        cudaGraphExec_t exec = nullptr;
+        e = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) return cuda_status(e, "cudaGraphInstantiate (group)");
+        it = g->graphs.emplace(key, exec).first;
+    }
+    PGB_CHECK_CUDA(cudaGraphLaunch(it->second, (cudaStream_t)stream));
+    return PYSIT_OK;
 }

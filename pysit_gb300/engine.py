@@ -19,7 +19,7 @@ import numpy as np
 from . import _native
 from .solvers.cda_time import axis_sigma_map
 
-__all__ = ["WavePlan", "padded_cells", "default_checkpoint_every"]
+__all__ = ["WavePlan", "PlanGroup", "padded_cells", "default_checkpoint_every"]
 
 _DESC_AXIS = {1: [2], 2: [0, 2], 3: [0, 1, 2]}  # mesh axis -> (x, y, z) slot of the descriptor
 
@@ -51,7 +51,10 @@ class WavePlan:
     """Device plan of one (solver configuration, shot list)."""
 
     def __init__(self, solver, shots, imaging_period=1, checkpoint_every=None, shots_per_launch=None,
-                 use_graph=None):
+                 use_graph=None, record_steps=None):
+        """``record_steps``: optional record length of each shot in time steps (<= solver.nsteps);
+        a shorter shot's residual is zero from its length on, so its misfit and gradient are those
+        of a run of that length (the shots of one plan still step together)."""
         torch = _native.require_cuda()
         lib = _native.load()
         self.solver = solver
@@ -108,6 +111,14 @@ class WavePlan:
                           self.shots_per_launch, d.psi_consistent)
         d.tile_x = _TUNED.get(self._tune_key, 0)
         self.tile_x = d.tile_x
+        self.record_steps = None
+        if record_steps is not None:
+            rs = np.ascontiguousarray(np.asarray(record_steps, dtype=np.int32).reshape(-1))
+            if rs.size != self.nshots:
+                raise ValueError("record_steps needs one entry per shot")
+            keep.append(rs)
+            d.shot_nsteps = rs.ctypes.data_as(C.POINTER(C.c_int32))
+            self.record_steps = rs.copy()
 
         ts = np.arange(self.nsteps) * self.dt
         # sources
@@ -273,6 +284,39 @@ class WavePlan:
             self._h, C.c_void_p(self.dobs.data_ptr()), C.c_void_p(self.rnorm2.data_ptr()),
             C.c_void_p(self.traces.data_ptr() if with_traces else None), C.c_void_p(_native.stream_handle())))
         return self.rnorm2
+
+
+class PlanGroup:
+    """Plans (e.g. of different grids) whose gradients run concurrently in one CUDA graph:
+    each plan on a stream of its own, forked from the current stream and joined back."""
+
+    def __init__(self, plans):
+        self.plans = list(plans)
+        arr = (C.c_void_p * len(self.plans))(*[p._h.value for p in self.plans])
+        h = C.c_void_p()
+        _native.check(_native.load().pysit_group_create(arr, len(self.plans), C.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                _native.load().pysit_group_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def gradient(self):
+        """Misfit and gradient of every plan on its loaded observed data: [(grad, rnorm2), ...]."""
+        for p in self.plans:
+            p.set_model()
+        n = len(self.plans)
+        dobs = (C.c_void_p * n)(*[p.dobs.data_ptr() for p in self.plans])
+        grad = (C.c_void_p * n)(*[p.grad.data_ptr() for p in self.plans])
+        rn = (C.c_void_p * n)(*[p.rnorm2.data_ptr() for p in self.plans])
+        _native.check(_native.load().pysit_group_gradient(self._h, dobs, grad, rn,
+                                                          C.c_void_p(_native.stream_handle())))
+        return [(p.grad, p.rnorm2) for p in self.plans]
 
 
 def plan_for(solver, shots, imaging_period=1, **kw):

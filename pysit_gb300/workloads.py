@@ -9,13 +9,19 @@ No public dataset is involved: each model is generated from a named seed.
   cfg3  3D FWI gradient: 400 x 400 x 300 cells at 15 m + 20-cell PML, order 8,
         layered + smoothed perturbation + Gaussian salt body at 4500 m/s,
         8 shots, 100 x 100 receivers, 6 Hz, 3000 steps.
+  cfg4  uneven batch: 256 shots over three 2D grids of one model (288 x 96 at
+        50 m / 2000 steps / 3 Hz, 576 x 192 at 25 m / 3000 / 5 Hz, 1152 x 384 at
+        12.5 m / 4000 / 8 Hz; 500 m of PML each), order 6, FP32, seeded random
+        source positions and record lengths; the three gradients run as one
+        plan group (one CUDA graph).
   cfg5  end-to-end FWI: PySIT's LBFGS (memory 10, backtracking) for 20 iterations
         on the cfg2 model with 128 shots, from the sigma = 30 smoothed model.
 ``scale`` shrinks a workload uniformly (cells per axis, shots, steps) for tests.
 
 ``python -m pysit_gb300.workloads cfg5 [--iterations N] [--shots N] [--scale s]
 [--nsteps N] [--plain]`` runs the FWI and prints one JSON line (objective history,
-relative L2 error of the final model, wall time).
+relative L2 error of the final model, wall time); ``... cfg4`` times the uneven
+batch, grid by grid and as one group.
 """
 from __future__ import annotations
 
@@ -26,7 +32,7 @@ from scipy.ndimage import gaussian_filter
 
 from . import core, solvers
 
-__all__ = ["layered_model", "cfg2", "cfg3", "cfg5", "run_lbfgs"]
+__all__ = ["layered_model", "cfg2", "cfg3", "cfg4", "cfg5", "run_lbfgs", "run_uneven_batch"]
 
 
 def layered_model(shape, nlayers, vmin, vmax, sigma_cells, amp, seed, clip=(1500.0, 5500.0)):
@@ -142,21 +148,116 @@ def run_lbfgs(m, shots, solver, C, C0, iterations=20, memory_length=10, batched=
             "seconds": seconds, "iterations": iterations, "shots": len(shots), "nsteps": solver.nsteps}
 
 
+def cfg4(scale=1.0, nshots=256, order=6, precision="single", seed=2028, cfl=0.4):
+    """The uneven batch: a list of three grids, each (mesh, shots, solver, C, C0, record_steps).
+
+    One model (the cfg2 model at 12.5 m) sampled every 4th / 2nd / 1st cell; shots split as
+    evenly as possible, source x seeded-random at the surface, all grid columns as
+    receivers, record lengths seeded-random in [nsteps/2, nsteps]."""
+    rng = np.random.default_rng(seed)
+    nx_f, nz_f = max(32, int(round(1152 * scale))) // 4 * 4, max(16, int(round(384 * scale))) // 4 * 4
+    C_f = layered_model((nx_f, nz_f), 12, 1500.0, 4500.0, 8 * max(scale, 0.125), 0.10, 2026)
+    grids = [(4, 50.0, 2000, 3.0), (2, 25.0, 3000, 5.0), (1, 12.5, 4000, 8.0)]
+    counts = [nshots // 3 + (1 if i < nshots % 3 else 0) for i in range(3)]
+    out = []
+    for (step, dx, nsteps, freq), ns in zip(grids, counts):
+        nsteps = max(16, int(round(nsteps * min(1.0, scale))))
+        C = np.ascontiguousarray(C_f[::step, ::step])
+        nx, nz = C.shape
+        npml = max(4, int(round(500.0 / dx * min(1.0, max(scale, 0.25)))))
+        amp = 3 * 4500.0 * math.log(1e3) / (2 * npml * dx)
+        pml = core.PML(npml * dx, amp)
+        d = core.RectangularDomain((0.0, (nx - 1) * dx, pml, pml), (0.0, (nz - 1) * dx, pml, pml))
+        m = core.CartesianMesh(d, nx, nz)
+        C0 = gaussian_filter(C, sigma=30.0 / step * max(scale, 0.05), mode="nearest")
+        T = _steps_T(C0, m.deltas, cfl, nsteps)
+        w = core.RickerWavelet(freq)
+        xs = rng.uniform(0.05, 0.95, size=ns) * (nx - 1) * dx
+        rec_x = np.arange(nx) * dx
+        shots = []
+        for x in xs:
+            src = core.PointSource(m, (float(x), 0.0), w)
+            rec = core.ReceiverSet(m, [core.PointReceiver(m, (float(r), 0.0)) for r in rec_x])
+            shots.append(core.Shot(src, rec))
+        solver = solvers.ConstantDensityAcousticWave(m, spatial_accuracy_order=order, trange=(0.0, T),
+                                                     kernel_implementation="cuda", precision=precision,
+                                                     cfl_safety=cfl, checkpoint_every=64, autotune=True)
+        record = rng.integers(nsteps // 2, nsteps + 1, size=ns)
+        out.append((m, shots, solver, C.reshape(-1, 1), C0.reshape(-1, 1), record))
+    return out
+
+
+def run_uneven_batch(grids, repeats=2):
+    """Observed data on the true models, then the gradients of all grids at the start models:
+    timed grid after grid (one plan call each) and as one plan group.  Returns shots/s of both."""
+    import time
+
+    import torch
+
+    from .engine import PlanGroup, WavePlan
+
+    plans = []
+    for m, shots, solver, C, C0, record in grids:
+        solver.model_parameters = solver.ModelParameters(m, {"C": C})
+        obs_plan = WavePlan(solver, shots)
+        obs = obs_plan.forward().clone()
+        ts_true = solver.ts()
+        del obs_plan
+        solver.model_parameters = solver.ModelParameters(m, {"C": C0})
+        # record lengths are counted on the start model's time axis
+        rec = np.minimum(record, solver.nsteps)
+        p = WavePlan(solver, shots, record_steps=rec)
+        p.autotune()
+        from .autograd import resample_linear
+        p.dobs.copy_(resample_linear(obs, ts_true, solver.ts()))
+        del obs
+        torch.cuda.empty_cache()
+        plans.append(p)
+    nshots = sum(len(g[1]) for g in grids)
+    group = PlanGroup(plans)
+    for p in plans:
+        p.gradient()
+    group.gradient()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(repeats):
+        for p in plans:
+            p.gradient()
+    torch.cuda.synchronize()
+    t_seq = (time.perf_counter() - t0) / repeats
+    t0 = time.perf_counter()
+    for _ in range(repeats):
+        group.gradient()
+    torch.cuda.synchronize()
+    t_grp = (time.perf_counter() - t0) / repeats
+    status = [p.status() for p in plans]
+    return {"shots": nshots, "grids": [[int(s) for s in g[0].shape(as_grid=True)] for g in grids],
+            "shots_per_grid": [len(g[1]) for g in grids], "nsteps": [int(p.nsteps) for p in plans],
+            "tile_x": [int(p.tile_x) for p in plans],
+            "sequential_s": t_seq, "group_s": t_grp, "shots_per_s_sequential": nshots / t_seq,
+            "shots_per_s_group": nshots / t_grp, "group_speedup": t_seq / t_grp, "status": status}
+
+
 def _main(argv=None):
     import argparse
     import json
 
     ap = argparse.ArgumentParser(prog="python -m pysit_gb300.workloads")
-    ap.add_argument("workload", choices=["cfg5"])
+    ap.add_argument("workload", choices=["cfg4", "cfg5"])
     ap.add_argument("--iterations", type=int, default=20)
-    ap.add_argument("--shots", type=int, default=128)
+    ap.add_argument("--shots", type=int, default=None, help="default 256 (cfg4), 128 (cfg5)")
     ap.add_argument("--nsteps", type=int, default=4000)
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--plain", action="store_true", help="per-shot FP64 objective instead of the batched FP32 one")
     ap.add_argument("--verbose", action="store_true")
     a = ap.parse_args(argv)
+    if a.workload == "cfg4":
+        out = run_uneven_batch(cfg4(scale=a.scale, nshots=a.shots or 256))
+        out.update(workload="cfg4", scale=a.scale)
+        print(json.dumps(out))
+        return
     prec = "double" if a.plain else "single"
-    m, shots, solver, C, C0 = cfg5(scale=a.scale, nshots=a.shots, nsteps=a.nsteps, precision=prec)
+    m, shots, solver, C, C0 = cfg5(scale=a.scale, nshots=a.shots or 128, nsteps=a.nsteps, precision=prec)
     out = run_lbfgs(m, shots, solver, C, C0, iterations=a.iterations, batched=not a.plain, verbose=a.verbose)
     out.update(workload=a.workload, path="plain FP64" if a.plain else "batched FP32", scale=a.scale)
     print(json.dumps(out))
