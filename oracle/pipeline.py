@@ -19,6 +19,8 @@ Restated reference functions (paths inside the pysit project):
     adjoint  TemporalModeling.adjoint_model      modeling/temporal_modeling.py:228-387
     fold     ModelPerturbationBase.add_padding   solvers/model_parameter.py:537-594
     gradient TemporalLeastSquares.compute_gradient objective_functions/temporal_least_squares.py:141-198
+    born     TemporalModeling.linear_forward_model modeling/temporal_modeling.py:389-546
+    hessian  TemporalLeastSquares.apply_hessian   objective_functions/temporal_least_squares.py:200-249
 """
 from __future__ import annotations
 
@@ -156,25 +158,104 @@ def forward(P, want_dwaveop=False, imaging_period=1, kind="oracle", dtype=np.flo
     return sim, dws
 
 
-def adjoint_image(P, resid, dws, imaging_period=1, kind="oracle", dtype=np.float64):
-    """Padded imaging condition -dt*p*sum_k q_k dWaveOp[k//p] of one shot."""
+def adjoint_image(P, resid, dws, imaging_period=1, kind="oracle", dtype=np.float64, extra_rhs=None,
+                  want_dwaveop=False):
+    """Padded imaging condition -dt*p*sum_k q_k dWaveOp[k//p] of one shot.
+
+    extra_rhs[k] (padded) is added to the adjoint source of step k (the Hessian's
+    operand_model * operand_dWaveOpAdj[k], _setup_adjoint_rhs :216-226); with
+    want_dwaveop the dWaveOp of the adjoint field after each step is returned too,
+    in forward time order (adjoint_model's 'dWaveOpAdj', :342-345 and :383-385)."""
     dim, n = P["dim"], int(np.prod(P["shape"]))
     qm = np.zeros(n, dtype)
     qc = np.zeros(n, dtype)
     aux = {a: np.zeros(n, dtype) for a in AUX[dim]}
     rcells, rrecs, rws, rwi, nrec = P["rec"]
     ic = np.zeros(n)
+    dwa = []
     for k in range(P["nsteps"] - 1, -1, -1):
         if k % imaging_period == 0:
             ic += qc * dws[k // imaging_period]
         rhs = np.zeros(n)
         np.add.at(rhs, rcells, rwi * resid[k, rrecs])
+        if extra_rhs is not None:
+            rhs += extra_rhs[k]
         qp, aux_n = step(kind, dim, P["order"], qm, aux, qc, P["C"], rhs, P["profiles"], P["dt"], P["deltas"],
                          P["shape"])
+        if want_dwaveop and k % imaging_period == 0:
+            dwa.append(dwaveop(P, qm.astype(float), qc.astype(float), qp.astype(float),
+                               aux["psi"].astype(float) if dim == 3 else None))
         if k == 0:
             break
         qm, qc, aux = qc, qp, aux_n
-    return ic * (-1 * P["dt"]) * imaging_period
+    ic = ic * (-1 * P["dt"]) * imaging_period
+    if want_dwaveop:
+        return ic, dwa[::-1]
+    return ic
+
+
+def pad(P, m, mode=None):
+    """Unpadded grid array -> padded grid: zeros (CartesianMesh.pad_array default, mesh.py:446-533)
+    or numpy.pad's `mode` ('edge' for linear_forward_model's m1, temporal_modeling.py:434)."""
+    pads = [tuple(p) for p in P["pads"]]
+    inner = [s - lo - hi for s, (lo, hi) in zip(P["shape"], pads)]
+    a = np.asarray(m, float).reshape(inner)
+    return np.pad(a, pads, mode=mode or "constant").reshape(-1)
+
+
+def born(P, m1, kind="oracle", dtype=np.float64, want_dwaveop1=False):
+    """linear_forward_model (temporal_modeling.py:389-546) of one shot about the model of P:
+    u1 driven by rhs_k = -m1_edge_padded * dWaveOp0_k, traces of u1_k recorded before step k.
+    Returns (traces [nsteps, nrec], dWaveOp0 list[, dWaveOp1 list])."""
+    dim, n = P["dim"], int(np.prod(P["shape"]))
+    _, dws = forward(P, True, 1, kind, dtype)
+    m1p = pad(P, m1, "edge")
+    um = np.zeros(n, dtype)
+    uc = np.zeros(n, dtype)
+    aux = {a: np.zeros(n, dtype) for a in AUX[dim]}
+    rcells, rrecs, rws, rwi, nrec = P["rec"]
+    sim = np.zeros((P["nsteps"], nrec))
+    dw1 = []
+    for k in range(P["nsteps"]):
+        np.add.at(sim[k], rrecs, rws * uc[rcells])
+        rhs = m1p * (-1 * dws[k])
+        up, aux_n = step(kind, dim, P["order"], um, aux, uc, P["C"], rhs, P["profiles"], P["dt"], P["deltas"],
+                         P["shape"])
+        if want_dwaveop1:
+            dw1.append(dwaveop(P, um.astype(float), uc.astype(float), up.astype(float),
+                               aux["psi"].astype(float) if dim == 3 else None))
+        if k == P["nsteps"] - 1:
+            break
+        um, uc, aux = uc, up, aux_n
+    if want_dwaveop1:
+        return sim, dws, dw1
+    return sim, dws
+
+
+def hessian(Ps, m1, hessian_mode="approximate", levenberg_mu=0.0, dobs=None, kind="oracle"):
+    """apply_hessian (temporal_least_squares.py:200-249) summed over shots, unpadded m-space.
+
+    approximate / levenberg: sum_s F_s* F_s m1 (+ mu m1); full: adds the second-order terms
+    driven by the residual r0 = dobs - F(m0) (needs dobs).  Every migration images at every
+    step (imaging_period 1, the step of the dWaveOp0 lists)."""
+    if hessian_mode not in ("approximate", "full", "levenberg"):
+        raise ValueError(hessian_mode)
+    out = np.zeros(np.asarray(m1).size)
+    for i, P in enumerate(Ps):
+        if hessian_mode in ("approximate", "levenberg"):
+            d1, dws = born(P, m1, kind)
+            out += fold(P, adjoint_image(P, d1, dws, 1, kind))
+        else:
+            sim0, _ = forward(P, False, 1, kind)
+            r0 = dobs[i] - sim0
+            d1, dws, dw1 = born(P, m1, kind, want_dwaveop1=True)
+            ic1, dwa1 = adjoint_image(P, r0, dw1, 1, kind, want_dwaveop=True)
+            m1z = pad(P, m1)
+            ic2 = adjoint_image(P, d1, dws, 1, kind, extra_rhs=[m1z * d for d in dwa1])
+            out += fold(P, ic1) + fold(P, ic2)
+    if hessian_mode == "levenberg":
+        out = out + levenberg_mu * np.asarray(m1, float).reshape(-1)
+    return out
 
 
 def fold(P, padded):

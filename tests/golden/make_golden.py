@@ -5,6 +5,7 @@ Run in a container that has the reference tree (default /root/reference) after
 
     python tests/golden/make_golden.py            # all problems of tests/problems.py
     python tests/golden/make_golden.py lbfgs:o2   # the reference's LBFGS run on problem o2
+    python tests/golden/make_golden.py born:o2    # Born modelling and Hessian applications on o2
 
 For every problem it stores (compressed .npz): the traces of every shot
 modelled on the true model by the reference's own ``generate_seismic_data``
@@ -109,10 +110,55 @@ def run_lbfgs(name):
           f"evaluate {calls['evaluate']} gradient {calls['gradient']}")
 
 
+BORN_SEED = 11
+LEVENBERG_MU = 1e5
+
+
+def born_perturbation(C0, seed=BORN_SEED):
+    """The model perturbation of the Born / Hessian fixtures: 1 % of m0 = C0**-2, seeded noise."""
+    rng = np.random.default_rng(seed)
+    c0 = np.asarray(C0, float).reshape(-1)
+    return 0.01 * rng.standard_normal(c0.size) / c0 ** 2
+
+
+def run_born(name):
+    """The reference's linear forward model (simdata of every shot, dWaveOp0 computed on the
+    fly) and its Hessian applications (approximate, levenberg with LEVENBERG_MU, full) at the
+    starting model, for the perturbation born_perturbation(C0).
+
+    apply_hessian calls migrate_shot without its positional imaging_period
+    (temporal_least_squares.py:217 against temporal_modeling.py:171), a TypeError; the
+    migrate_shot used here supplies imaging_period = 1, the period of the dWaveOp0 lists."""
+    pysit = pysit_live.import_pysit()
+    m, shots, solver, C, C0 = problems.build(pysit, name, kernel="cpp")
+    pysit.generate_seismic_data(shots, solver, solver.ModelParameters(m, {"C": C}))
+    m0 = solver.ModelParameters(m, {"C": C0})
+    m1v = born_perturbation(C0)
+    m1 = m0.perturbation(data=m1v.reshape(-1, 1))
+    obj = pysit.TemporalLeastSquares(solver)
+    tm = obj.modeling_tools
+    d1 = np.stack([tm.linear_forward_model(s, m0, m1, ["simdata"])["simdata"] for s in shots])
+    mig = tm.migrate_shot
+
+    def migrate_shot(shot, m0_, operand_simdata, imaging_period=1, *a, **k):
+        return mig(shot, m0_, operand_simdata, imaging_period, *a, **k)
+
+    tm.migrate_shot = migrate_shot
+    out = dict(m1=m1v, d1=d1, dt0=solver.dt, nsteps0=solver.nsteps, levenberg_mu=LEVENBERG_MU)
+    for mode in ("approximate", "levenberg", "full"):
+        h = obj.apply_hessian(shots, m0, m1, hessian_mode=mode, levenberg_mu=LEVENBERG_MU)
+        out[f"hess_{mode}"] = np.asarray(h.data).reshape(-1)
+    np.savez_compressed(os.path.join(HERE, f"born_{name}.npz"), **out)
+    print(f"born_{name}: |d1|={np.linalg.norm(d1):.6e} |H m1|={np.linalg.norm(out['hess_approximate']):.6e} "
+          f"|H_full m1|={np.linalg.norm(out['hess_full']):.6e}")
+
+
 if __name__ == "__main__":
     names = sys.argv[1:] or list(problems.SPECS)
     for n in names:
         if n.startswith("lbfgs:"):
             run_lbfgs(n.split(":", 1)[1])
+        elif n.startswith("born:"):
+            run_born(n.split(":", 1)[1])
         else:
             run(n)
