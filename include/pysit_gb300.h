@@ -187,6 +187,23 @@ int pysit_plan_migrate(pysit_plan* plan, const void* operand_dev, double* image_
 /* Misfit only (TemporalLeastSquares.evaluate without the 0.5*dt factor). */
 int pysit_plan_misfit(pysit_plan* plan, const void* dobs_dev, double* rnorm2_dev,
                       void* traces_dev, void* stream);
+/* Linearised (Born) modelling of every shot about the plan's model:
+ * TemporalModeling.linear_forward_model(shot, m0, m1, ['simdata'])
+ * (pysit/modeling/temporal_modeling.py:389-546).  m1_dev: model perturbation
+ * (m = C^-2 space, FP64, device) on the unpadded grid in PySIT's flat order; it is
+ * edge-padded on the device as the reference does (:434).  traces_dev: device
+ * [nshots][nsteps][nrec] of the plan's dtype, u1 sampled before each step. */
+int pysit_plan_born(pysit_plan* plan, const double* m1_dev, void* traces_dev, void* stream);
+/* Gauss-Newton Hessian application summed over the shots:
+ * TemporalLeastSquares.apply_hessian(shots, m0, m1, 'approximate')
+ * (pysit/objective_functions/temporal_least_squares.py:200-249), i.e. the sum over
+ * shots of migrate_shot(F_s m1) imaging every step: out_dev (FP64, unpadded) =
+ * sum_s -dt sum_k q_k dWaveOp0_k with the strips folded, q driven by the Born
+ * traces d1.  d1norm2_dev [1] (may be NULL) = ||d1||^2.  'levenberg' adds mu*m1,
+ * which the caller does.  Each shot group runs one Born sweep (saving the background
+ * checkpoints) and one checkpointed migration. */
+int pysit_plan_hessian(pysit_plan* plan, const double* m1_dev, double* out_dev, double* d1norm2_dev,
+                       void* stream);
 /* Reads and clears the plan's device status word (synchronises `stream`):
  * bit 0 (1) = a bounded wait for a bulk copy expired (results invalid),
  * bit 1 (2) = a non-finite wavefield value appeared (unstable time step). */

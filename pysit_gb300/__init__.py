@@ -5,7 +5,7 @@ acoustic solver with PML and its adjoint-state FWI gradient.
 this path (RectangularDomain, PML, CartesianMesh, PointSource, ReceiverSet,
 RickerWavelet, equispaced_acquisition, ConstantDensityAcousticWave,
 generate_seismic_data, TemporalModeling, TemporalLeastSquares, LBFGS,
-GradientDescent), with
+GradientDescent, GaussNewton), with
 ``kernel_implementation='cuda'``.  ``pysit_gb300.plugin.register()`` adds the
 same solvers to an installed PySIT's own factory instead.
 """
@@ -15,6 +15,6 @@ from .solvers import (ConstantDensityAcousticWave, ConstantDensityAcousticParame
                       ConstantDensityAcousticTimeScalar_3D_cuda, NoMatchError, MultipleMatchError)
 from .modeling import TemporalModeling, generate_seismic_data, generate_shot_data_time  # noqa: F401
 from .objective_functions import TemporalLeastSquares  # noqa: F401
-from .optimization import LBFGS, GradientDescent  # noqa: F401
+from .optimization import LBFGS, GradientDescent, GaussNewton  # noqa: F401
 
 __version__ = "0.1.0"

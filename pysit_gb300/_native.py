@@ -79,6 +79,8 @@ _PROTOS = {
     "pysit_plan_gradient": (_i, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "pysit_plan_misfit": (_i, [_vp, _vp, _vp, _vp, _vp]),
     "pysit_plan_migrate": (_i, [_vp, _vp, _vp, _vp, _vp]),
+    "pysit_plan_born": (_i, [_vp, _vp, _vp, _vp]),
+    "pysit_plan_hessian": (_i, [_vp, _vp, _vp, _vp, _vp]),
     "pysit_plan_status": (_i, [_vp, C.POINTER(_i), _vp]),
     "pysit_misfit_per_shot_noalloc": (_i, [_i, _vp, _vp, _i, C.c_int64, _vp, _vp, _vp]),
     "pysit_plan_last_launch_count": (_i, [_vp, C.POINTER(C.c_int64)]),

@@ -109,6 +109,53 @@ __global__ void inject_scatter3d_kernel(const WaveParams<T> p, int cells_max) {
     }
 }
 
+// Born source of one step added after the stencil kernels of the scattered field u1:
+//     u1_{k+1} += fac C^2 rhs1,   rhs1 = -m1 dWaveOp0_k
+// (TemporalModeling.linear_forward_model, pysit/modeling/temporal_modeling.py:520-525; the
+// step is linear in rhs, fac as in inject_scatter2d/3d_kernel).  One block per row
+// (shot, x, y) of the padded grid, threads along z; cells of the outer ring are skipped as
+// the reference's step skips them.  m1 and C^2 are shared by the shots; dw holds dWaveOp0_k
+// of every shot of the launch.
+template <typename T>
+__global__ void __launch_bounds__(128) born_source_kernel(const WaveParams<T> p, int dim, const T* __restrict__ m1,
+                                                          const T* __restrict__ dw) {
+    const long long rows = (long long)p.nshot * p.nx * p.ny;
+    for (long long r = blockIdx.x; r < rows; r += gridDim.x) {
+        const int shot = (int)(r / ((long long)p.nx * p.ny));
+        const int xy = (int)(r - (long long)shot * p.nx * p.ny);
+        const int x = xy / p.ny, y = xy - x * p.ny;
+        if (dim >= 2 && (x == 0 || x == p.nx - 1)) continue;
+        if (dim == 3 && (y == 0 || y == p.ny - 1)) continue;
+        const T sxy = p.sgx[x] + p.sgy[y];
+        const long long row = ((long long)(x + p.hx) * p.rows_y + (y + p.hy)) * p.ldz + kOZ;
+        const long long sh = (long long)shot * p.fstride;
+        for (int z = 1 + threadIdx.x; z < p.nz - 1; z += blockDim.x) {
+            const T s = sxy + p.sgz[z];
+            const bool pml = p.sgx[x] != T(0) || p.sgy[y] != T(0) || p.sgz[z] != T(0);
+            const T fac = pml ? T(2) * p.dt2 / (T(2) + p.dt * s) : p.dt2;
+            const long long o = row + z;
+            p.u_prev[sh + o] -= fac * __ldg(p.c2 + o) * (__ldg(m1 + o) * __ldcs(dw + sh + o));
+        }
+    }
+}
+
+// m1 of the unpadded grid (FP64, PySIT's flat order) -> the padded internal layout with
+// numpy.pad(mode='edge') semantics: every padding cell takes the value of the nearest
+// physical cell (m1.with_padding(padding_mode='edge'), temporal_modeling.py:434).
+template <typename T>
+__global__ void edge_pad_kernel(const double* __restrict__ m, int nx, int ny, int nz, int lx, int ly, int lz,
+                                int px, int py, int pz, int hx, int hy, int rows_y, int ldz, T* __restrict__ out) {
+    const long long n = (long long)nx * ny * nz;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
+         c += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(c % nz);
+        const long long r = c / nz;
+        const int j = (int)(r % ny), i = (int)(r / ny);
+        const int ii = min(max(i - lx, 0), px - 1), jj = min(max(j - ly, 0), py - 1), kk = min(max(k - lz, 0), pz - 1);
+        out[ioff(i, j, k, hx, hy, rows_y, ldz)] = T(m[((long long)ii * py + jj) * pz + kk]);
+    }
+}
+
 // trace recorder as a kernel of its own (runs beside the stencil kernels: it only reads u_k)
 template <typename T>
 __global__ void record_kernel(const WaveParams<T> p) {
@@ -119,7 +166,8 @@ constexpr int kRedBlocks = 1024;
 constexpr int kRedThreads = 256;
 
 // resid = dobs - dsim (in place over the trace buffer); per-block FP64 partial
-// sums of resid^2 in a fixed order (deterministic).
+// sums of resid^2 in a fixed order (deterministic).  operand = 1: resid = dobs (a
+// migration operand); dobs = NULL: the operand is already in the trace buffer.
 template <typename T>
 __global__ void __launch_bounds__(kRedThreads) residual_kernel(const T* __restrict__ dobs,
                                                                T* __restrict__ tr, long long n,
@@ -130,7 +178,7 @@ __global__ void __launch_bounds__(kRedThreads) residual_kernel(const T* __restri
     const long long per_shot = (long long)nsteps * nrec;
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
          c += (long long)gridDim.x * blockDim.x) {
-        T r = operand ? dobs[c] : dobs[c] - tr[c];
+        T r = !dobs ? tr[c] : operand ? dobs[c] : dobs[c] - tr[c];
         // a shot's record ends at its own length: no residual after it
         if (shot_steps) {
             const long long sh = c / per_shot;
@@ -240,6 +288,9 @@ struct pysit_plan {
     virtual int autotune(const int* cand, int ncand, int nsteps, int* chosen, double* ms, cudaStream_t s) = 0;
     // enqueue misfit + gradient on s without graph handling (for a group's capture)
     virtual int enqueue_grad_raw(const void* dobs, double* grad, double* rnorm2, cudaStream_t s) = 0;
+    // linearised modelling / Gauss-Newton Hessian application for a model perturbation
+    virtual int born(const double* m1, void* traces, cudaStream_t s) = 0;
+    virtual int hessian(const double* m1, double* out, double* d1norm2, cudaStream_t s) = 0;
     int64_t last_launches = 0;
 };
 
@@ -285,7 +336,7 @@ struct PlanT final : public pysit_plan {
         size_t c2, sgx, sgy, sgz, mgx, mgy, mgz;
         size_t U[2], PX[2], PY[2], PZ[2], PS[2];   // forward state
         size_t A[2], AX[2], AY[2], AZ[2], AS[2];   // adjoint state
-        size_t ic, replay, ckpt, traces, srcamp;
+        size_t ic, replay, ckpt, traces, srcamp, m1;
         size_t sbox, srpb, srow, spt, sw;          // source injection
         size_t rbox, rrpb, rrow, rpt, rw;          // receiver injection
         size_t recrow, recoff, recw;               // recording
@@ -635,6 +686,7 @@ struct PlanT final : public pysit_plan {
             off.AS[b] = dim == 3 ? take(field_bytes) : off.AZ[b];
         }
         off.ic = take(field_bytes);
+        off.m1 = take(one);
         off.replay = take(field_bytes * (size_t)S);
         off.ckpt = take(field_bytes * (size_t)ckpt_fields * nseg);
         off.traces = take((size_t)G * nsteps * nrec * sizeof(T));
@@ -1004,7 +1056,8 @@ struct PlanT final : public pysit_plan {
         }
     }
 
-    void backward_sweep(int g0, int gn, cudaStream_t s) {
+    void backward_sweep(int g0, int gn, cudaStream_t s, int period = 0) {
+        if (period <= 0) period = p_img;
         zero_state(off.A, off.AX, off.AY, off.AZ, off.AS, s);
         cudaMemsetAsync(ws + off.ic, 0, field_bytes, s);
         State adj = make_state(off.A, off.AX, off.AY, off.AZ, off.AS);
@@ -1023,7 +1076,7 @@ struct PlanT final : public pysit_plan {
             for (int k = k0; k <= k1; ++k) {
                 bind_state(p, fw);
                 set_inject(p, true, g0, k, nullptr);
-                p.dw_out = (k % p_img == 0) ? fld(off.replay) + (size_t)(k - k0) * fstride * G : nullptr;
+                p.dw_out = (k % period == 0) ? fld(off.replay) + (size_t)(k - k0) * fstride * G : nullptr;
                 launch(p, kRecomp, s);
                 advance(fw);
             }
@@ -1031,13 +1084,122 @@ struct PlanT final : public pysit_plan {
             for (int k = k1; k >= k0; --k) {
                 bind_state(q, adj);
                 set_inject(q, false, g0, k, resid);
-                q.image = (k % p_img == 0);
+                q.image = (k % period == 0);
                 q.dw_in = fld(off.replay) + (size_t)(k - k0) * fstride * G;
                 q.ic = fld(off.ic);
                 launch(q, kAdj, s);
                 advance(adj);
             }
         }
+    }
+
+    // Linearised (Born) sweep of one group: the background field u0 (forward buffers) steps in
+    // recompute mode, writing dWaveOp0_k into replay slot 0; the scattered field u1 (adjoint
+    // buffers) steps without a source, its traces recorded before each step, then takes the
+    // Born source -m1 dWaveOp0_k (linear_forward_model, temporal_modeling.py:485-535).  With
+    // `checkpoints` the u0 state is saved every S steps as the forward sweep does.
+    void born_sweep(int g0, int gn, bool checkpoints, cudaStream_t s) {
+        zero_state(off.U, off.PX, off.PY, off.PZ, off.PS, s);
+        zero_state(off.A, off.AX, off.AY, off.AZ, off.AS, s);
+        State u0 = make_state(off.U, off.PX, off.PY, off.PZ, off.PS);
+        State u1 = make_state(off.A, off.AX, off.AY, off.AZ, off.AS);
+        WaveParams<T> p0 = base_params(g0, gn), p1 = base_params(g0, gn);
+        T* tr = at<T>(off.traces);
+        T* dw = fld(off.replay);
+        const long long rows = (long long)gn * nx * ny;
+        const int nb = (int)std::min<long long>(rows, 152LL * 16);
+        for (int k = 0; k < nsteps; ++k) {
+            if (checkpoints && k % S == 0) {
+                T* src[6]; T* dst[6];
+                ckpt_ptrs(u0, src);
+                for (int f = 0; f < ckpt_fields; ++f) dst[f] = ckpt_slot(k / S, f);
+                copy_fields(dst, src, s);
+            }
+            bind_state(p0, u0);
+            set_inject(p0, true, g0, k, nullptr);
+            p0.dw_out = dw;
+            launch(p0, kRecomp, s);
+            bind_state(p1, u1);
+            set_inject(p1, true, g0, k, nullptr);  // valid tables, switched off: u1 has no source
+            p1.inj.on = 0;
+            set_recording(p1, g0, gn, tr + (long long)k * nrec);
+            launch(p1, kFwd, s);
+            born_source_kernel<T><<<nb, 128, 0, s>>>(p1, dim, at<T>(off.m1), dw);
+            ++launches;
+            advance(u0);
+            advance(u1);
+        }
+    }
+
+    void pad_perturbation(const double* m1, cudaStream_t s) {
+        const long long n = (long long)nx * ny * nz;
+        const int px = nx - pad_lo[0] - pad_hi[0], py = ny - pad_lo[1] - pad_hi[1], pz = nz - pad_lo[2] - pad_hi[2];
+        edge_pad_kernel<T><<<grid_for(n, 256), 256, 0, s>>>(m1, nx, ny, nz, pad_lo[0], pad_lo[1], pad_lo[2], px, py,
+                                                            pz, hx, hy, rows_y, ldz, at<T>(off.m1));
+        ++launches;
+    }
+
+    void enqueue_born(const double* m1, void* traces_out, cudaStream_t s) {
+        reset_task_counter(s);
+        pad_perturbation(m1, s);
+        const size_t tr_group = (size_t)nsteps * nrec * sizeof(T);
+        for (int g0 = 0; g0 < nshots; g0 += G) {
+            const int gn = std::min(G, nshots - g0);
+            born_sweep(g0, gn, false, s);
+            if (nrec > 0)
+                cudaMemcpyAsync(static_cast<char*>(traces_out) + (size_t)g0 * tr_group, ws + off.traces, tr_group * gn,
+                                cudaMemcpyDeviceToDevice, s);
+        }
+    }
+
+    // sum_s F_s* F_s m1: each group's Born traces d1 are migrated at once with the u0
+    // checkpoints the Born sweep saved (apply_hessian 'approximate',
+    // temporal_least_squares.py:209-217; migrate_shot images every step)
+    void enqueue_hessian(const double* m1, double* out, double* d1norm2, cudaStream_t s) {
+        reset_task_counter(s);
+        pad_perturbation(m1, s);
+        cudaMemsetAsync(ws + off.gpad, 0, (size_t)nx * ny * nz * sizeof(double), s);
+        cudaMemsetAsync(ws + off.rnorm, 0, sizeof(double), s);
+        for (int g0 = 0; g0 < nshots; g0 += G) {
+            const int gn = std::min(G, nshots - g0);
+            born_sweep(g0, gn, true, s);
+            const long long n = (long long)gn * nsteps * nrec;
+            if (n > 0) {  // ||d1||^2, and a shot's record ends at its own length
+                residual_kernel<T><<<kRedBlocks, kRedThreads, 0, s>>>(
+                    nullptr, at<T>(off.traces), n, at<double>(off.partial), 1,
+                    shot_steps.empty() ? nullptr : at<int>(off.shsteps) + g0, nsteps, nrec);
+                sum_partials_kernel<<<1, kRedThreads, 0, s>>>(at<double>(off.partial), kRedBlocks, at<double>(off.rnorm),
+                                                              1);
+                launches += 2;
+            }
+            backward_sweep(g0, gn, s, 1);
+            const long long nc = (long long)nx * ny * nz;
+            reduce_ic_kernel<T><<<grid_for(nc, 256), 256, 0, s>>>(fld(off.ic), fstride, gn, nx, ny, nz, hx, hy, rows_y,
+                                                                  ldz, -dt, at<double>(off.gpad));
+            ++launches;
+        }
+        const int px = nx - pad_lo[0] - pad_hi[0], py = ny - pad_lo[1] - pad_hi[1], pz = nz - pad_lo[2] - pad_hi[2];
+        fold_kernel<<<grid_for((long long)px * py * pz, 256), 256, 0, s>>>(at<double>(off.gpad), nx, ny, nz, pad_lo[0],
+                                                                           pad_hi[0], pad_lo[1], pad_hi[1], pad_lo[2],
+                                                                           pad_hi[2], out);
+        ++launches;
+        if (d1norm2) cudaMemcpyAsync(d1norm2, ws + off.rnorm, sizeof(double), cudaMemcpyDeviceToDevice, s);
+    }
+
+    int born(const double* m1, void* traces, cudaStream_t s) override {
+        PGB_REQUIRE(ws, "no workspace bound");
+        PGB_REQUIRE(model_set, "pysit_plan_set_model must be called first");
+        PGB_REQUIRE(m1, "NULL model perturbation");
+        PGB_REQUIRE(traces || nrec == 0, "NULL traces output");
+        return run(4, m1, traces, nullptr, nullptr, s, [&](cudaStream_t st) { enqueue_born(m1, traces, st); });
+    }
+
+    int hessian(const double* m1, double* out, double* d1norm2, cudaStream_t s) override {
+        PGB_REQUIRE(ws, "no workspace bound");
+        PGB_REQUIRE(model_set, "pysit_plan_set_model must be called first");
+        PGB_REQUIRE(m1 && out, "NULL argument");
+        return run(5, m1, out, d1norm2, nullptr, s,
+                   [&](cudaStream_t st) { enqueue_hessian(m1, out, d1norm2, st); });
     }
 
     // the 2D sweep's task counter restarts at zero with every run (eager or graph replay)
@@ -1340,6 +1502,16 @@ extern "C" int pysit_plan_misfit(pysit_plan* p, const void* dobs, double* rnorm2
                                  void* stream) {
     PGB_REQUIRE(p, "NULL plan");
     return p->gradient(dobs, nullptr, rnorm2, traces, (cudaStream_t)stream, false, false);
+}
+
+extern "C" int pysit_plan_born(pysit_plan* p, const double* m1, void* traces, void* stream) {
+    PGB_REQUIRE(p, "NULL plan");
+    return p->born(m1, traces, (cudaStream_t)stream);
+}
+
+extern "C" int pysit_plan_hessian(pysit_plan* p, const double* m1, double* out, double* d1norm2, void* stream) {
+    PGB_REQUIRE(p, "NULL plan");
+    return p->hessian(m1, out, d1norm2, (cudaStream_t)stream);
 }
 
 extern "C" int pysit_plan_status(pysit_plan* p, int* flags, void* stream) {

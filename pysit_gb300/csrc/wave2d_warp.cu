@@ -255,8 +255,9 @@ __device__ __forceinline__ void sweep(const WaveParams<T>& p, unsigned char* wsm
         sgz[v] = (PML && z < p.nz) ? __ldg(p.sgz + z) : T(0);
         mgz[v] = (PML && MODE == kRecomp && z < p.nz) ? __ldg(p.mgz + z) : T(0);
     }
+    // the box is read only when the step injects (its table may be absent otherwise)
     const int* bx = p.inj.box + shot * 6;
-    const int bx0 = __ldg(bx), bx1 = __ldg(bx + 1);
+    const int bx0 = p.inj.on ? __ldg(bx) : 0, bx1 = p.inj.on ? __ldg(bx + 1) : 0;
     const bool inj_task = p.inj.on && bx0 < x1 && bx1 > x0 && __ldg(bx + 4) < ze && __ldg(bx + 5) > zs;
     // weight pairs, built once per task
     P wx[R + 1], wz[R + 1], a1[R + 1];

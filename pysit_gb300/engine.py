@@ -249,6 +249,40 @@ class WavePlan:
             C.c_void_p(self.rnorm2.data_ptr()), C.c_void_p(_native.stream_handle())))
         return self.grad
 
+    def _perturbation(self, m1):
+        """Copy a model perturbation (unpadded, m-space) into the plan's FP64 device buffer."""
+        torch = _native.require_cuda()
+        if not hasattr(self, "m1"):
+            self.m1 = torch.zeros(self.mesh.dof(include_bc=False), dtype=torch.float64, device="cuda")
+            self.hess = torch.zeros_like(self.m1)
+        data = m1.data if hasattr(m1, "with_padding") else m1  # a model perturbation or an array
+        if isinstance(data, torch.Tensor):
+            self.m1.copy_(data.reshape(-1).to(torch.float64))
+        else:
+            self.m1.copy_(torch.from_numpy(np.ascontiguousarray(np.asarray(data, dtype=np.float64).reshape(-1))))
+        return self.m1
+
+    def born(self, m1):
+        """Linearised traces F m1 of all shots [nshots, nsteps, nrec] (device): the u1 field of
+        TemporalModeling.linear_forward_model driven by -m1 dWaveOp0 (m1 edge-padded)."""
+        self.set_model()
+        m = self._perturbation(m1)
+        _native.check(_native.load().pysit_plan_born(self._h, C.c_void_p(m.data_ptr()),
+                                                     C.c_void_p(self.traces.data_ptr()),
+                                                     C.c_void_p(_native.stream_handle())))
+        return self.traces
+
+    def hessian(self, m1):
+        """Gauss-Newton Hessian application sum_s F_s* F_s m1 (FP64 device, unpadded, m-space),
+        apply_hessian 'approximate'; returns (H m1, ||F m1||^2)."""
+        self.set_model()
+        m = self._perturbation(m1)
+        _native.check(_native.load().pysit_plan_hessian(self._h, C.c_void_p(m.data_ptr()),
+                                                        C.c_void_p(self.hess.data_ptr()),
+                                                        C.c_void_p(self.rnorm2.data_ptr()),
+                                                        C.c_void_p(_native.stream_handle())))
+        return self.hess, self.rnorm2
+
     def autotune(self, candidates=None, nsteps=16):
         """Time the task lengths along x in `candidates` (forward + adjoint steps on this plan's
         buffers), keep the fastest for this plan and for later plans of the same configuration.

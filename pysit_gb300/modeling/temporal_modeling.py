@@ -5,10 +5,12 @@
   migrate_shot(shot, m0, operand_simdata, imaging_period, ..., dWaveOp=None) (:171-214)
   adjoint_model(shot, m0, operand_simdata, imaging_period=1, operand_dWaveOpAdj=None,
                 operand_model=None, return_parameters=[], dWaveOp=None, wavefield=None) (:228-387)
+  linear_forward_model(shot, m0, m1, return_parameters=[], dWaveOp0=None)   (:389-546)
 
 Two device paths implement them:
   * the batched plan (engine.WavePlan) when only traces or an image are asked
-    for: forward_model(..., ['simdata']) and migrate_shot without dWaveOp;
+    for: forward_model(..., ['simdata']), linear_forward_model(..., ['simdata'])
+    and migrate_shot without dWaveOp;
   * the plain per-step loop of the reference, every step on the GPU
     (solver.time_step on device-resident solver data, dWaveOp stored per step
     on the device), for 'wavefield' / 'dWaveOp' / 'adjointfield' outputs and for
@@ -123,6 +125,82 @@ class TemporalModeling:
             retval["wavefield"] = us
         if "dWaveOp" in rp:
             retval["dWaveOp"] = dwo if device_outputs else [d.cpu().numpy() for d in dwo]
+        if simdata is not None:
+            retval["simdata"] = simdata if device_outputs else simdata.double().cpu().numpy()
+        return retval
+
+    # ------------------------------------------------------------------------------
+    def linear_forward_model(self, shot, m0, m1, return_parameters=[], dWaveOp0=None):
+        """Born modelling about m0: u1 driven by rhs_k = -m1_edge * dWaveOp0_k, traces of u1_k
+        recorded before step k.  'simdata' alone (dWaveOp0 not given) runs the batched plan;
+        'wavefield1', 'dWaveOp0', 'dWaveOp1' or a given dWaveOp0 run the reference's loop
+        step by step on the device."""
+        solver = self.solver
+        solver.model_parameters = m0
+        rp = set(return_parameters)
+        if self.batched and rp <= {"simdata"} and dWaveOp0 is None:
+            retval = {}
+            if "simdata" in rp:
+                plan = plan_for(solver, [shot])
+                tr = plan.born(m1)
+                retval["simdata"] = tr[0, :, :shot.receivers.receiver_count].to(
+                    dtype=__import__("torch").float64).cpu().numpy()
+            return retval
+        return self._linear_plain(shot, m1, rp, dWaveOp0)
+
+    def _linear_plain(self, shot, m1, rp, dWaveOp0=None, device_outputs=False):
+        torch = _native.require_cuda()
+        solver = self.solver
+        mesh = solver.mesh
+        nsteps = solver.nsteps
+        ops = _DeviceOps(solver, shot)
+        dev = lambda a: a.reshape(-1) if isinstance(a, torch.Tensor) else torch.as_tensor(  # noqa: E731
+            np.asarray(a).reshape(-1), dtype=ops.tdt, device="cuda")
+        m1p = torch.as_tensor(np.asarray(m1.with_padding(padding_mode="edge").data).reshape(-1), dtype=ops.tdt,
+                              device="cuda")
+        sd = solver.DeviceSolverData()
+        rhs = torch.zeros(ops.dof, dtype=ops.tdt, device="cuda")
+        if dWaveOp0 is None:
+            # background field one step ahead: dWaveOp0_k needs u0_{k+1}
+            sd0 = solver.DeviceSolverData()
+            rhs0 = torch.zeros(ops.dof, dtype=ops.tdt, device="cuda")
+            solver.time_step(sd0, ops.source_rhs(0, rhs0), None)
+            dw0_k = solver.compute_dWaveOp("time", sd0)
+            sd0.advance()
+        us, dw0s, dw1s = [], [], []
+        simdata = torch.zeros((nsteps, ops.nrec), dtype=ops.tdt, device="cuda") if "simdata" in rp else None
+        for k in range(nsteps):
+            uk = sd.k.u
+            if "wavefield1" in rp:
+                us.append(mesh.unpad_array(uk.reshape(-1, 1)).cpu().numpy().copy())
+            if simdata is not None:
+                ops.sample(uk, simdata[k])
+            if dWaveOp0 is None:
+                solver.time_step(sd0, ops.source_rhs(k + 1, rhs0), None)
+                dw0_kp1 = solver.compute_dWaveOp("time", sd0)
+                sd0.advance()
+            else:
+                dw0_k = dev(dWaveOp0[k])
+            if "dWaveOp0" in rp:
+                dw0s.append(dw0_k)
+            torch.mul(m1p, dw0_k.reshape(-1), out=rhs)
+            rhs.neg_()
+            solver.time_step(sd, rhs, None)
+            if "dWaveOp1" in rp:
+                dw1s.append(solver.compute_dWaveOp("time", sd))
+            if k == nsteps - 1:
+                break
+            sd.advance()
+            if dWaveOp0 is None:
+                dw0_k = dw0_kp1
+        host = (lambda L: L) if device_outputs else (lambda L: [d.cpu().numpy() for d in L])  # noqa: E731
+        retval = {}
+        if "wavefield1" in rp:
+            retval["wavefield1"] = us
+        if "dWaveOp0" in rp:
+            retval["dWaveOp0"] = host(dw0s)
+        if "dWaveOp1" in rp:
+            retval["dWaveOp1"] = host(dw1s)
         if simdata is not None:
             retval["simdata"] = simdata if device_outputs else simdata.double().cpu().numpy()
         return retval

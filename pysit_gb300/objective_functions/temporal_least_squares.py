@@ -141,4 +141,42 @@ class TemporalLeastSquares(ObjectiveFunctionBase):
         return grad
 
     def apply_hessian(self, shots, m0, m1, hessian_mode="approximate", levenberg_mu=0.0, *args, **kwargs):
-        raise NotImplementedError("Hessian application (Born modelling) is not implemented in pysit_gb300 yet")
+        """Hessian application at m0 (temporal_least_squares.py:200-249).
+
+        'approximate' (Gauss-Newton, sum_s F_s* F_s m1) and 'levenberg' (+ mu m1) run as one
+        batched plan call over all shots when ``batched``; 'full' adds the second-order terms
+        driven by the residual and runs the reference's per-shot loop on the plain device path.
+        Every migration images at every step (imaging period 1, the period of the dWaveOp0
+        lists; the reference's call of migrate_shot omits that positional argument).  `m1` is
+        a model perturbation or a plain array of the unpadded grid."""
+        modes = ["approximate", "full", "levenberg"]
+        if hessian_mode not in modes:
+            raise ValueError("Invalid Hessian mode.  Valid options for applying hessian are {0}".format(modes))
+        if not hasattr(m1, "with_padding"):
+            m1 = m0.perturbation(data=np.asarray(m1, dtype=float).reshape(-1, 1))
+        mt = self.modeling_tools
+        if self.batched and hessian_mode in ("approximate", "levenberg"):
+            self.solver.model_parameters = m0
+            plan = plan_for(self.solver, list(shots), 1, **self.plan_kwargs)
+            self.last_plan = plan
+            h, _ = plan.hessian(m1)
+            result = m0.perturbation(data=h.cpu().numpy().reshape(-1, 1))
+        else:
+            result = m0.perturbation()
+            for shot in shots:
+                if hessian_mode in ("approximate", "levenberg"):
+                    self.solver.model_parameters = m0
+                    dWaveOp0 = mt._forward_plain(shot, 1, {"dWaveOp"}, device_outputs=True)["dWaveOp"]
+                    d1 = mt._linear_plain(shot, m1, {"simdata"}, dWaveOp0=dWaveOp0, device_outputs=True)["simdata"]
+                    result += mt.migrate_shot(shot, m0, d1, 1, dWaveOp=dWaveOp0)
+                else:
+                    dWaveOp0 = []
+                    r0 = self._residual(shot, m0, dWaveOp=dWaveOp0)
+                    lin = mt._linear_plain(shot, m1, {"simdata", "dWaveOp1"}, dWaveOp0=dWaveOp0, device_outputs=True)
+                    dWaveOpAdj1 = []
+                    result += mt.migrate_shot(shot, m0, r0, 1, dWaveOp=lin["dWaveOp1"], dWaveOpAdj=dWaveOpAdj1)
+                    result += mt.migrate_shot(shot, m0, lin["simdata"], 1, operand_dWaveOpAdj=dWaveOpAdj1,
+                                              operand_model=m1, dWaveOp=dWaveOp0)
+        if hessian_mode == "levenberg":
+            result += levenberg_mu * m1
+        return result

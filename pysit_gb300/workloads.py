@@ -21,7 +21,9 @@ No public dataset is involved: each model is generated from a named seed.
 ``python -m pysit_gb300.workloads cfg5 [--iterations N] [--shots N] [--scale s]
 [--nsteps N] [--plain]`` runs the FWI and prints one JSON line (objective history,
 relative L2 error of the final model, wall time); ``... cfg4`` times the uneven
-batch, grid by grid and as one group.
+batch, grid by grid and as one group; ``... hessian`` times the gradient, Born
+modelling and the Gauss-Newton Hessian application of the cfg2 workload; ``... gn``
+runs Gauss-Newton iterations (GMRES on the GPU Hessian) on the cfg5 model.
 """
 from __future__ import annotations
 
@@ -32,7 +34,8 @@ from scipy.ndimage import gaussian_filter
 
 from . import core, solvers
 
-__all__ = ["layered_model", "cfg2", "cfg3", "cfg4", "cfg5", "run_lbfgs", "run_uneven_batch"]
+__all__ = ["layered_model", "cfg2", "cfg3", "cfg4", "cfg5", "run_lbfgs", "run_uneven_batch", "run_hessian",
+           "run_gauss_newton"]
 
 
 def layered_model(shape, nlayers, vmin, vmax, sigma_cells, amp, seed, clip=(1500.0, 5500.0)):
@@ -238,12 +241,81 @@ def run_uneven_batch(grids, repeats=2):
             "shots_per_s_group": nshots / t_grp, "group_speedup": t_seq / t_grp, "status": status}
 
 
+def run_hessian(m, shots, solver, C, C0, repeats=2):
+    """Observed data on the true model, then at the start model: the batched gradient, Born
+    modelling F m1 and the Gauss-Newton Hessian application sum_s F_s* F_s m1 of all shots, each
+    timed as one plan call (m1 a seeded smooth perturbation of 1 % of m0).  Returns seconds and
+    shots/s of each."""
+    import time
+
+    import torch
+
+    from .engine import WavePlan
+
+    solver.model_parameters = solver.ModelParameters(m, {"C": C})
+    obs = WavePlan(solver, shots).forward().clone()
+    ts_true = solver.ts()
+    solver.model_parameters = solver.ModelParameters(m, {"C": C0})
+    plan = WavePlan(solver, shots)
+    plan.autotune()
+    from .autograd import resample_linear
+    plan.dobs.copy_(resample_linear(obs, ts_true, solver.ts()))
+    del obs
+    torch.cuda.empty_cache()
+    shape = tuple(m.shape(as_grid=True))
+    rng = np.random.default_rng(2029)
+    m1 = 0.01 * gaussian_filter(rng.standard_normal(shape), 4.0).reshape(-1) / np.asarray(C0).reshape(-1) ** 2
+    out = {"shots": len(shots), "grid": [int(v) for v in shape], "nsteps": int(plan.nsteps), "tile_x": int(plan.tile_x)}
+    for name, fn in (("gradient", plan.gradient), ("born", lambda: plan.born(m1)),
+                     ("hessian", lambda: plan.hessian(m1))):
+        fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(repeats):
+            fn()
+        torch.cuda.synchronize()
+        t = (time.perf_counter() - t0) / repeats
+        out[f"{name}_s"] = t
+        out[f"{name}_shots_per_s"] = len(shots) / t
+        out[f"{name}_launches"] = plan.launches()
+    out["hessian_norm"] = float(plan.hess.norm().item())
+    out["status"] = plan.status()
+    return out
+
+
+def run_gauss_newton(m, shots, solver, C, C0, iterations=3, krylov_maxiter=5, batched=True, verbose=False):
+    """PySIT-style Gauss-Newton (GMRES inner solve on the batched GPU Hessian, backtracking line
+    search with alpha0 = 1) from the smoothed start model; objective history, relative model
+    error before and after, wall time."""
+    import time
+
+    from .modeling import generate_seismic_data
+    from .objective_functions import TemporalLeastSquares
+    from .optimization import GaussNewton
+
+    generate_seismic_data(shots, solver, solver.ModelParameters(m, {"C": C}))
+    obj = TemporalLeastSquares(solver, batched=batched)
+    gn = GaussNewton(obj, krylov_maxiter=krylov_maxiter)
+    start = solver.ModelParameters(m, {"C": C0})
+    t0 = time.perf_counter()
+    final = gn(shots, start, iterations, line_search="backtrack", verbose=verbose,
+               status_configuration={"objective_frequency": 1})
+    wall = time.perf_counter() - t0
+    _, objective = gn.retrieve_history("objective")
+    _, alpha = gn.retrieve_history("alpha")
+    err = lambda c: float(np.linalg.norm(np.asarray(c).reshape(-1) - C.reshape(-1)) / np.linalg.norm(C))  # noqa: E731
+    return {"iterations": iterations, "krylov_maxiter": krylov_maxiter, "shots": len(shots),
+            "objective": [float(v) for v in objective], "alpha": [float(v) for v in alpha],
+            "model_error_start": err(C0), "model_error_final": err(final.C), "wall_s": wall}
+
+
 def _main(argv=None):
     import argparse
     import json
 
     ap = argparse.ArgumentParser(prog="python -m pysit_gb300.workloads")
-    ap.add_argument("workload", choices=["cfg4", "cfg5"])
+    ap.add_argument("workload", choices=["cfg4", "cfg5", "hessian", "gn"])
+    ap.add_argument("--krylov", type=int, default=5, help="gn: GMRES iterations per Gauss-Newton step")
     ap.add_argument("--iterations", type=int, default=20)
     ap.add_argument("--shots", type=int, default=None, help="default 256 (cfg4), 128 (cfg5)")
     ap.add_argument("--nsteps", type=int, default=4000)
@@ -256,7 +328,21 @@ def _main(argv=None):
         out.update(workload="cfg4", scale=a.scale)
         print(json.dumps(out))
         return
+    if a.workload == "hessian":
+        m, shots, solver, C, C0 = cfg2(scale=a.scale, nshots=a.shots or 64, nsteps=a.nsteps)
+        out = run_hessian(m, shots, solver, C, C0)
+        out.update(workload="hessian on the cfg2 model", scale=a.scale)
+        print(json.dumps(out))
+        return
     prec = "double" if a.plain else "single"
+    if a.workload == "gn":
+        m, shots, solver, C, C0 = cfg5(scale=a.scale, nshots=a.shots or 64, nsteps=a.nsteps, precision=prec)
+        out = run_gauss_newton(m, shots, solver, C, C0, iterations=a.iterations, krylov_maxiter=a.krylov,
+                               batched=not a.plain, verbose=a.verbose)
+        out.update(workload="Gauss-Newton on the cfg5 model", path="plain FP64" if a.plain else "batched FP32",
+                   scale=a.scale)
+        print(json.dumps(out))
+        return
     m, shots, solver, C, C0 = cfg5(scale=a.scale, nshots=a.shots or 128, nsteps=a.nsteps, precision=prec)
     out = run_lbfgs(m, shots, solver, C, C0, iterations=a.iterations, batched=not a.plain, verbose=a.verbose)
     out.update(workload=a.workload, path="plain FP64" if a.plain else "batched FP32", scale=a.scale)

@@ -126,3 +126,81 @@ def test_optimizer_matches_the_reference_class(ref_optimization, which, kw, ls):
     assert np.all(np.isfinite(fin_new.C)) and v_new[-1] < v_new[0]
     np.testing.assert_allclose(fin_new.C, fin_ref.C, rtol=1e-12, atol=0)
     assert (o_new.n_eval, o_new.n_grad) == (o_ref.n_eval, o_ref.n_grad)
+
+
+# ---- Gauss-Newton and its Krylov solvers ------------------------------------------------
+
+class _ObjectiveGN(_Objective):
+    """_Objective with its Gauss-Newton Hessian H v = (a + 3 b d^2) v (same inner product)."""
+
+    def __init__(self, *args):
+        super().__init__(*args)
+        self.n_hess = 0
+
+    def apply_hessian(self, shots, m0, m1, hessian_mode="approximate", levenberg_mu=0.0, **kwargs):
+        self.n_hess += 1
+        d = self._d(m0)
+        v = np.asarray(getattr(m1, "data", m1), dtype=float).reshape(d.shape)
+        return m0.perturbation(data=(self.a + 3 * self.b * d ** 2) * v)
+
+
+def test_gmres_and_cg_solve_small_systems():
+    from pysit_gb300.optimization import krylov
+    rng = np.random.default_rng(4)
+    n = 40
+    A = np.eye(n) * 4 + rng.standard_normal((n, n)) * 0.3
+    b = rng.standard_normal(n)
+    x_true = np.linalg.solve(A, b)
+    res = []
+    x, info = krylov.gmres(lambda v: A @ v, b, tol=1e-12, maxiter=n, residuals=res)
+    assert info == 0 and np.linalg.norm(x - x_true) < 1e-9 * np.linalg.norm(x_true)
+    assert res[0] == pytest.approx(np.linalg.norm(b)) and res[-1] <= 1e-12 * np.linalg.norm(b) * 1.0001
+    # restarted: 10 cycles of 8
+    x, info = krylov.gmres(A, b, tol=1e-10, restrt=8, maxiter=10)
+    assert info == 0 and np.linalg.norm(A @ x - b) <= 1e-10 * np.linalg.norm(b) * 1.0001
+    # too few iterations: info = iterations run, residual still decreasing
+    res = []
+    x, info = krylov.gmres(A, b, tol=1e-14, maxiter=3, residuals=res)
+    assert info == 3 and len(res) == 4 and res[-1] < res[0]
+    assert res[-1] == pytest.approx(np.linalg.norm(A @ x - b), rel=1e-8)
+    # SPD system with cg
+    S = A @ A.T + np.eye(n)
+    x, info = krylov.cg(lambda v: S @ v, b, tol=1e-12, maxiter=200)
+    assert info == 0 and np.linalg.norm(S @ x - b) <= 1e-11 * np.linalg.norm(b)
+    x, info = krylov.gmres(A, np.zeros(n))
+    assert info == 0 and not x.any()
+
+
+def test_gauss_newton_converges_fast_and_keeps_histories():
+    m, C0, m_true, a, b = _problem()
+    obj = _ObjectiveGN(m, m_true, a, b)
+    opt, final = _run(api.GaussNewton, obj, m, C0, 6, krylov_maxiter=10)
+    _, vals = opt.retrieve_history("objective")
+    assert all(v1 < v0 for v0, v1 in zip(vals, vals[1:]))
+    assert vals[-1] < 1e-6 * vals[0]  # Newton: linear far out on the quartic, then quadratic
+    assert vals[-1] / vals[-2] < 1e-3
+    _, alphas = opt.retrieve_history("alpha")
+    assert len(alphas) == 6 and alphas[0] <= 1.0
+    assert obj.n_hess >= 6
+    assert opt.krylov_residuals[-1] < opt.krylov_residuals[0]
+
+
+def test_gauss_newton_matches_the_reference_class(ref_optimization, monkeypatch):
+    """The reference's GaussNewton takes pyamg.krylov.gmres (absent here); with this package's
+    gmres in its place both classes take the same steps on the same objective."""
+    from pysit_gb300.optimization import krylov
+    ref_gn = sys.modules[ref_optimization.GaussNewton.__module__]
+    monkeypatch.setattr(ref_gn, "gmres", krylov.gmres)
+    m, C0, m_true, a, b = _problem()
+    o_ref = _ObjectiveGN(m, m_true, a, b)
+    opt_ref, fin_ref = _run(ref_optimization.GaussNewton, o_ref, m, C0, 3, krylov_maxiter=6)
+    o_new = _ObjectiveGN(m, m_true, a, b)
+    opt_new, fin_new = _run(api.GaussNewton, o_new, m, C0, 3, krylov_maxiter=6)
+    _, v_ref = opt_ref.retrieve_history("objective")
+    _, v_new = opt_new.retrieve_history("objective")
+    np.testing.assert_allclose(v_new, v_ref, rtol=1e-12, atol=0)
+    _, a_ref = opt_ref.retrieve_history("alpha")
+    _, a_new = opt_new.retrieve_history("alpha")
+    np.testing.assert_allclose(a_new, a_ref, rtol=1e-12, atol=0)
+    np.testing.assert_allclose(fin_new.C, fin_ref.C, rtol=1e-12, atol=0)
+    assert (o_new.n_eval, o_new.n_grad, o_new.n_hess) == (o_ref.n_eval, o_ref.n_grad, o_ref.n_hess)
