@@ -13,7 +13,8 @@ from .core import *  # noqa: F401,F403
 from .solvers import (ConstantDensityAcousticWave, ConstantDensityAcousticParameters,  # noqa: F401
                       ConstantDensityAcousticTimeScalar_1D_cuda, ConstantDensityAcousticTimeScalar_2D_cuda,
                       ConstantDensityAcousticTimeScalar_3D_cuda, NoMatchError, MultipleMatchError)
-from .modeling import TemporalModeling, generate_seismic_data, generate_shot_data_time  # noqa: F401
+from .modeling import (TemporalModeling, generate_seismic_data, generate_seismic_data_from_file,  # noqa: F401
+                       generate_shot_data_time)
 from .objective_functions import TemporalLeastSquares  # noqa: F401
 from .optimization import LBFGS, GradientDescent, GaussNewton  # noqa: F401
 

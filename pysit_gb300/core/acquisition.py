@@ -30,7 +30,8 @@ import numpy as np
 import scipy.sparse as spsp
 
 __all__ = ["DerivativeGaussianPulse", "RickerWavelet", "GaussianPulse", "PointSource", "SourceSet",
-           "PointReceiver", "ReceiverSet", "Shot", "equispaced_acquisition", "linear_interpolate"]
+           "PointReceiver", "ReceiverSet", "Shot", "SourceEncodedSupershot", "equispaced_acquisition",
+           "linear_interpolate"]
 
 _SQRT2 = math.sqrt(2.0)
 
@@ -383,6 +384,87 @@ class Shot:
         if offset is not None:
             raise NotImplementedError("Gather by offset not yet implemented.")
         return self.receivers.data if as_array else self.receivers
+
+
+class SourceEncodedSupershot(Shot):
+    """Source-encoded supershot (pysit/core/shot.py:148-345), time domain.
+
+    The member shots' point sources fire together, source i with intensity code_i; the
+    observed data are encoded the same way, sum_i code_i d_i.  Codes are i.i.d. standard
+    normal ('gaussian') or +-1 with equal odds ('krebs'); ``encode()`` draws new ones.
+    The members must have point sources, the same receivers (fixed spread: identical
+    sampling operators) and recorded time data.  On the GPU a supershot is one shot of
+    the batched plan with one injection point per member source.
+
+    The reference class cannot be constructed: its encoded source set calls
+    ``super().__init__(self, ...)`` (shot.py:196), a TypeError, and its 'krebs' codes use
+    ``np.random.random_integers``, removed from numpy.  Here the set is a SourceSet of
+    copies of the member sources and 'krebs' draws ``randint(0, 2)`` (the same draw).
+    Codes come from numpy's global generator as in the reference, or from ``rng`` (a
+    numpy Generator) when given.  The frequency-domain branch is outside this path.
+    """
+
+    def __init__(self, shots, weight_type="gaussian", rng=None):
+        self.weight_type = weight_type
+        self._rng = rng
+        self.encoding = 0  # bumped by every encode(); plans built for an older encoding are not reused
+        self.sequential_shots = shots
+
+    def generate_weight_vector(self):
+        n = self._nshots
+        if self.weight_type == "gaussian":
+            return self._rng.standard_normal(n) if self._rng is not None else np.random.randn(n)
+        if self.weight_type == "krebs":
+            draw = self._rng.integers(0, 2, n) if self._rng is not None else np.random.randint(0, 2, n)
+            return 2 * draw - 1
+        raise Exception("Incorrect weight type supplied.")
+
+    def encode(self, codes=None):
+        """Draw new codes (or take `codes`), rebuild the encoded sources and data."""
+        import copy
+        shots = self._sequential_shots
+        codes = self.generate_weight_vector() if codes is None else np.asarray(codes, dtype=float)
+        if len(codes) != self._nshots:
+            raise ValueError("one code per member shot is needed")
+        sources = []
+        for shot, c in zip(shots, codes):
+            src = copy.copy(shot.sources)
+            src.intensity = float(c) * shot.sources.intensity
+            sources.append(src)
+        enc = SourceSet(shots[0].sources.mesh, sources)
+        receivers = copy.deepcopy(shots[0].receivers)
+        receivers.data = sum(float(c) * np.asarray(s.receivers.data, dtype=float) for s, c in zip(shots, codes))
+        self.codes = np.asarray(codes, dtype=float)
+        self.sources = enc
+        enc.set_shot(self)
+        self.receivers = receivers
+        receivers.set_shot(self)
+        self.encoding += 1
+
+    @property
+    def sequential_shots(self):
+        return self._sequential_shots
+
+    @sequential_shots.setter
+    def sequential_shots(self, shots):
+        shots = list(shots)
+        if not shots:
+            raise ValueError("a supershot needs at least one shot")
+        for shot in shots:
+            if type(shot.sources) is not PointSource:
+                raise Exception("The shots have to have a PointSource as source.")
+        ref_op = shots[0].receivers.sampling_operator
+        for shot in shots:
+            op = shot.receivers.sampling_operator
+            if op.shape != ref_op.shape or abs(op - ref_op).nnz != 0:
+                raise Exception("The receiver acquisition has to be the same for each shot in order to "
+                                "construct a supershot.")
+        if getattr(shots[0].receivers, "data", None) is None:
+            raise Exception("No time data recorded yet.")
+        self._sequential_shots = shots
+        self._nshots = len(shots)
+        self.is_time_simulation = True
+        self.encode()
 
 
 def equispaced_acquisition(mesh, wavelet, sources=1, receivers="max", source_depth=None,

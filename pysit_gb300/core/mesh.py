@@ -171,23 +171,26 @@ class CartesianMesh:
         sh_in_g = self.shape(include_bc=False, as_grid=True)
         sh_out_v = self.shape(include_bc=True, as_grid=False)
         sh_out_g = self.shape(include_bc=True, as_grid=True)
+        # a caller's out_array is filled through a grid-shaped view of it (the reference
+        # reshapes it in place; the returned array has the reference's shape either way)
         if out_array is not None:
-            out_array.shape = sh_out_g
+            grid = out_array.reshape(sh_out_g)
+            if not np.shares_memory(grid, out_array):
+                raise ValueError("out_array must be contiguous")
         if padding_mode is not None:
             pads = tuple((self.parameters[i].lbc.n, self.parameters[i].rbc.n) for i in range(self.dim))
             padded = np.pad(np.asarray(in_array).reshape(sh_in_g), pads, mode=padding_mode)
             if out_array is not None:
-                out_array[:] = padded
+                grid[:] = padded
             else:
-                out_array = padded
+                grid = padded
         else:
             if out_array is None:
-                out_array = np.zeros(sh_out_g, dtype=in_array.dtype)
+                grid = np.zeros(sh_out_g, dtype=in_array.dtype)
             sl = tuple(slice(self.parameters[i].lbc.n, sh_out_g[i] - self.parameters[i].rbc.n)
                        for i in range(self.dim))
-            out_array[sl] = np.asarray(in_array).reshape(sh_in_g)
-        out_array.shape = sh_out_v if tuple(in_array.shape) == sh_in_v else sh_out_g
-        return out_array
+            grid[sl] = np.asarray(in_array).reshape(sh_in_g)
+        return grid.reshape(sh_out_v if tuple(in_array.shape) == sh_in_v else sh_out_g)
 
     def inner_product(self, a, b):
         return np.dot(np.ravel(a), np.ravel(b)) * math.prod(self.deltas)

@@ -355,7 +355,8 @@ class PlanGroup:
 
 def plan_for(solver, shots, imaging_period=1, **kw):
     """Cached WavePlan of a solver for a shot list (rebuilt when dt/nsteps change)."""
-    key = (tuple(id(s) for s in shots), solver.dt, solver.nsteps, solver.precision,
+    # a source-encoded supershot carries an encoding counter: a new encoding needs a new plan
+    key = (tuple((id(s), getattr(s, "encoding", 0)) for s in shots), solver.dt, solver.nsteps, solver.precision,
            solver.spatial_accuracy_order, getattr(solver, "pml_psi", "reference"), int(imaging_period),
            tuple(sorted(kw.items())))
     cache = solver._plans
