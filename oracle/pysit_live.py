@@ -49,6 +49,14 @@ def _absent(*args, **kwargs):
     raise RuntimeError("optional dependency is absent in this environment")
 
 
+def _stub_getattr(attr):
+    # dunder names (__file__, __spec__ ...) stay absent, so that tools walking
+    # sys.modules (inspect.getmodule) see an ordinary module without a file
+    if attr.startswith("__") and attr.endswith("__"):
+        raise AttributeError(attr)
+    return _absent
+
+
 def _stub(name):
     if name in sys.modules:
         return sys.modules[name]
@@ -56,7 +64,7 @@ def _stub(name):
     mod.__path__ = []  # behave as a package so submodule stubs can hang off it
     # any attribute (e.g. pyamg.gallery.stencil_grid) resolves to a callable that
     # raises only if the reference actually uses it on the path under test
-    mod.__getattr__ = lambda attr: _absent
+    mod.__getattr__ = _stub_getattr
     sys.modules[name] = mod
     parent, _, child = name.rpartition(".")
     if parent and parent in sys.modules:
