@@ -3,8 +3,11 @@
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--scale s]
 
 A step is one full misfit + gradient of the 64-shot batch (1152 x 384 cells at
-12.5 m + 40-cell PML, order 8, 4000 time steps, checkpoints every 64 steps,
-seeded synthetic model: pysit_gb300.workloads.cfg2).  Output: one JSON line.
+12.5 m + 40-cell PML, order 8, 4000 time steps, seeded synthetic model:
+pysit_gb300.workloads.cfg2).  The gradient schedule is chosen by --schedule
+(default auto): 'store' keeps dWaveOp of every step in HBM (as many shots per
+launch as fit, no recompute sweep), 'checkpoint' recomputes it from checkpoints
+every 64 steps.  Output: one JSON line.
   value  shots/s with the observed data already resident in HBM (plan call)
   e2e    shots/s through the public torch.autograd API (FWIMisfit): every step
          copies the velocity and the observed traces from pinned host memory to
@@ -165,6 +168,8 @@ def main():
     ap.add_argument("--shots", type=int, default=64)
     ap.add_argument("--nsteps", type=int, default=4000)
     ap.add_argument("--shots-per-launch", type=int, default=None)
+    ap.add_argument("--schedule", default="auto", choices=["checkpoint", "store", "auto"],
+                    help="gradient schedule: recompute from checkpoints, or keep dWaveOp in HBM")
     ap.add_argument("--cpu-sample", type=int, default=40)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain per-shot FP64 GPU path")
@@ -212,8 +217,7 @@ def main():
                                              shots_per_launch=args.shots_per_launch)
     solver.model_parameters = solver.ModelParameters(m, {"C": C})
     ts_obs = solver.ts()
-    fplan = WavePlan(solver, shots, checkpoint_every=solver.checkpoint_every,
-                     shots_per_launch=args.shots_per_launch)
+    fplan = WavePlan(solver, shots, shots_per_launch=args.shots_per_launch, forward_only=True)
     tuned = fplan.autotune()  # task length along x (untimed setup; later plans reuse it)
     obs_dev = fplan.forward().clone()
     # kernel roofline: the forward step kernel, graph of nsteps launches
@@ -246,8 +250,15 @@ def main():
     m0 = solver.ModelParameters(m, {"C": C0})
     solver.model_parameters = m0
     from pysit_gb300.autograd import resample_linear
+    solver.gradient_schedule = args.schedule
     plan = WavePlan(solver, shots, checkpoint_every=solver.checkpoint_every, shots_per_launch=args.shots_per_launch)
+    tuned_grad = plan.autotune()  # the gradient plan's own launch size (untimed setup)
     plan.dobs.copy_(resample_linear(obs_host.cuda(), ts_obs, solver.ts()))
+    config["gradient_schedule"] = plan.gradient_schedule
+    config["shots_per_launch"] = plan.shots_per_launch
+    if plan.gradient_schedule == "store":
+        config["workload"] = config["workload"].replace(", checkpoints every 64", "")
+        config.pop("checkpoint_every", None)
     for _ in range(args.warmup):
         plan.gradient()
     torch.cuda.synchronize()
@@ -333,7 +344,8 @@ def main():
                          "forward_graph": {"launch_ms": fwd_launch_ms, "achieved_gbs": achieved,
                                            "gcell_per_s": fwd_gcells}},
             "gpu_launches": launches, "misfit_rnorm2": rn, "clocks": clocks,
-            "autotune": {"tile_x": tuned["chosen"], "ms": {str(k): v for k, v in tuned["ms"].items()}}}
+            "autotune": {"tile_x": tuned_grad["chosen"], "ms": {str(k): v for k, v in tuned_grad["ms"].items()},
+                         "forward_plan_tile_x": tuned["chosen"]}}
     if rank == 0 and not args.no_plain:
         plain = plain_fp64_baseline(scale=args.scale, nsteps_full=args.nsteps)
         plain["batched_over_plain"] = line["value"] / world / plain["value"]

@@ -152,6 +152,13 @@ typedef struct {
     const int32_t* shot_nsteps;    /* host [nshots] or NULL: the record length of each shot in steps
                                       (1..nsteps); the residual of a shot is zero from its length on, so
                                       its misfit and gradient are those of a run of that many steps */
+    int store_dwaveop;             /* 0 = checkpointed gradient (forward, recompute, adjoint sweeps);
+                                      1 = the forward sweep keeps dWaveOp of every imaged step in the
+                                      workspace and the adjoint reads it back (no checkpoints, no
+                                      recompute; about ceil(nsteps / imaging_period) fields per shot of
+                                      a launch).  Same results; needs imaging_period 1 for the Hessian */
+    int forward_only;              /* 1 = only forward modelling (pysit_plan_forward): no adjoint,
+                                      checkpoint or imaging buffers; other runs return PYSIT_EINVAL */
 } pysit_plan_desc;
 
 int pysit_plan_create(const pysit_plan_desc* desc, pysit_plan** out);

@@ -55,6 +55,8 @@ class PlanDesc(C.Structure):
         ("psi_consistent", _i),
         ("tile_x", _i),
         ("shot_nsteps", C.POINTER(C.c_int32)),
+        ("store_dwaveop", _i),
+        ("forward_only", _i),
     ]
 
 

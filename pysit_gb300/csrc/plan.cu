@@ -301,6 +301,9 @@ template <typename T>
 struct PlanT final : public pysit_plan {
     // ---- description -------------------------------------------------------
     int dim, order, R, nx, ny, nz, nsteps, p_img, S, G, nshots, nsrc, nrec, use_graph, psi_consistent;
+    int store_all = 0;           // the forward sweep keeps every imaged dWaveOp (no checkpoints, no recompute)
+    int fwd_only = 0;            // forward modelling only: no adjoint, imaging or checkpoint buffers
+    int nslots = 1;              // replay slots: S (checkpointed) or ceil(nsteps / p_img) (kept)
     int tile_req = 0;            // requested task length along x (0: default)
     std::vector<int> shot_steps; // record length of each shot in steps (empty: all nsteps)
     size_t task_cap = 0;         // ints the task buffer holds (enough for the shortest x-chunk)
@@ -389,6 +392,8 @@ struct PlanT final : public pysit_plan {
         nshots = d.nshots; G = std::min(d.shots_per_launch, d.nshots); nsrc = d.nsrc; nrec = d.nrec;
         use_graph = d.use_graph;
         psi_consistent = d.psi_consistent ? 1 : 0;
+        store_all = d.store_dwaveop ? 1 : 0;
+        fwd_only = d.forward_only ? 1 : 0;
         tile_req = d.tile_x > 0 ? d.tile_x : 0;
         shot_steps.clear();
         if (d.shot_nsteps) {
@@ -425,6 +430,7 @@ struct PlanT final : public pysit_plan {
         fstride = (fstride + 63) / 64 * 64;
         field_bytes = (size_t)fstride * G * sizeof(T);
         nseg = (nsteps + S - 1) / S;
+        nslots = store_all ? (nsteps + p_img - 1) / p_img : S;
         ckpt_fields = dim == 1 ? 3 : dim == 2 ? 4 : 6;
         choose_tiling();
         // acquisition
@@ -675,20 +681,23 @@ struct PlanT final : public pysit_plan {
         off.c2 = take(one);
         off.sgx = take(nx * sizeof(T)); off.sgy = take(ny * sizeof(T)); off.sgz = take(nz * sizeof(T));
         off.mgx = take(nx * sizeof(T)); off.mgy = take(ny * sizeof(T)); off.mgz = take(nz * sizeof(T));
+        // a forward-only plan aliases the adjoint state onto the forward one and keeps
+        // no imaging, replay or checkpoint storage
+        const size_t adj_bytes = fwd_only ? 0 : field_bytes;
         for (int b = 0; b < 2; ++b) {
-            off.U[b] = take(field_bytes); off.A[b] = take(field_bytes);
-            off.PZ[b] = take(field_bytes); off.AZ[b] = take(field_bytes);
+            off.U[b] = take(field_bytes); off.A[b] = fwd_only ? off.U[b] : take(adj_bytes);
+            off.PZ[b] = take(field_bytes); off.AZ[b] = fwd_only ? off.PZ[b] : take(adj_bytes);
             off.PX[b] = dim >= 2 ? take(field_bytes) : off.PZ[b];
-            off.AX[b] = dim >= 2 ? take(field_bytes) : off.AZ[b];
+            off.AX[b] = fwd_only ? off.PX[b] : dim >= 2 ? take(adj_bytes) : off.AZ[b];
             off.PY[b] = dim == 3 ? take(field_bytes) : off.PZ[b];
-            off.AY[b] = dim == 3 ? take(field_bytes) : off.AZ[b];
+            off.AY[b] = fwd_only ? off.PY[b] : dim == 3 ? take(adj_bytes) : off.AZ[b];
             off.PS[b] = dim == 3 ? take(field_bytes) : off.PZ[b];
-            off.AS[b] = dim == 3 ? take(field_bytes) : off.AZ[b];
+            off.AS[b] = fwd_only ? off.PS[b] : dim == 3 ? take(adj_bytes) : off.AZ[b];
         }
-        off.ic = take(field_bytes);
-        off.m1 = take(one);
-        off.replay = take(field_bytes * (size_t)S);
-        off.ckpt = take(field_bytes * (size_t)ckpt_fields * nseg);
+        off.ic = take(adj_bytes);
+        off.m1 = take(fwd_only ? 0 : one);
+        off.replay = take(fwd_only ? 0 : field_bytes * (size_t)nslots);
+        off.ckpt = take(fwd_only || store_all ? 0 : field_bytes * (size_t)ckpt_fields * nseg);
         off.traces = take((size_t)G * nsteps * nrec * sizeof(T));
         off.srcamp = take((size_t)nshots * nsteps * nsrc * sizeof(T));
         auto take_inj = [&](std::vector<CSRBox>& v, size_t& box, size_t& rpb, size_t& row, size_t& pt,
@@ -879,7 +888,7 @@ struct PlanT final : public pysit_plan {
         // the adjoint source covers every receiver: added by a scatter kernel after the step
         const bool scatter = MODE == kAdj && q.inj.on && rec_box_max > 0;
         if (scatter) q.inj.on = 0;
-        const bool rec = MODE == kFwd && q.rec.blocks > 0;
+        const bool rec = MODE != kAdj && q.rec.blocks > 0;
         const int recb = q.rec.blocks;
         q.rec.blocks = 0;
         const bool fork = ntask2d[1] > 0 && ntask2d[0] > 0;
@@ -921,7 +930,7 @@ struct PlanT final : public pysit_plan {
         WaveParams<T> q = p;
         const bool scatter = MODE == kAdj && q.inj.on && rec_box_max > 0;
         if (scatter) q.inj.on = 0;
-        const bool rec = MODE == kFwd && q.rec.blocks > 0;
+        const bool rec = MODE != kAdj && q.rec.blocks > 0;
         const bool fork = ntask3d[0] > 0 && (ntask3d[1] > 0 || rec);
         cudaStream_t side = fork ? aux : s;
         if (fork) {
@@ -1031,17 +1040,31 @@ struct PlanT final : public pysit_plan {
             if (dst[f] && src[f]) cudaMemcpyAsync(dst[f], src[f], field_bytes, cudaMemcpyDeviceToDevice, s);
     }
 
+    T* replay_slot(long long i) const { return fld(off.replay) + (size_t)i * fstride * G; }
+
     T* ckpt_slot(int seg, int f) const {
         return reinterpret_cast<T*>(ws + off.ckpt + ((size_t)seg * ckpt_fields + f) * field_bytes);
     }
 
-    // forward sweep of one group; optional checkpoints
+    // forward sweep of one group; with `checkpoints` (a gradient follows) it saves the
+    // checkpoints, or with store_all writes dWaveOp of every imaged step instead
     void forward_sweep(int g0, int gn, bool checkpoints, cudaStream_t s) {
         zero_state(off.U, off.PX, off.PY, off.PZ, off.PS, s);
         State st = make_state(off.U, off.PX, off.PY, off.PZ, off.PS);
         WaveParams<T> p = base_params(g0, gn);
         T* tr = at<T>(off.traces);
+        const bool keep = checkpoints && store_all;
         for (int k = 0; k < nsteps; ++k) {
+            if (keep) {
+                bind_state(p, st);
+                set_inject(p, true, g0, k, nullptr);
+                set_recording(p, g0, gn, tr + (long long)k * nrec);
+                p.dw_out = (k % p_img == 0) ? replay_slot(k / p_img) : nullptr;
+                p.nan_check = 1;
+                launch(p, kRecomp, s);
+                advance(st);
+                continue;
+            }
             if (checkpoints && k % S == 0) {
                 T* src[6]; T* dst[6];
                 ckpt_ptrs(st, src);
@@ -1062,6 +1085,19 @@ struct PlanT final : public pysit_plan {
         cudaMemsetAsync(ws + off.ic, 0, field_bytes, s);
         State adj = make_state(off.A, off.AX, off.AY, off.AZ, off.AS);
         const T* resid = at<T>(off.traces);
+        if (store_all) {  // dWaveOp of every imaged step is in the replay buffer already
+            WaveParams<T> q = base_params(g0, gn);
+            for (int k = nsteps - 1; k >= 0; --k) {
+                bind_state(q, adj);
+                set_inject(q, false, g0, k, resid);
+                q.image = (k % period == 0);
+                q.dw_in = replay_slot(k / period);
+                q.ic = fld(off.ic);
+                launch(q, kAdj, s);
+                advance(adj);
+            }
+            return;
+        }
         for (int seg = nseg - 1; seg >= 0; --seg) {
             const int k0 = seg * S, k1 = std::min(k0 + S, nsteps) - 1;
             // restore the forward state at k0 into buffer set 0
@@ -1105,11 +1141,12 @@ struct PlanT final : public pysit_plan {
         State u1 = make_state(off.A, off.AX, off.AY, off.AZ, off.AS);
         WaveParams<T> p0 = base_params(g0, gn), p1 = base_params(g0, gn);
         T* tr = at<T>(off.traces);
-        T* dw = fld(off.replay);
         const long long rows = (long long)gn * nx * ny;
         const int nb = (int)std::min<long long>(rows, 152LL * 16);
         for (int k = 0; k < nsteps; ++k) {
-            if (checkpoints && k % S == 0) {
+            // kept schedule: dWaveOp0 of every step stays for the migration (imaging every step)
+            T* dw = checkpoints && store_all ? replay_slot(k) : replay_slot(0);
+            if (checkpoints && !store_all && k % S == 0) {
                 T* src[6]; T* dst[6];
                 ckpt_ptrs(u0, src);
                 for (int f = 0; f < ckpt_fields; ++f) dst[f] = ckpt_slot(k / S, f);
@@ -1188,6 +1225,7 @@ struct PlanT final : public pysit_plan {
 
     int born(const double* m1, void* traces, cudaStream_t s) override {
         PGB_REQUIRE(ws, "no workspace bound");
+        PGB_REQUIRE(!fwd_only, "the plan was built for forward modelling only");
         PGB_REQUIRE(model_set, "pysit_plan_set_model must be called first");
         PGB_REQUIRE(m1, "NULL model perturbation");
         PGB_REQUIRE(traces || nrec == 0, "NULL traces output");
@@ -1196,6 +1234,8 @@ struct PlanT final : public pysit_plan {
 
     int hessian(const double* m1, double* out, double* d1norm2, cudaStream_t s) override {
         PGB_REQUIRE(ws, "no workspace bound");
+        PGB_REQUIRE(!fwd_only, "the plan was built for forward modelling only");
+        PGB_REQUIRE(!store_all || p_img == 1, "a plan that keeps dWaveOp applies the Hessian with imaging_period 1 only");
         PGB_REQUIRE(model_set, "pysit_plan_set_model must be called first");
         PGB_REQUIRE(m1 && out, "NULL argument");
         return run(5, m1, out, d1norm2, nullptr, s,
@@ -1214,6 +1254,7 @@ struct PlanT final : public pysit_plan {
         PGB_REQUIRE(ws, "no workspace bound");
         PGB_REQUIRE(model_set, "pysit_plan_set_model must be called first");
         PGB_REQUIRE(mode >= kFwd && mode <= kAdj, "mode must be 0 (forward), 1 (recompute) or 2 (adjoint)");
+        PGB_REQUIRE(!fwd_only || mode == kFwd, "the plan was built for forward modelling only");
         PGB_REQUIRE(n >= 0, "nsteps must be >= 0");
         launches = 0;
         reset_task_counter(s);
@@ -1227,11 +1268,11 @@ struct PlanT final : public pysit_plan {
             if (mode == kAdj) {
                 set_inject(p, false, 0, k, at<T>(off.traces));
                 p.image = 1;
-                p.dw_in = fld(off.replay) + (size_t)(k % S) * fstride * G;
+                p.dw_in = replay_slot(k % nslots);
                 p.ic = fld(off.ic);
             } else {
                 set_inject(p, true, 0, k, nullptr);
-                if (mode == kRecomp) p.dw_out = fld(off.replay) + (size_t)(k % S) * fstride * G;
+                if (mode == kRecomp) p.dw_out = replay_slot(k % nslots);
                 else set_recording(p, 0, gn, at<T>(off.traces) + (long long)k * nrec);
             }
             launch(p, mode, s);
@@ -1261,7 +1302,7 @@ struct PlanT final : public pysit_plan {
             if ((rc = use_tile(cand[c], s))) break;
             if ((rc = step_loop(kFwd, 2, s))) break;  // warm-up
             cudaEventRecord(e0, s);
-            if ((rc = step_loop(kFwd, n, s)) || (rc = step_loop(kAdj, n, s))) break;
+            if ((rc = step_loop(kFwd, n, s)) || (!fwd_only && (rc = step_loop(kAdj, n, s)))) break;
             cudaEventRecord(e1, s);
             if (cudaEventSynchronize(e1) != cudaSuccess) { rc = cuda_status(cudaGetLastError(), "autotune"); break; }
             float ms = 0.f;
@@ -1401,6 +1442,7 @@ struct PlanT final : public pysit_plan {
         PGB_REQUIRE(model_set, "pysit_plan_set_model must be called first");
         PGB_REQUIRE(dobs || nrec == 0, "NULL observed data");
         PGB_REQUIRE(rnorm2, "NULL misfit output");
+        PGB_REQUIRE(!fwd_only || !with_grad, "the plan was built for forward modelling only");
         PGB_REQUIRE(!with_grad || grad, "NULL gradient output");
         return run(migrate ? 3 : with_grad ? 1 : 2, dobs, grad, rnorm2, traces, s, [&](cudaStream_t st) {
             enqueue_gradient(dobs, grad, rnorm2, traces, with_grad, migrate, st);
@@ -1411,6 +1453,7 @@ struct PlanT final : public pysit_plan {
         PGB_REQUIRE(ws, "no workspace bound");
         PGB_REQUIRE(model_set, "pysit_plan_set_model must be called first");
         PGB_REQUIRE((dobs || nrec == 0) && grad && rnorm2, "NULL argument");
+        PGB_REQUIRE(!fwd_only, "the plan was built for forward modelling only");
         launches = 0;
         enqueue_gradient(dobs, grad, rnorm2, nullptr, true, false, s);
         last_launches = launches;

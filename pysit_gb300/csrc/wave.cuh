@@ -138,6 +138,7 @@ struct WaveParams {
     int image;               // kAdj: accumulate this step
     int* err;                // device error word (PGB_ERR_* bits), may be NULL
     int psi_c2;              // 3D: 1 = C^2 multiplies sigma_x sigma_y sigma_z psi (the reference), 0 = not
+    int nan_check;           // kRecomp: flag non-finite u_{k+1} as kFwd does (a forward sweep that keeps dWaveOp)
     // 2D persistent sweep: task counters (interior, PML shell) shared by the
     // launches of one run; this launch's tasks of kind 0 are the counter values
     // task_base .. task_base + tasks - 1 of task_ctr[0], those of kind 1 start at

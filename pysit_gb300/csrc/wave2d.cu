@@ -70,7 +70,7 @@ __global__ void __launch_bounds__(kNT, 2) wave2d_kernel(const WaveParams<T> p) {
     const int ntiles = p.ntz * p.ntx;
     const int b = blockIdx.x;
     if (b >= ntiles * p.nshot) {
-        if (MODE == kFwd) record_block(p, b - ntiles * p.nshot);
+        if (MODE != kAdj) record_block(p, b - ntiles * p.nshot);
         return;
     }
     const int shot = b / ntiles;
@@ -322,7 +322,7 @@ __global__ void __launch_bounds__(kNT, 2) wave2d_kernel(const WaveParams<T> p) {
             }
         }
 
-        if (MODE == kFwd) {
+        if (MODE == kFwd || (MODE == kRecomp && p.nan_check)) {
 #pragma unroll
             for (int v = 0; v < V; ++v) bad |= !isfinite(un.v[v]);
         }
@@ -346,7 +346,7 @@ __global__ void __launch_bounds__(kNT, 2) wave2d_kernel(const WaveParams<T> p) {
             issue(i + kD);
         }
     }
-    if (MODE == kFwd && bad && p.err) atomicOr(p.err, PGB_ERR_NONFINITE);
+    if (MODE != kAdj && bad && p.err) atomicOr(p.err, PGB_ERR_NONFINITE);
 }
 
 }  // namespace
@@ -355,7 +355,7 @@ template <typename T, int R, int MODE>
 void launch_wave2d(const WaveParams<T>& p, int bz, cudaStream_t s) {
     (void)bz;
     const int ntiles = p.ntz * p.ntx;
-    int grid = ntiles * p.nshot + (MODE == kFwd ? p.rec.blocks : 0);
+    int grid = ntiles * p.nshot + (MODE != kAdj ? p.rec.blocks : 0);
     wave2d_kernel<T, R, MODE><<<grid, kNT, Smem2<T, R>::bytes, s>>>(p);
 }
 

@@ -416,7 +416,7 @@ __device__ __forceinline__ void sweep(const WaveParams<T>& p, unsigned char* wsm
                     ico.v[v0 + 1] = ic.y;
                 }
             }
-            if (MODE == kFwd) {  // a NaN or Inf anywhere in the lane's cells survives the sum
+            if (MODE == kFwd || (MODE == kRecomp && p.nan_check)) {  // a NaN or Inf anywhere in the lane's cells survives the sum
                 T sum = T(0);
 #pragma unroll
                 for (int v = 0; v < V; ++v) sum += un.v[v];
@@ -502,7 +502,7 @@ __global__ void __launch_bounds__(kWarps * 32, (MinBlocks<T, KIND>::value))
         for (int j = 0; j < A; ++j) mbar_wait_bounded(&bar[j], j < pp.s ? pp.ph : (pp.ph ^ 1u), kPolls);
     }
     if (p.err) {
-        if (MODE == kFwd && bad) atomicOr(p.err, PGB_ERR_NONFINITE);
+        if (MODE != kAdj && bad) atomicOr(p.err, PGB_ERR_NONFINITE);
         if (late && lane == 0) atomicOr(p.err, PGB_ERR_TIMEOUT);
     }
 }

@@ -126,7 +126,8 @@ __device__ __forceinline__ void cell3d(const WaveParams<T>& p, const int shot, c
         __stcs(p.dw_out + sh + o, ok ? d : T(0));
     }
     if (MODE == kAdj && p.image) p.ic[sh + o] += uc * __ldcs(p.dw_in + sh + o);
-    if (MODE == kFwd && p.err && !isfinite(unew)) atomicOr(p.err, PGB_ERR_NONFINITE);
+    if ((MODE == kFwd || (MODE == kRecomp && p.nan_check)) && p.err && !isfinite(unew))
+        atomicOr(p.err, PGB_ERR_NONFINITE);
 }
 
 // ---- task sweeps ---------------------------------------------------------------
@@ -341,14 +342,14 @@ __global__ void __launch_bounds__(kW3 * 32, (sizeof(T) == 4 ? PGB_3D_INT_MINB : 
         *reinterpret_cast<VT*>(p.u_prev + sh + o) = *reinterpret_cast<const VT*>(un);
         if (MODE == kRecomp && p.dw_out) __stcs(reinterpret_cast<VT*>(p.dw_out + sh + o), *reinterpret_cast<const VT*>(dwo));
         if (MODE == kAdj && p.image) *reinterpret_cast<VT*>(p.ic + sh + o) = *reinterpret_cast<const VT*>(ico);
-        if (MODE == kFwd) {
+        if (MODE == kFwd || (MODE == kRecomp && p.nan_check)) {
             T sum = T(0);
 #pragma unroll
             for (int v = 0; v < V; ++v) sum += un[v];
             bad |= !isfinite(sum);
         }
     }
-    if (MODE == kFwd && bad && p.err) atomicOr(p.err, PGB_ERR_NONFINITE);
+    if (MODE != kAdj && bad && p.err) atomicOr(p.err, PGB_ERR_NONFINITE);
 }
 
 // 1D: one axis (z), Phi_z only (_1D.h:117-129).
@@ -356,7 +357,7 @@ template <typename T, int R, int MODE>
 __global__ void __launch_bounds__(256) wave1d_kernel(const WaveParams<T> p, int ntile) {
     const int b = blockIdx.x;
     if (b >= ntile * p.nshot) {
-        if (MODE == kFwd) record3(p, (long long)(b - ntile * p.nshot) * blockDim.x + threadIdx.x);
+        if (MODE != kAdj) record3(p, (long long)(b - ntile * p.nshot) * blockDim.x + threadIdx.x);
         return;
     }
     const int shot = b / ntile;
@@ -415,7 +416,7 @@ void launch_wave1d(const WaveParams<T>& p, int bz, cudaStream_t s) {
     const int tb = 128;
     int ntile = ceil_div(p.nz, tb);
     int grid = ntile * p.nshot;
-    if (MODE == kFwd && p.rec.nrec > 0) grid += ceil_div((long long)p.nshot * p.rec.nrec, tb);
+    if (MODE != kAdj && p.rec.nrec > 0 && p.rec.traces) grid += ceil_div((long long)p.nshot * p.rec.nrec, tb);
     wave1d_kernel<T, R, MODE><<<grid, tb, 0, s>>>(p, ntile);
 }
 

@@ -51,10 +51,17 @@ class WavePlan:
     """Device plan of one (solver configuration, shot list)."""
 
     def __init__(self, solver, shots, imaging_period=1, checkpoint_every=None, shots_per_launch=None,
-                 use_graph=None, record_steps=None):
+                 use_graph=None, record_steps=None, gradient_schedule=None, forward_only=False):
         """``record_steps``: optional record length of each shot in time steps (<= solver.nsteps);
         a shorter shot's residual is zero from its length on, so its misfit and gradient are those
-        of a run of that length (the shots of one plan still step together)."""
+        of a run of that length (the shots of one plan still step together).
+
+        ``gradient_schedule`` ('checkpoint' | 'store' | 'auto', default the solver's): how a
+        gradient recovers dWaveOp of the forward field - recomputed from checkpoints, or kept
+        from the forward sweep in HBM (no recompute sweep; about ceil(nsteps / imaging_period)
+        fields per shot of a launch).  'auto' keeps them when the launch fits in free device
+        memory, taking as many shots per launch as fit unless shots_per_launch is fixed.
+        ``forward_only`` plans model data only (no adjoint, imaging or checkpoint storage)."""
         torch = _native.require_cuda()
         lib = _native.load()
         self.solver = solver
@@ -70,9 +77,17 @@ class WavePlan:
         if checkpoint_every is None:
             checkpoint_every = solver.checkpoint_every or default_checkpoint_every(self.nsteps, self.dim)
         self.checkpoint_every = int(min(max(1, checkpoint_every), self.nsteps))
+        fixed_launch = shots_per_launch is not None or bool(solver.shots_per_launch)
         if shots_per_launch is None:
             shots_per_launch = solver.shots_per_launch or self.nshots
         self.shots_per_launch = int(max(1, min(shots_per_launch, self.nshots)))
+        self.forward_only = bool(forward_only)
+        if gradient_schedule is None:
+            gradient_schedule = getattr(solver, "gradient_schedule", "checkpoint")
+        if gradient_schedule not in ("checkpoint", "store", "auto"):
+            raise ValueError("gradient_schedule must be 'checkpoint', 'store' or 'auto'")
+        if self.forward_only:
+            gradient_schedule = "checkpoint"
         use_graph = solver.use_graph if use_graph is None else use_graph
 
         d = _native.PlanDesc()
@@ -157,6 +172,12 @@ class WavePlan:
             setattr(d, k, v.ctypes.data_as(C.POINTER(ctype[v.dtype.type])))
         d.nsrc = nsrc
         d.nrec = nrec
+        d.forward_only = 1 if self.forward_only else 0
+        if gradient_schedule == "auto":
+            gradient_schedule = self._choose_schedule(lib, d, fixed_launch, nrec)
+        d.store_dwaveop = 1 if gradient_schedule == "store" else 0
+        d.shots_per_launch = self.shots_per_launch
+        self.gradient_schedule = gradient_schedule
 
         h = C.c_void_p()
         _native.check(lib.pysit_plan_create(C.byref(d), C.byref(h)))
@@ -185,6 +206,43 @@ class WavePlan:
             except Exception:
                 pass
             self._h = None
+
+    @staticmethod
+    def _workspace_for(lib, d, shots_per_launch, store):
+        d.shots_per_launch = int(shots_per_launch)
+        d.store_dwaveop = 1 if store else 0
+        h = C.c_void_p()
+        _native.check(lib.pysit_plan_create(C.byref(d), C.byref(h)))
+        n = C.c_uint64()
+        try:
+            _native.check(lib.pysit_plan_workspace_bytes(h, C.byref(n)))
+        finally:
+            lib.pysit_plan_destroy(h)
+        return int(n.value)
+
+    def _choose_schedule(self, lib, d, fixed_launch, nrec):
+        """'store' with the largest balanced launch that fits in free device memory (at least
+        16 shots or all of them), else 'checkpoint'."""
+        torch = _native.require_cuda()
+        free = torch.cuda.mem_get_info()[0]
+        elem = 8 if self.tdtype == torch.float64 else 4
+        outputs = 2 * self.nshots * self.nsteps * nrec * elem  # traces + observed data of the plan
+        budget = free - outputs - max(2 << 30, int(0.03 * free))
+        G = self.shots_per_launch
+        if fixed_launch:
+            return "store" if self._workspace_for(lib, d, G, True) <= budget else "checkpoint"
+        b1 = self._workspace_for(lib, d, 1, True)
+        per = self._workspace_for(lib, d, 2, True) - b1
+        gmax = self.nshots if per <= 0 else int((budget - (b1 - per)) // per)
+        gmax = min(gmax, self.nshots)
+        if gmax < min(16, self.nshots):
+            return "checkpoint"
+        launches = -(-self.nshots // gmax)
+        G = -(-self.nshots // launches)
+        while G > 1 and self._workspace_for(lib, d, G, True) > budget:
+            G -= 1
+        self.shots_per_launch = G
+        return "store"
 
     # ---------------------------------------------------------------------------
     def set_model(self):
@@ -357,14 +415,18 @@ def plan_for(solver, shots, imaging_period=1, **kw):
     """Cached WavePlan of a solver for a shot list (rebuilt when dt/nsteps change)."""
     # a source-encoded supershot carries an encoding counter: a new encoding needs a new plan
     key = (tuple((id(s), getattr(s, "encoding", 0)) for s in shots), solver.dt, solver.nsteps, solver.precision,
-           solver.spatial_accuracy_order, getattr(solver, "pml_psi", "reference"), int(imaging_period),
-           tuple(sorted(kw.items())))
+           solver.spatial_accuracy_order, getattr(solver, "pml_psi", "reference"),
+           getattr(solver, "gradient_schedule", "checkpoint"), int(imaging_period), tuple(sorted(kw.items())))
     cache = solver._plans
     p = cache.get(key)
     if p is None:
         # keep at most a few plans alive (each owns a workspace)
         while len(cache) >= 2:
             cache.pop(next(iter(cache)))
+        if getattr(solver, "gradient_schedule", "checkpoint") != "checkpoint":
+            # a plan that keeps dWaveOp sizes itself to the free memory: release the others first
+            cache.clear()
+            _native.require_cuda().cuda.empty_cache()
         p = WavePlan(solver, shots, imaging_period=imaging_period, **kw)
         if getattr(solver, "autotune", False) and p._tune_key not in _TUNED:
             p.autotune()

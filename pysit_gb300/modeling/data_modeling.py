@@ -132,7 +132,7 @@ def generate_seismic_data(shots, solver, model, verbose=False, frequencies=None,
     else:
         solver.model_parameters = model
         ts = solver.ts()
-        plan = plan_for(solver, shots)
+        plan = plan_for(solver, shots, forward_only=True)
         traces = plan.forward().double().cpu().numpy()
         for i, shot in enumerate(shots):
             shot.reset_time_series(ts)

@@ -90,7 +90,7 @@ class TemporalModeling:
         if self.batched and rp <= {"simdata"}:
             retval = {}
             if "simdata" in rp:
-                plan = plan_for(solver, [shot], imaging_period)
+                plan = plan_for(solver, [shot], imaging_period, forward_only=True)
                 tr = plan.forward()
                 retval["simdata"] = tr[0, :, :shot.receivers.receiver_count].to(dtype=__import__("torch").float64) \
                     .cpu().numpy()

@@ -170,7 +170,7 @@ class _CDATimeScalarCuda:
 
     def __init__(self, mesh, spatial_accuracy_order=4, trange=(0.0, 1.0), cfl_safety=1 / 6,
                  precision="double", checkpoint_every=None, shots_per_launch=None, use_graph=True,
-                 pml_psi="reference", autotune=False, **kwargs):
+                 pml_psi="reference", autotune=False, gradient_schedule="checkpoint", **kwargs):
         if mesh.dim != self._dim:
             raise ValueError(f"{type(self).__name__} needs a {self._dim}D mesh")
         if spatial_accuracy_order not in (2, 4, 6, 8):
@@ -179,6 +179,8 @@ class _CDATimeScalarCuda:
             raise ValueError("precision must be 'single' or 'double'")
         if pml_psi not in ("reference", "consistent"):
             raise ValueError("pml_psi must be 'reference' or 'consistent'")
+        if gradient_schedule not in ("checkpoint", "store", "auto"):
+            raise ValueError("gradient_schedule must be 'checkpoint', 'store' or 'auto'")
         for i in range(mesh.dim):
             for bc in (mesh.parameters[i].lbc, mesh.parameters[i].rbc):
                 if bc.type == "pml" and getattr(bc.domain_bc, "compact", False):
@@ -202,6 +204,11 @@ class _CDATimeScalarCuda:
         self.pml_psi = pml_psi
         # choose the 2D/3D task length along x by timing when a batched plan is first built
         self.autotune = autotune
+        # batched gradients: 'checkpoint' (forward, recompute and adjoint sweeps over
+        # checkpoints), 'store' (the forward sweep keeps dWaveOp of every imaged step in
+        # HBM, no recompute), 'auto' (store when the shots of a launch fit in free device
+        # memory, with as many shots per launch as fit, else checkpoint)
+        self.gradient_schedule = gradient_schedule
         self._mp = None
         self._model_change_count = 0
         self._C_dev = None

@@ -57,7 +57,7 @@ def _steps_T(C0, deltas, cfl, nsteps):
 
 
 def cfg2(scale=1.0, nshots=64, nsteps=4000, order=8, precision="single", cfl=0.4, checkpoint_every=64,
-         shots_per_launch=None, seed=2026):
+         shots_per_launch=None, seed=2026, gradient_schedule="checkpoint"):
     """(mesh, shots, solver, C_true, C_start) of the 2D batched-gradient workload."""
     nx, nz = max(16, int(round(1152 * scale))), max(12, int(round(384 * scale)))
     npml = max(4, int(round(40 * scale)))
@@ -74,7 +74,8 @@ def cfg2(scale=1.0, nshots=64, nsteps=4000, order=8, precision="single", cfl=0.4
     solver = solvers.ConstantDensityAcousticWave(m, spatial_accuracy_order=order, trange=(0.0, T),
                                                  kernel_implementation="cuda", precision=precision,
                                                  cfl_safety=cfl, checkpoint_every=checkpoint_every,
-                                                 shots_per_launch=shots_per_launch, autotune=True)
+                                                 shots_per_launch=shots_per_launch, autotune=True,
+                                                 gradient_schedule=gradient_schedule)
     return m, shots, solver, C, C0
 
 
@@ -202,7 +203,7 @@ def run_uneven_batch(grids, repeats=2):
     plans = []
     for m, shots, solver, C, C0, record in grids:
         solver.model_parameters = solver.ModelParameters(m, {"C": C})
-        obs_plan = WavePlan(solver, shots)
+        obs_plan = WavePlan(solver, shots, forward_only=True)
         obs = obs_plan.forward().clone()
         ts_true = solver.ts()
         del obs_plan
@@ -253,7 +254,7 @@ def run_hessian(m, shots, solver, C, C0, repeats=2):
     from .engine import WavePlan
 
     solver.model_parameters = solver.ModelParameters(m, {"C": C})
-    obs = WavePlan(solver, shots).forward().clone()
+    obs = WavePlan(solver, shots, forward_only=True).forward().clone()
     ts_true = solver.ts()
     solver.model_parameters = solver.ModelParameters(m, {"C": C0})
     plan = WavePlan(solver, shots)

@@ -141,3 +141,23 @@ def test_plan_workspace_scales_with_checkpoint_interval(lib):
         lib.pysit_plan_destroy(h)
     # replay grows with S, checkpoints shrink with it: S=7 is the cheapest of the three
     assert sizes[1] < sizes[0] and sizes[1] < sizes[2]
+
+
+def test_workspace_of_the_schedules(lib):
+    """store_dwaveop keeps one field per imaged step instead of checkpoints + a replay of S
+    steps; forward_only drops every adjoint, imaging, replay and checkpoint buffer."""
+    sizes = {}
+    for name, store, fwd, period in (("ckpt", 0, 0, 1), ("store", 1, 0, 1), ("store_p2", 1, 0, 2),
+                                     ("fwd", 0, 1, 1)):
+        keep = []
+        d = _desc(keep=keep, nsteps=50)
+        d.store_dwaveop, d.forward_only, d.imaging_period = store, fwd, period
+        h = C.c_void_p()
+        _native.check(lib.pysit_plan_create(C.byref(d), C.byref(h)))
+        nb = C.c_uint64()
+        _native.check(lib.pysit_plan_workspace_bytes(h, C.byref(nb)))
+        sizes[name] = nb.value
+        lib.pysit_plan_destroy(h)
+    field = (30 + 8) * 32 * 4 * 2  # one FP32 field of the 2 shots (rows x pitch), lower bound
+    assert sizes["store"] - sizes["store_p2"] >= 24 * field  # 50 vs 25 kept steps
+    assert sizes["store"] > sizes["ckpt"] > sizes["fwd"]

@@ -1,0 +1,90 @@
+"""Gradient schedules on the GPU: 'store' (the forward sweep keeps dWaveOp of every imaged
+step in HBM, the adjoint reads it back) against 'checkpoint' (recomputed from checkpoints).
+Both run the same step kernels on the same values, so misfits, gradients, migrations and
+Hessian applications agree to the last bit; forward-only plans model the same traces."""
+import numpy as np
+import pytest
+
+import problems
+import pysit_gb300 as api
+from pysit_gb300 import _native
+from pysit_gb300.engine import WavePlan
+
+pytestmark = pytest.mark.gpu
+
+
+def _setup(name, precision="double", golden=None, **kw):
+    m, shots, solver, C, C0 = problems.build(api, name, precision=precision)
+    api.generate_seismic_data(shots, solver, solver.ModelParameters(m, {"C": C}))
+    solver.model_parameters = solver.ModelParameters(m, {"C": C0})
+    return m, shots, solver, C, C0
+
+
+def _grad(solver, shots, schedule, **kw):
+    plan = WavePlan(solver, shots, gradient_schedule=schedule, **kw)
+    plan.load_observed()
+    g, rn = plan.gradient(with_traces=True)
+    out = (g.cpu().numpy().copy(), float(rn.item()), plan.traces.cpu().numpy().copy(), plan.status())
+    assert plan.gradient_schedule == schedule
+    return out
+
+
+@pytest.mark.parametrize("precision", ["double", "single"])
+@pytest.mark.parametrize("name", ["o8", "1d", "3d", "dirichlet"])
+def test_store_schedule_equals_checkpoint_schedule(name, precision):
+    m, shots, solver, C, C0 = _setup(name, precision)
+    a = _grad(solver, shots, "checkpoint", checkpoint_every=5)
+    b = _grad(solver, shots, "store")
+    np.testing.assert_array_equal(b[0], a[0])
+    assert b[1] == a[1]
+    np.testing.assert_array_equal(b[2], a[2])
+    assert a[3] == 0 and b[3] == 0
+
+
+def test_store_schedule_with_imaging_period_groups_and_record_lengths():
+    m, shots, solver, C, C0 = _setup("o2")
+    kw = dict(imaging_period=3, shots_per_launch=1, record_steps=[solver.nsteps, solver.nsteps // 2])
+    a = _grad(solver, shots, "checkpoint", checkpoint_every=7, **kw)
+    b = _grad(solver, shots, "store", **kw)
+    np.testing.assert_array_equal(b[0], a[0])
+    assert b[1] == a[1]
+
+
+def test_store_schedule_hessian_and_migration():
+    import torch
+    m, shots, solver, C, C0 = _setup("o8")
+    rng = np.random.default_rng(1)
+    m1 = rng.standard_normal(m.dof()) * 1e-9
+    pa = WavePlan(solver, shots, gradient_schedule="checkpoint", checkpoint_every=6)
+    pb = WavePlan(solver, shots, gradient_schedule="store")
+    np.testing.assert_array_equal(pb.hessian(m1)[0].cpu().numpy(), pa.hessian(m1)[0].cpu().numpy())
+    d = torch.as_tensor(rng.standard_normal(tuple(pa.traces.shape)), device="cuda")
+    np.testing.assert_array_equal(pb.migrate(d).cpu().numpy(), pa.migrate(d).cpu().numpy())
+    np.testing.assert_array_equal(pb.born(m1).cpu().numpy(), pa.born(m1).cpu().numpy())
+
+
+def test_forward_only_plan():
+    m, shots, solver, C, C0 = _setup("o6")
+    full = WavePlan(solver, shots)
+    fwd = WavePlan(solver, shots, forward_only=True)
+    assert fwd.workspace_bytes < full.workspace_bytes
+    np.testing.assert_array_equal(fwd.forward().cpu().numpy(), full.forward().cpu().numpy())
+    fwd.load_observed()
+    full.load_observed()
+    assert float(fwd.misfit().item()) == float(full.misfit().item())
+    with pytest.raises(_native.PysitCudaError, match="forward modelling only"):
+        fwd.gradient()
+    with pytest.raises(_native.PysitCudaError, match="forward modelling only"):
+        fwd.step_loop(2, 1)
+
+
+def test_auto_schedule_keeps_dwaveop_when_it_fits():
+    m, shots, solver, C, C0 = _setup("o2")
+    plan = WavePlan(solver, shots, gradient_schedule="auto")
+    assert plan.gradient_schedule == "store" and plan.shots_per_launch == len(shots)
+    solver.gradient_schedule = "auto"
+    obj = api.TemporalLeastSquares(solver)
+    g = obj.compute_gradient(shots, solver.ModelParameters(m, {"C": C0}))
+    assert obj.last_plan.gradient_schedule == "store"
+    ref = _grad(solver, shots, "checkpoint")[0]
+    np.testing.assert_array_equal(np.ravel(g.data), ref)
