@@ -21,7 +21,8 @@ No public dataset is involved: each model is generated from a named seed.
 ``python -m pysit_gb300.workloads cfg5 [--iterations N] [--shots N] [--scale s]
 [--nsteps N] [--plain]`` runs the FWI and prints one JSON line (objective history,
 relative L2 error of the final model, wall time); ``... cfg4`` times the uneven
-batch, grid by grid and as one group; ``... hessian`` times the gradient, Born
+batch, grid by grid and as one group; ``... steps2d`` / ``steps3d`` time the three
+step kernels of the cfg2 / cfg3 grids alone; ``... hessian`` times the gradient, Born
 modelling and the Gauss-Newton Hessian application of the cfg2 workload; ``... gn``
 runs Gauss-Newton iterations (GMRES on the GPU Hessian) on the cfg5 model.
 """
@@ -35,7 +36,7 @@ from scipy.ndimage import gaussian_filter
 from . import core, solvers
 
 __all__ = ["layered_model", "cfg2", "cfg3", "cfg4", "cfg5", "run_lbfgs", "run_uneven_batch", "run_hessian",
-           "run_gauss_newton"]
+           "run_gauss_newton", "run_steps"]
 
 
 def layered_model(shape, nlayers, vmin, vmax, sigma_cells, amp, seed, clip=(1500.0, 5500.0)):
@@ -284,6 +285,46 @@ def run_hessian(m, shots, solver, C, C0, repeats=2):
     return out
 
 
+def run_steps(workload="cfg2", scale=1.0, nshots=None, nsteps=64, shots_per_launch=None, reps=32):
+    """Per-launch times of the three step kernels (forward, recompute, adjoint) of a workload's
+    first shot group, each timed alone with CUDA events (pysit_plan_step_loop), with the
+    algorithmic bytes of the step and Gcell/s (a benchmarking aid for profiling)."""
+    import torch
+
+    from .engine import WavePlan
+
+    if workload == "cfg2":
+        m, shots, solver, C, C0 = cfg2(scale=scale, nshots=nshots or 64, nsteps=nsteps)
+        pml_extra = (4, 4)  # Phi_x, Phi_z in and out
+    else:
+        m, shots, solver, C, C0 = cfg3(scale=scale, nshots=nshots or 1, nsteps=nsteps)
+        pml_extra = (8, 8)  # Phi_x, Phi_y, Phi_z, psi in and out
+    solver.model_parameters = solver.ModelParameters(m, {"C": C0})
+    plan = WavePlan(solver, shots, shots_per_launch=shots_per_launch or len(shots), gradient_schedule="checkpoint")
+    plan.forward()
+    torch.cuda.synchronize()
+    n_all = int(np.prod(m.shape(include_bc=True, as_grid=True)))
+    n_int = m.dof()
+    n_pml = n_all - n_int
+    w = 4 if solver.precision == "single" else 8
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    out = {"workload": workload, "scale": scale, "grid": [int(v) for v in m.shape(include_bc=True, as_grid=True)],
+           "shots_per_launch": plan.shots_per_launch, "modes": {}}
+    for mode, name, extra in ((0, "forward", 0), (1, "recompute", 1), (2, "adjoint", 3)):
+        plan.step_loop(mode, 4)
+        torch.cuda.synchronize()
+        e0.record()
+        plan.step_loop(mode, reps)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        nb = w * ((4 + extra) * n_int + (4 + pml_extra[0] + extra) * n_pml) * plan.shots_per_launch
+        out["modes"][name] = {"launch_ms": ms, "gbs": nb / (ms * 1e-3) / 1e9,
+                              "gcell_per_s": n_all * plan.shots_per_launch / (ms * 1e-3) / 1e9}
+    out["status"] = plan.status()
+    return out
+
+
 def run_gauss_newton(m, shots, solver, C, C0, iterations=3, krylov_maxiter=5, batched=True, verbose=False):
     """PySIT-style Gauss-Newton (GMRES inner solve on the batched GPU Hessian, backtracking line
     search with alpha0 = 1) from the smoothed start model; objective history, relative model
@@ -315,7 +356,8 @@ def _main(argv=None):
     import json
 
     ap = argparse.ArgumentParser(prog="python -m pysit_gb300.workloads")
-    ap.add_argument("workload", choices=["cfg4", "cfg5", "hessian", "gn"])
+    ap.add_argument("workload", choices=["cfg4", "cfg5", "hessian", "gn", "steps2d", "steps3d"])
+    ap.add_argument("--shots-per-launch", type=int, default=None)
     ap.add_argument("--krylov", type=int, default=5, help="gn: GMRES iterations per Gauss-Newton step")
     ap.add_argument("--iterations", type=int, default=20)
     ap.add_argument("--shots", type=int, default=None, help="default 256 (cfg4), 128 (cfg5)")
@@ -327,6 +369,11 @@ def _main(argv=None):
     if a.workload == "cfg4":
         out = run_uneven_batch(cfg4(scale=a.scale, nshots=a.shots or 256))
         out.update(workload="cfg4", scale=a.scale)
+        print(json.dumps(out))
+        return
+    if a.workload in ("steps2d", "steps3d"):
+        out = run_steps("cfg2" if a.workload == "steps2d" else "cfg3", scale=a.scale, nshots=a.shots,
+                        nsteps=a.nsteps, shots_per_launch=a.shots_per_launch)
         print(json.dumps(out))
         return
     if a.workload == "hessian":
