@@ -347,7 +347,7 @@ def main():
                                            "gcell_per_s": fwd_gcells}},
             "gpu_launches": launches, "misfit_rnorm2": rn, "clocks": clocks,
             "autotune": {"tile_x": tuned_grad["chosen"], "ms": {str(k): v for k, v in tuned_grad["ms"].items()},
-                         "forward_plan_tile_x": tuned["chosen"]}}
+                         "shell_share": tuned_grad.get("shell_share"), "forward_plan_tile_x": tuned["chosen"]}}
     if rank == 0 and not args.no_plain:
         plain = plain_fp64_baseline(scale=args.scale, nsteps_full=args.nsteps)
         plain["batched_over_plain"] = line["value"] / world / plain["value"]

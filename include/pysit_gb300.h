@@ -159,6 +159,11 @@ typedef struct {
                                       a launch).  Same results; needs imaging_period 1 for the Hessian */
     int forward_only;              /* 1 = only forward modelling (pysit_plan_forward): no adjoint,
                                       checkpoint or imaging buffers; other runs return PYSIT_EINVAL */
+    double shell_share[3];         /* 2D, per step mode (forward, recompute, adjoint): share of the GPU's
+                                      resident blocks given to the PML-shell kernel, in (0, 1), so that it
+                                      runs beside the interior kernel from the start; 0 = each kernel sized
+                                      for the whole GPU (the default: inside the CUDA graph of a sweep
+                                      that balanced the two kernels best in measurements) */
 } pysit_plan_desc;
 
 int pysit_plan_create(const pysit_plan_desc* desc, pysit_plan** out);
@@ -248,6 +253,9 @@ int pysit_plan_step_loop(pysit_plan* plan, int mode, int nsteps, void* stream);
  * wavefield buffers are left in an arbitrary state, as after step_loop. */
 int pysit_plan_autotune(pysit_plan* plan, const int* candidates, int ncand, int nsteps, int* chosen,
                         double* ms, void* stream);
+/* The plan's current tuning: task length along x and the three 2D shell block shares
+ * (pysit_plan_desc.shell_share).  Either output may be NULL. */
+int pysit_plan_get_tuning(const pysit_plan* plan, int* tile_x, double* shell_share);
 
 /* ------------------------------------------------------------------------
  * Plan groups, no counterpart in the reference (it runs shots one after the

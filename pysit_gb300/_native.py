@@ -57,6 +57,7 @@ class PlanDesc(C.Structure):
         ("shot_nsteps", C.POINTER(C.c_int32)),
         ("store_dwaveop", _i),
         ("forward_only", _i),
+        ("shell_share", _d * 3),
     ]
 
 
@@ -81,6 +82,7 @@ _PROTOS = {
     "pysit_plan_gradient": (_i, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "pysit_plan_misfit": (_i, [_vp, _vp, _vp, _vp, _vp]),
     "pysit_plan_migrate": (_i, [_vp, _vp, _vp, _vp, _vp]),
+    "pysit_plan_get_tuning": (_i, [_vp, C.POINTER(_i), C.POINTER(_d)]),
     "pysit_plan_born": (_i, [_vp, _vp, _vp, _vp]),
     "pysit_plan_hessian": (_i, [_vp, _vp, _vp, _vp, _vp]),
     "pysit_plan_status": (_i, [_vp, C.POINTER(_i), _vp]),

@@ -4,6 +4,10 @@
 parallel with nvcc (``-gencode arch=compute_103a,code=sm_103a``) and links the
 shared library in-tree (``pysit_gb300/libpysit_gb300.so``).  Object files go
 to ``pysit_gb300/_build/``.  Nothing is installed into site-packages.
+
+``PYSIT_CUDA_DEFINES`` (space-separated ``NAME=VALUE``) passes tuning macros of the
+kernels (e.g. ``PGB_SHELL_MINB=5``) as ``-D`` flags; a change of them rebuilds every
+object.
 """
 from __future__ import annotations
 
@@ -28,9 +32,13 @@ def _nvcc() -> str:
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build pysit_gb300")
 
 
+def _defines() -> list[str]:
+    return ["-D" + d for d in os.environ.get("PYSIT_CUDA_DEFINES", "").split() if d]
+
+
 def _flags(verbose_ptxas: bool = False) -> list[str]:
     f = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
-                "--expt-relaxed-constexpr", "-I", os.path.join(ROOT, "include")]
+                "--expt-relaxed-constexpr", "-I", os.path.join(ROOT, "include")] + _defines()
     if verbose_ptxas:
         f += ["-Xptxas", "-v"]
     return f
@@ -57,6 +65,15 @@ def _compile(src: str, verbose_ptxas: bool) -> tuple[str, str]:
 def build(verbose_ptxas: bool = False, jobs: int | None = None) -> str:
     """Compile and link the CUDA library; returns its path."""
     os.makedirs(OBJ, exist_ok=True)
+    stamp = os.path.join(OBJ, "defines.txt")
+    want = " ".join(_defines())
+    have = open(stamp).read() if os.path.exists(stamp) else ""
+    if want != have:  # other macros: every object is stale
+        for f in os.listdir(OBJ):
+            if f.endswith(".o"):
+                os.remove(os.path.join(OBJ, f))
+        with open(stamp, "w") as fh:
+            fh.write(want)
     srcs = sources()
     jobs = jobs or min(len(srcs), os.cpu_count() or 4)
     logs = []

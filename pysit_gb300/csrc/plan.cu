@@ -286,6 +286,7 @@ struct pysit_plan {
     virtual int status(int* flags, cudaStream_t s) = 0;
     virtual int step_loop(int mode, int nsteps, cudaStream_t s) = 0;
     virtual int autotune(const int* cand, int ncand, int nsteps, int* chosen, double* ms, cudaStream_t s) = 0;
+    virtual int tuning(int* tile, double* share) const = 0;
     // enqueue misfit + gradient on s without graph handling (for a group's capture)
     virtual int enqueue_grad_raw(const void* dobs, double* grad, double* rnorm2, cudaStream_t s) = 0;
     // linearised modelling / Gauss-Newton Hessian application for a model perturbation
@@ -323,6 +324,9 @@ struct PlanT final : public pysit_plan {
     int ntask3d[2] = {0, 0};
     int blocks2d[3][2] = {{1, 1}, {1, 1}, {1, 1}};  // resident task blocks per mode and kind (whole GPU)
     unsigned long long ctr_next[2] = {0, 0};  // task-counter values the next 2D launch starts at
+    double shell_frac[3] = {0.0, 0.0, 0.0};  // 2D, per mode: share of the resident blocks given to the
+                                 // PML-shell kernel (0: each kernel is sized for the whole GPU and they
+                                 // overlap only where one runs out)
     cudaStream_t aux = nullptr;  // second stream of the 2D step (shell kernel beside the interior one)
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     // ---- acquisition (host) ----------------------------------------------------
@@ -395,6 +399,8 @@ struct PlanT final : public pysit_plan {
         store_all = d.store_dwaveop ? 1 : 0;
         fwd_only = d.forward_only ? 1 : 0;
         tile_req = d.tile_x > 0 ? d.tile_x : 0;
+        for (int m = 0; m < 3; ++m)
+            shell_frac[m] = d.shell_share[m] > 0 && d.shell_share[m] < 1 ? d.shell_share[m] : 0.0;
         shot_steps.clear();
         if (d.shot_nsteps) {
             for (int s2 = 0; s2 < d.nshots; ++s2) {
@@ -457,6 +463,8 @@ struct PlanT final : public pysit_plan {
         bool have = e && sscanf(e, "%d,%d", &ebz, &etx) == 2 && ebz >= 32 && ebz <= 256 && ebz % 32 == 0 &&
                     etx >= 1;
         if (dim == 2) {
+            const char* f = getenv("PYSIT_CUDA_SHELL_FRAC");  // tuning: block share of the shell kernel
+            if (f) shell_frac[0] = shell_frac[1] = shell_frac[2] = std::min(0.95, std::max(0.0, atof(f)));
             const char* k = getenv("PYSIT_CUDA_2D");  // "tma" selects the bulk-copy pipeline
             warp2d = !(k && strcmp(k, "tma") == 0);
             if (warp2d) {
@@ -881,9 +889,15 @@ struct PlanT final : public pysit_plan {
         q.task_base = ctr_next[0];
         q.task_base2 = ctr_next[1];
         int nb[2];
+        // with a shell share the two kernels split the resident block slots (they run side by
+        // side from the start); otherwise each is sized for the whole GPU
+        const double fr = shell_frac[MODE];
+        const int cap1 = fr > 0 ? std::max(1, (int)(fr * blocks2d[MODE][1] + 0.5)) : blocks2d[MODE][1];
+        const int cap0 = fr > 0 ? std::max(1, blocks2d[MODE][0] - (int)(fr * blocks2d[MODE][0] + 0.5))
+                                : blocks2d[MODE][0];
         for (int k = 0; k < 2; ++k) {
             const long long need = ((long long)ntask2d[k] * p.nshot + wpb - 1) / wpb;
-            nb[k] = (int)std::min<long long>(need, blocks2d[MODE][k]);
+            nb[k] = (int)std::min<long long>(need, k ? cap1 : cap0);
         }
         // the adjoint source covers every receiver: added by a scatter kernel after the step
         const bool scatter = MODE == kAdj && q.inj.on && rec_box_max > 0;
@@ -1273,7 +1287,8 @@ struct PlanT final : public pysit_plan {
             } else {
                 set_inject(p, true, 0, k, nullptr);
                 if (mode == kRecomp) p.dw_out = replay_slot(k % nslots);
-                else set_recording(p, 0, gn, at<T>(off.traces) + (long long)k * nrec);
+                // the forward sweep records traces (the kept schedule's runs in recompute mode)
+                if (mode == kFwd || store_all) set_recording(p, 0, gn, at<T>(off.traces) + (long long)k * nrec);
             }
             launch(p, mode, s);
             advance(st);
@@ -1310,11 +1325,18 @@ struct PlanT final : public pysit_plan {
             if (ms_out) ms_out[c] = ms;
             if (ms < best_ms) { best_ms = ms; best = cand[c]; }
         }
+        if (rc == PYSIT_OK) rc = use_tile(best, s);
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         if (rc) return rc;
-        if ((rc = use_tile(best, s))) return rc;
         *chosen = best;
+        return PYSIT_OK;
+    }
+
+    int tuning(int* tile, double* share) const override {
+        if (tile) *tile = tx;
+        if (share)
+            for (int m = 0; m < 3; ++m) share[m] = shell_frac[m];
         return PYSIT_OK;
     }
 
@@ -1571,6 +1593,11 @@ extern "C" int pysit_plan_last_launch_count(const pysit_plan* p, int64_t* n) {
 extern "C" int pysit_plan_step_loop(pysit_plan* p, int mode, int nsteps, void* stream) {
     PGB_REQUIRE(p, "NULL plan");
     return p->step_loop(mode, nsteps, (cudaStream_t)stream);
+}
+
+extern "C" int pysit_plan_get_tuning(const pysit_plan* p, int* tile_x, double* shell_share) {
+    PGB_REQUIRE(p, "NULL plan");
+    return p->tuning(tile_x, shell_share);
 }
 
 extern "C" int pysit_plan_autotune(pysit_plan* p, const int* candidates, int ncand, int nsteps, int* chosen,

@@ -456,9 +456,12 @@ __device__ __forceinline__ void sweep(const WaveParams<T>& p, unsigned char* wsm
 
 // Resident blocks per SM the register budget aims at (FP32): four 4-warp blocks
 // (128 registers); a one-row interior sweep fits five (96 registers).
+#ifndef PGB_SHELL_MINB
+#define PGB_SHELL_MINB 4   // resident 4-warp blocks per SM the FP32 PML-shell kernel aims at
+#endif
 template <typename T, int KIND>
 struct MinBlocks {
-    static constexpr int value = sizeof(T) == 4 ? (KIND == 0 && PGB_RING_RB == 1 ? 5 : 4) : 1;
+    static constexpr int value = sizeof(T) == 4 ? (KIND == 0 ? (PGB_RING_RB == 1 ? 5 : 4) : PGB_SHELL_MINB) : 1;
 };
 
 template <typename T, int R, int MODE, int KIND>

@@ -23,8 +23,9 @@ __all__ = ["WavePlan", "PlanGroup", "padded_cells", "default_checkpoint_every"]
 
 _DESC_AXIS = {1: [2], 2: [0, 2], 3: [0, 1, 2]}  # mesh axis -> (x, y, z) slot of the descriptor
 
-# task lengths along x chosen by WavePlan.autotune, per (dim, order, padded grid, dtype,
-# shots per launch, psi form); later plans of the same configuration start from them
+# tunings chosen by WavePlan.autotune (task length along x, 2D shell block shares per step
+# mode), per (dim, order, padded grid, dtype, shots per launch, psi form, schedule); later
+# plans of the same configuration start from them
 _TUNED = {}
 TILE_CANDIDATES = {2: (16, 32, 64), 3: (16, 32, 64, 128)}
 
@@ -123,9 +124,7 @@ class WavePlan:
         d.use_graph = 1 if use_graph else 0
         d.psi_consistent = 1 if getattr(solver, "pml_psi", "reference") == "consistent" else 0
         self._tune_key = (self.dim, solver.spatial_accuracy_order, tuple(full), str(solver.dtype),
-                          self.shots_per_launch, d.psi_consistent)
-        d.tile_x = _TUNED.get(self._tune_key, 0)
-        self.tile_x = d.tile_x
+                          d.psi_consistent)
         self.record_steps = None
         if record_steps is not None:
             rs = np.ascontiguousarray(np.asarray(record_steps, dtype=np.int32).reshape(-1))
@@ -178,6 +177,13 @@ class WavePlan:
         d.store_dwaveop = 1 if gradient_schedule == "store" else 0
         d.shots_per_launch = self.shots_per_launch
         self.gradient_schedule = gradient_schedule
+        # the tuning key knows the launch size and schedule only now
+        self._tune_key = self._tune_key + (self.shots_per_launch, gradient_schedule, self.forward_only)
+        tuned = _TUNED.get(self._tune_key)
+        d.tile_x = tuned[0] if tuned else 0
+        for k in range(3):
+            d.shell_share[k] = tuned[1][k] if tuned else 0.0
+        self.tile_x = d.tile_x
 
         h = C.c_void_p()
         _native.check(lib.pysit_plan_create(C.byref(d), C.byref(h)))
@@ -355,8 +361,11 @@ class WavePlan:
         _native.check(_native.load().pysit_plan_autotune(self._h, arr, len(cand), int(nsteps), C.byref(chosen), ms,
                                                          C.c_void_p(_native.stream_handle())))
         self.tile_x = int(chosen.value)
-        _TUNED[self._tune_key] = self.tile_x
-        return {"chosen": self.tile_x, "ms": dict(zip(cand, list(ms)))}
+        tile, share = C.c_int(), (C.c_double * 3)()
+        _native.check(_native.load().pysit_plan_get_tuning(self._h, C.byref(tile), share))
+        self.shell_share = [float(v) for v in share]
+        _TUNED[self._tune_key] = (self.tile_x, tuple(self.shell_share))
+        return {"chosen": self.tile_x, "ms": dict(zip(cand, list(ms))), "shell_share": self.shell_share}
 
     def step_loop(self, mode, nsteps):
         """Enqueue `nsteps` launches of one step kernel (0 forward, 1 recompute, 2 adjoint) on the
