@@ -170,6 +170,7 @@ def main():
     ap.add_argument("--shots-per-launch", type=int, default=None)
     ap.add_argument("--schedule", default="auto", choices=["checkpoint", "store", "auto"],
                     help="gradient schedule: recompute from checkpoints, or keep dWaveOp in HBM")
+    ap.add_argument("--lanes", type=int, default=None, help="concurrent shot lanes (default: the schedule's choice)")
     ap.add_argument("--cpu-sample", type=int, default=40)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain per-shot FP64 GPU path")
@@ -251,11 +252,13 @@ def main():
     solver.model_parameters = m0
     from pysit_gb300.autograd import resample_linear
     solver.gradient_schedule = args.schedule
-    plan = WavePlan(solver, shots, checkpoint_every=solver.checkpoint_every, shots_per_launch=args.shots_per_launch)
+    plan = WavePlan(solver, shots, checkpoint_every=solver.checkpoint_every, shots_per_launch=args.shots_per_launch,
+                    lanes=args.lanes)
     tuned_grad = plan.autotune()  # the gradient plan's own launch size (untimed setup)
     plan.dobs.copy_(resample_linear(obs_host.cuda(), ts_obs, solver.ts()))
     config["gradient_schedule"] = plan.gradient_schedule
     config["shots_per_launch"] = plan.shots_per_launch
+    config["lanes"] = plan.lanes
     if plan.gradient_schedule == "store":
         config["workload"] = config["workload"].replace(", checkpoints every 64", "")
         config.pop("checkpoint_every", None)

@@ -164,6 +164,10 @@ typedef struct {
                                       runs beside the interior kernel from the start; 0 = each kernel sized
                                       for the whole GPU (the default: inside the CUDA graph of a sweep
                                       that balanced the two kernels best in measurements) */
+    int lanes;                     /* >= 2: the shots are split into that many contiguous ranges whose
+                                      launch sequences run side by side on their own streams (each lane
+                                      with its own buffers: lanes x the workspace of its shots); 0 or 1 =
+                                      one sequence.  Results are the lanes' sums, in lane order */
 } pysit_plan_desc;
 
 int pysit_plan_create(const pysit_plan_desc* desc, pysit_plan** out);

@@ -58,6 +58,7 @@ class PlanDesc(C.Structure):
         ("store_dwaveop", _i),
         ("forward_only", _i),
         ("shell_share", _d * 3),
+        ("lanes", _i),
     ]
 
 

@@ -26,6 +26,7 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <tuple>
 #include <vector>
 
 #include "wave.cuh"
@@ -1315,9 +1316,11 @@ struct PlanT final : public pysit_plan {
         int rc = PYSIT_OK;
         for (int c = 0; c < ncand && rc == PYSIT_OK; ++c) {
             if ((rc = use_tile(cand[c], s))) break;
-            if ((rc = step_loop(kFwd, 2, s))) break;  // warm-up
+            // the sweeps a gradient runs: forward (in recompute mode when dWaveOp is kept) and adjoint
+            const int fmode = store_all ? kRecomp : kFwd;
+            if ((rc = step_loop(fmode, 2, s))) break;  // warm-up
             cudaEventRecord(e0, s);
-            if ((rc = step_loop(kFwd, n, s)) || (!fwd_only && (rc = step_loop(kAdj, n, s)))) break;
+            if ((rc = step_loop(fmode, n, s)) || (!fwd_only && (rc = step_loop(kAdj, n, s)))) break;
             cudaEventRecord(e1, s);
             if (cudaEventSynchronize(e1) != cudaSuccess) { rc = cuda_status(cudaGetLastError(), "autotune"); break; }
             float ms = 0.f;
@@ -1483,6 +1486,300 @@ struct PlanT final : public pysit_plan {
     }
 };
 
+// out[i] = sum over lanes of g[lane][i] (lanes in order: deterministic); rn_out = sum of rn
+__global__ void lanes_sum_kernel(const double* __restrict__ g, int lanes, long long n, double* __restrict__ out,
+                                 const double* __restrict__ rn, double* __restrict__ rn_out) {
+    if (out)
+        for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+             i += (long long)gridDim.x * blockDim.x) {
+            double a = 0.0;
+            for (int c = 0; c < lanes; ++c) a += g[(long long)c * n + i];
+            out[i] = a;
+        }
+    if (rn_out && blockIdx.x == 0 && threadIdx.x == 0) {
+        double a = 0.0;
+        for (int c = 0; c < lanes; ++c) a += rn[c];
+        *rn_out = a;
+    }
+}
+
+// A plan whose shots are split into `lanes` contiguous ranges, each a plan of its own
+// (own workspace slice, streams and task counters), whose launch sequences run side by side:
+// forked from the caller's stream, joined back, captured in one graph.  The sequences never
+// wait for each other, so one lane's step kernels fill the gaps at the other's step
+// boundaries.  Gradients, images and misfits of the lanes are summed in a fixed order.
+template <typename T>
+struct LanesPlan final : public pysit_plan {
+    std::vector<std::unique_ptr<PlanT<T>>> kids;
+    std::vector<int> first;             // first shot of each lane
+    std::vector<size_t> kid_off;        // workspace offset of each lane
+    size_t off_g = 0, off_rn = 0;       // per-lane unpadded sums and misfits
+    long long ndof = 0;                 // unpadded cells
+    size_t tr_shot = 0;                 // bytes of one shot's traces
+    uint64_t ws_need = 0;
+    char* ws = nullptr;
+    int use_graph = 1;
+    std::vector<cudaStream_t> st;
+    std::vector<cudaEvent_t> done;
+    cudaEvent_t root = nullptr;
+    cudaStream_t cap = nullptr;
+    struct Key {
+        int kind;
+        const void *a, *b, *c, *d;
+        bool operator<(const Key& o) const {
+            return std::tie(kind, a, b, c, d) < std::tie(o.kind, o.a, o.b, o.c, o.d);
+        }
+    };
+    std::map<Key, std::pair<cudaGraphExec_t, int64_t>> graphs;
+
+    ~LanesPlan() override {
+        for (auto& kv : graphs)
+            if (kv.second.first) cudaGraphExecDestroy(kv.second.first);
+        for (auto x : st) cudaStreamDestroy(x);
+        for (auto e : done) cudaEventDestroy(e);
+        if (root) cudaEventDestroy(root);
+        if (cap) cudaStreamDestroy(cap);
+    }
+
+    int init(const pysit_plan_desc& d, int lanes) {
+        use_graph = d.use_graph;
+        for (int c = 0; c < lanes; ++c) {
+            const int s0 = (int)((long long)c * d.nshots / lanes), s1 = (int)((long long)(c + 1) * d.nshots / lanes);
+            first.push_back(s0);
+            pysit_plan_desc k = d;  // the lane's shots: per-shot arrays re-based at s0
+            std::vector<int64_t> sp, rp;
+            k.nshots = s1 - s0;
+            k.shots_per_launch = std::min(d.shots_per_launch, s1 - s0);
+            k.lanes = 1;
+            if (d.src_tap_ptr) {
+                const int64_t b = d.src_tap_ptr[s0];
+                for (int q = s0; q <= s1; ++q) sp.push_back(d.src_tap_ptr[q] - b);
+                k.src_tap_ptr = sp.data();
+                if (d.src_tap_cell) k.src_tap_cell = d.src_tap_cell + b;
+                if (d.src_tap_point) k.src_tap_point = d.src_tap_point + b;
+                if (d.src_tap_w) k.src_tap_w = d.src_tap_w + b;
+            }
+            if (d.src_amp) k.src_amp = d.src_amp + (size_t)s0 * d.nsteps * d.nsrc;
+            if (d.rec_tap_ptr) {
+                const int64_t b = d.rec_tap_ptr[s0];
+                for (int q = s0; q <= s1; ++q) rp.push_back(d.rec_tap_ptr[q] - b);
+                k.rec_tap_ptr = rp.data();
+                if (d.rec_tap_cell) k.rec_tap_cell = d.rec_tap_cell + b;
+                if (d.rec_tap_point) k.rec_tap_point = d.rec_tap_point + b;
+                if (d.rec_tap_wsample) k.rec_tap_wsample = d.rec_tap_wsample + b;
+                if (d.rec_tap_winject) k.rec_tap_winject = d.rec_tap_winject + b;
+            }
+            if (d.shot_nsteps) k.shot_nsteps = d.shot_nsteps + s0;
+            auto kid = std::make_unique<PlanT<T>>();
+            int rc = kid->init(k);  // copies everything it keeps: the re-based arrays may go
+            if (rc) return rc;
+            kids.push_back(std::move(kid));
+        }
+        const PlanT<T>& k0 = *kids[0];
+        ndof = (long long)(k0.nx - k0.pad_lo[0] - k0.pad_hi[0]) * (k0.ny - k0.pad_lo[1] - k0.pad_hi[1]) *
+               (k0.nz - k0.pad_lo[2] - k0.pad_hi[2]);
+        tr_shot = (size_t)k0.nsteps * k0.nrec * sizeof(T);
+        size_t tot = 0;
+        auto take = [&](size_t bytes) { size_t o = tot; tot += (bytes + 255) / 256 * 256; return o; };
+        for (auto& kid : kids) kid_off.push_back(take(kid->ws_need));
+        off_g = take((size_t)lanes * ndof * sizeof(double));
+        off_rn = take((size_t)lanes * sizeof(double));
+        ws_need = tot;
+        return PYSIT_OK;
+    }
+
+    int lanes() const { return (int)kids.size(); }
+    double* g_lane(int c) const { return reinterpret_cast<double*>(ws + off_g) + (size_t)c * ndof; }
+    double* rn_lane(int c) const { return reinterpret_cast<double*>(ws + off_rn) + c; }
+    template <typename P> static P* shift(P* base, size_t bytes) {
+        return base ? reinterpret_cast<P*>(reinterpret_cast<char*>(const_cast<void*>(static_cast<const void*>(base))) + bytes) : nullptr;
+    }
+
+    int workspace_bytes(uint64_t* b) const override { *b = ws_need; return PYSIT_OK; }
+
+    int bind(void* w, uint64_t bytes, cudaStream_t s) override {
+        PGB_REQUIRE(w != nullptr, "NULL workspace");
+        PGB_REQUIRE(aligned(w, 256), "workspace must be 256-byte aligned");
+        PGB_REQUIRE(bytes >= ws_need, "workspace too small: %llu < %llu bytes", (unsigned long long)bytes,
+                    (unsigned long long)ws_need);
+        for (auto& kv : graphs)
+            if (kv.second.first) cudaGraphExecDestroy(kv.second.first);
+        graphs.clear();
+        ws = static_cast<char*>(w);
+        for (int c = 0; c < lanes(); ++c) {
+            int rc = kids[c]->bind(ws + kid_off[c], kids[c]->ws_need, s);
+            if (rc) return rc;
+        }
+        PGB_CHECK_CUDA(cudaMemsetAsync(ws + off_g, 0, ws_need - off_g, s));
+        if (!cap) {
+            PGB_CHECK_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+            PGB_CHECK_CUDA(cudaEventCreateWithFlags(&root, cudaEventDisableTiming));
+            for (int c = 0; c < lanes(); ++c) {
+                cudaStream_t x;
+                cudaEvent_t e;
+                PGB_CHECK_CUDA(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
+                st.push_back(x);
+                PGB_CHECK_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+                done.push_back(e);
+            }
+        }
+        return PYSIT_OK;
+    }
+
+    int set_model(const double* C, cudaStream_t s) override {
+        for (auto& kid : kids) {
+            int rc = kid->set_model(C, s);
+            if (rc) return rc;
+        }
+        return PYSIT_OK;
+    }
+
+    int status(int* flags, cudaStream_t s) override {
+        int all = 0;
+        for (auto& kid : kids) {
+            int f = 0, rc = kid->status(&f, s);
+            if (rc) return rc;
+            all |= f;
+        }
+        *flags = all;
+        return PYSIT_OK;
+    }
+
+    // every lane's sequence on its own stream, forked from s and joined back into s
+    template <typename F>
+    void fork(cudaStream_t s, F fn) {
+        cudaEventRecord(root, s);
+        for (int c = 0; c < lanes(); ++c) {
+            cudaStreamWaitEvent(st[c], root, 0);
+            fn(c, st[c]);
+            cudaEventRecord(done[c], st[c]);
+        }
+        for (int c = 0; c < lanes(); ++c) cudaStreamWaitEvent(s, done[c], 0);
+    }
+
+    void sum(double* out, double* rn_out, cudaStream_t s) {
+        lanes_sum_kernel<<<grid_for(ndof, 256), 256, 0, s>>>(reinterpret_cast<const double*>(ws + off_g), lanes(), ndof,
+                                                            out, reinterpret_cast<const double*>(ws + off_rn), rn_out);
+    }
+
+    int64_t kid_launches() const {
+        int64_t n = 0;
+        for (auto& kid : kids) n += kid->launches;
+        return n;
+    }
+
+    template <typename F>
+    int run(int kind, const void* a, const void* b, const void* c, const void* d, cudaStream_t s, F enqueue) {
+        for (auto& kid : kids) kid->launches = 0;
+        if (!use_graph) {
+            enqueue(s);
+            PGB_CHECK_CUDA(cudaGetLastError());
+            last_launches = kid_launches() + 1;
+            return PYSIT_OK;
+        }
+        Key key{kind, a, b, c, d};
+        auto it = graphs.find(key);
+        if (it == graphs.end()) {
+            cudaGraph_t graph = nullptr;
+            PGB_CHECK_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+            enqueue(cap);
+            cudaError_t e = cudaStreamEndCapture(cap, &graph);
+            if (e != cudaSuccess) return cuda_status(e, "cudaStreamEndCapture");
+            cudaGraphExec_t exec = nullptr;
+            e = cudaGraphInstantiate(&exec, graph, 0);
+            cudaGraphDestroy(graph);
+            if (e != cudaSuccess) return cuda_status(e, "cudaGraphInstantiate");
+            it = graphs.emplace(key, std::make_pair(exec, kid_launches() + 1)).first;
+        }
+        PGB_CHECK_CUDA(cudaGraphLaunch(it->second.first, s));
+        last_launches = it->second.second;
+        return PYSIT_OK;
+    }
+
+    int ready() const {
+        PGB_REQUIRE(ws, "no workspace bound");
+        PGB_REQUIRE(kids[0]->model_set, "pysit_plan_set_model must be called first");
+        return PYSIT_OK;
+    }
+
+    int forward(void* traces, cudaStream_t s) override {
+        if (int rc = ready()) return rc;
+        return run(0, traces, nullptr, nullptr, nullptr, s, [&](cudaStream_t q) {
+            fork(q, [&](int c, cudaStream_t x) { kids[c]->enqueue_forward(shift(traces, first[c] * tr_shot), x); });
+        });
+    }
+
+    void enqueue_grad(const void* dobs, double* grad, double* rnorm2, void* traces, bool with_grad, bool migrate,
+                      cudaStream_t q) {
+        fork(q, [&](int c, cudaStream_t x) {
+            kids[c]->enqueue_gradient(shift(dobs, first[c] * tr_shot), with_grad ? g_lane(c) : nullptr, rn_lane(c),
+                                      shift(traces, first[c] * tr_shot), with_grad, migrate, x);
+        });
+        sum(with_grad ? grad : nullptr, rnorm2, q);
+    }
+
+    int gradient(const void* dobs, double* grad, double* rnorm2, void* traces, cudaStream_t s, bool with_grad,
+                 bool migrate) override {
+        if (int rc = ready()) return rc;
+        const PlanT<T>& k0 = *kids[0];
+        PGB_REQUIRE(dobs || k0.nrec == 0, "NULL observed data");
+        PGB_REQUIRE(rnorm2, "NULL misfit output");
+        PGB_REQUIRE(!k0.fwd_only || !with_grad, "the plan was built for forward modelling only");
+        PGB_REQUIRE(!with_grad || grad, "NULL gradient output");
+        return run(migrate ? 3 : with_grad ? 1 : 2, dobs, grad, rnorm2, traces, s, [&](cudaStream_t q) {
+            enqueue_grad(dobs, grad, rnorm2, traces, with_grad, migrate, q);
+        });
+    }
+
+    int enqueue_grad_raw(const void* dobs, double* grad, double* rnorm2, cudaStream_t s) override {
+        if (int rc = ready()) return rc;
+        PGB_REQUIRE((dobs || kids[0]->nrec == 0) && grad && rnorm2, "NULL argument");
+        PGB_REQUIRE(!kids[0]->fwd_only, "the plan was built for forward modelling only");
+        for (auto& kid : kids) kid->launches = 0;
+        enqueue_grad(dobs, grad, rnorm2, nullptr, true, false, s);
+        last_launches = kid_launches() + 1;
+        return PYSIT_OK;
+    }
+
+    int born(const double* m1, void* traces, cudaStream_t s) override {
+        if (int rc = ready()) return rc;
+        PGB_REQUIRE(!kids[0]->fwd_only, "the plan was built for forward modelling only");
+        PGB_REQUIRE(m1, "NULL model perturbation");
+        PGB_REQUIRE(traces || kids[0]->nrec == 0, "NULL traces output");
+        return run(4, m1, traces, nullptr, nullptr, s, [&](cudaStream_t q) {
+            fork(q, [&](int c, cudaStream_t x) { kids[c]->enqueue_born(m1, shift(traces, first[c] * tr_shot), x); });
+        });
+    }
+
+    int hessian(const double* m1, double* out, double* d1norm2, cudaStream_t s) override {
+        if (int rc = ready()) return rc;
+        const PlanT<T>& k0 = *kids[0];
+        PGB_REQUIRE(!k0.fwd_only, "the plan was built for forward modelling only");
+        PGB_REQUIRE(!k0.store_all || k0.p_img == 1, "a plan that keeps dWaveOp applies the Hessian with imaging_period 1 only");
+        PGB_REQUIRE(m1 && out, "NULL argument");
+        return run(5, m1, out, d1norm2, nullptr, s, [&](cudaStream_t q) {
+            fork(q, [&](int c, cudaStream_t x) { kids[c]->enqueue_hessian(m1, g_lane(c), rn_lane(c), x); });
+            sum(out, d1norm2, q);
+        });
+    }
+
+    // timing and tuning act on the first lane's buffers; the chosen task length goes to all
+    int step_loop(int mode, int n, cudaStream_t s) override {
+        int rc = kids[0]->step_loop(mode, n, s);
+        last_launches = kids[0]->last_launches;
+        return rc;
+    }
+    int autotune(const int* cand, int ncand, int n, int* chosen, double* ms, cudaStream_t s) override {
+        int rc = kids[0]->autotune(cand, ncand, n, chosen, ms, s);
+        for (int c = 1; c < lanes() && rc == PYSIT_OK; ++c) rc = kids[c]->use_tile(*chosen, s);
+        for (auto& kv : graphs)
+            if (kv.second.first) cudaGraphExecDestroy(kv.second.first);
+        graphs.clear();
+        return rc;
+    }
+    int tuning(int* tile, double* share) const override { return kids[0]->tuning(tile, share); }
+};
+
 }  // namespace
 }  // namespace pgb
 
@@ -1512,7 +1809,16 @@ extern "C" int pysit_plan_create(const pysit_plan_desc* d, pysit_plan** out) {
     if (d->dim == 3) PGB_REQUIRE(d->n[1] >= 3, "3D needs ny >= 3");
     std::unique_ptr<pysit_plan> p;
     int rc;
-    if (d->dtype == PYSIT_F64) {
+    const int lanes = std::min(std::max(d->lanes, 1), d->nshots);
+    if (lanes > 1 && d->dtype == PYSIT_F64) {
+        auto q = std::make_unique<LanesPlan<double>>();
+        rc = q->init(*d, lanes);
+        p = std::move(q);
+    } else if (lanes > 1) {
+        auto q = std::make_unique<LanesPlan<float>>();
+        rc = q->init(*d, lanes);
+        p = std::move(q);
+    } else if (d->dtype == PYSIT_F64) {
         auto q = std::make_unique<PlanT<double>>();
         rc = q->init(*d);
         p = std::move(q);

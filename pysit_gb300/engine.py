@@ -52,7 +52,7 @@ class WavePlan:
     """Device plan of one (solver configuration, shot list)."""
 
     def __init__(self, solver, shots, imaging_period=1, checkpoint_every=None, shots_per_launch=None,
-                 use_graph=None, record_steps=None, gradient_schedule=None, forward_only=False):
+                 use_graph=None, record_steps=None, gradient_schedule=None, forward_only=False, lanes=None):
         """``record_steps``: optional record length of each shot in time steps (<= solver.nsteps);
         a shorter shot's residual is zero from its length on, so its misfit and gradient are those
         of a run of that length (the shots of one plan still step together).
@@ -62,7 +62,9 @@ class WavePlan:
         from the forward sweep in HBM (no recompute sweep; about ceil(nsteps / imaging_period)
         fields per shot of a launch).  'auto' keeps them when the launch fits in free device
         memory, taking as many shots per launch as fit unless shots_per_launch is fixed.
-        ``forward_only`` plans model data only (no adjoint, imaging or checkpoint storage)."""
+        ``forward_only`` plans model data only (no adjoint, imaging or checkpoint storage).
+        ``lanes`` (default 1): the shots split into that many ranges whose launch sequences run
+        side by side on their own streams, shots_per_launch being per lane."""
         torch = _native.require_cuda()
         lib = _native.load()
         self.solver = solver
@@ -83,6 +85,7 @@ class WavePlan:
             shots_per_launch = solver.shots_per_launch or self.nshots
         self.shots_per_launch = int(max(1, min(shots_per_launch, self.nshots)))
         self.forward_only = bool(forward_only)
+        self.lanes = int(max(1, min(lanes or 1, self.nshots)))
         if gradient_schedule is None:
             gradient_schedule = getattr(solver, "gradient_schedule", "checkpoint")
         if gradient_schedule not in ("checkpoint", "store", "auto"):
@@ -172,13 +175,15 @@ class WavePlan:
         d.nsrc = nsrc
         d.nrec = nrec
         d.forward_only = 1 if self.forward_only else 0
+        d.lanes = self.lanes
         if gradient_schedule == "auto":
             gradient_schedule = self._choose_schedule(lib, d, fixed_launch, nrec)
+        d.lanes = self.lanes
         d.store_dwaveop = 1 if gradient_schedule == "store" else 0
         d.shots_per_launch = self.shots_per_launch
         self.gradient_schedule = gradient_schedule
         # the tuning key knows the launch size and schedule only now
-        self._tune_key = self._tune_key + (self.shots_per_launch, gradient_schedule, self.forward_only)
+        self._tune_key = self._tune_key + (self.shots_per_launch, gradient_schedule, self.forward_only, self.lanes)
         tuned = _TUNED.get(self._tune_key)
         d.tile_x = tuned[0] if tuned else 0
         for k in range(3):
@@ -214,9 +219,10 @@ class WavePlan:
             self._h = None
 
     @staticmethod
-    def _workspace_for(lib, d, shots_per_launch, store):
+    def _workspace_for(lib, d, shots_per_launch, store, lanes=1):
         d.shots_per_launch = int(shots_per_launch)
         d.store_dwaveop = 1 if store else 0
+        d.lanes = int(lanes)
         h = C.c_void_p()
         _native.check(lib.pysit_plan_create(C.byref(d), C.byref(h)))
         n = C.c_uint64()
@@ -236,18 +242,22 @@ class WavePlan:
         budget = free - outputs - max(2 << 30, int(0.03 * free))
         G = self.shots_per_launch
         if fixed_launch:
-            return "store" if self._workspace_for(lib, d, G, True) <= budget else "checkpoint"
+            return "store" if self._workspace_for(lib, d, G, True, self.lanes) <= budget else "checkpoint"
         b1 = self._workspace_for(lib, d, 1, True)
         per = self._workspace_for(lib, d, 2, True) - b1
         gmax = self.nshots if per <= 0 else int((budget - (b1 - per)) // per)
         gmax = min(gmax, self.nshots)
         if gmax < min(16, self.nshots):
             return "checkpoint"
-        launches = -(-self.nshots // gmax)
-        G = -(-self.nshots // launches)
-        while G > 1 and self._workspace_for(lib, d, G, True) > budget:
+        lanes = self.lanes  # lanes are not split further: two half-size lanes measured slower in 2D
+        per_lane = -(-self.nshots // lanes)           # shots of the largest lane
+        glane = min(gmax // lanes, per_lane)
+        launches = -(-per_lane // glane)
+        G = -(-per_lane // launches)
+        while G > 1 and self._workspace_for(lib, d, G, True, lanes) > budget:
             G -= 1
         self.shots_per_launch = G
+        self.lanes = lanes
         return "store"
 
     # ---------------------------------------------------------------------------
@@ -347,7 +357,7 @@ class WavePlan:
                                                         C.c_void_p(_native.stream_handle())))
         return self.hess, self.rnorm2
 
-    def autotune(self, candidates=None, nsteps=16):
+    def autotune(self, candidates=None, nsteps=48):
         """Time the task lengths along x in `candidates` (forward + adjoint steps on this plan's
         buffers), keep the fastest for this plan and for later plans of the same configuration.
         Returns {"chosen": rows, "ms": {candidate: milliseconds}}.  1D plans have no tiles."""

@@ -161,3 +161,22 @@ def test_workspace_of_the_schedules(lib):
     field = (30 + 8) * 32 * 4 * 2  # one FP32 field of the 2 shots (rows x pitch), lower bound
     assert sizes["store"] - sizes["store_p2"] >= 24 * field  # 50 vs 25 kept steps
     assert sizes["store"] > sizes["ckpt"] > sizes["fwd"]
+
+
+def test_lanes_plan_workspace(lib):
+    """lanes = 2 builds one plan per shot range; its workspace holds both plus the lane sums."""
+    sizes = {}
+    for lanes in (1, 2):
+        keep = []
+        d = _desc(keep=keep, nshots=2)
+        d.shots_per_launch = 1
+        d.lanes = lanes
+        h = C.c_void_p()
+        _native.check(lib.pysit_plan_create(C.byref(d), C.byref(h)))
+        nb = C.c_uint64()
+        _native.check(lib.pysit_plan_workspace_bytes(h, C.byref(nb)))
+        sizes[lanes] = nb.value
+        tile = C.c_int()
+        _native.check(lib.pysit_plan_get_tuning(h, C.byref(tile), None))
+        lib.pysit_plan_destroy(h)
+    assert sizes[2] > sizes[1]

@@ -88,3 +88,46 @@ def test_auto_schedule_keeps_dwaveop_when_it_fits():
     assert obj.last_plan.gradient_schedule == "store"
     ref = _grad(solver, shots, "checkpoint")[0]
     np.testing.assert_array_equal(np.ravel(g.data), ref)
+
+
+@pytest.mark.parametrize("schedule", ["store", "checkpoint"])
+def test_lanes_match_one_sequence(schedule):
+    """Two lanes (independent launch sequences side by side) give the same traces to the bit and
+    the same sums up to their order of summation."""
+    import torch
+    m, shots, solver, C, C0 = problems.build(api, "o6", spec_overrides=dict(nsrc=5))
+    api.generate_seismic_data(shots, solver, solver.ModelParameters(m, {"C": C}))
+    solver.model_parameters = solver.ModelParameters(m, {"C": C0})
+    one = WavePlan(solver, shots, gradient_schedule=schedule, shots_per_launch=2, checkpoint_every=6)
+    two = WavePlan(solver, shots, gradient_schedule=schedule, shots_per_launch=2, checkpoint_every=6, lanes=2)
+    assert two.lanes == 2
+    np.testing.assert_array_equal(two.forward().cpu().numpy(), one.forward().cpu().numpy())
+    for p in (one, two):
+        p.load_observed()
+    g1, r1 = (t.cpu().numpy().copy() for t in one.gradient(with_traces=True))
+    g2, r2 = (t.cpu().numpy().copy() for t in two.gradient(with_traces=True))
+    np.testing.assert_array_equal(two.traces.cpu().numpy(), one.traces.cpu().numpy())
+    assert np.linalg.norm(g2 - g1) <= 1e-13 * np.linalg.norm(g1)
+    assert r2[0] == pytest.approx(r1[0], rel=1e-13)
+    assert float(two.misfit().item()) == pytest.approx(float(one.misfit().item()), rel=1e-13)
+    rng = np.random.default_rng(2)
+    m1 = rng.standard_normal(m.dof()) * 1e-9
+    h1 = one.hessian(m1)[0].cpu().numpy().copy()
+    h2 = two.hessian(m1)[0].cpu().numpy().copy()
+    assert np.linalg.norm(h2 - h1) <= 1e-13 * np.linalg.norm(h1)
+    np.testing.assert_array_equal(two.born(m1).cpu().numpy(), one.born(m1).cpu().numpy())
+    d = torch.as_tensor(rng.standard_normal(tuple(one.traces.shape)), device="cuda")
+    i1 = one.migrate(d).cpu().numpy().copy()
+    i2 = two.migrate(d).cpu().numpy().copy()
+    assert np.linalg.norm(i2 - i1) <= 1e-13 * np.linalg.norm(i1)
+    assert two.status() == 0
+    # a lanes plan inside a plan group (migrate left its operand in the observed-data buffer)
+    from pysit_gb300.engine import PlanGroup
+    two.load_observed()
+    grp = PlanGroup([two])
+    (gg, rr), = grp.gradient()
+    assert np.linalg.norm(gg.cpu().numpy() - g1) <= 1e-13 * np.linalg.norm(g1)
+    # tuning reaches every lane
+    two.autotune(candidates=(8, 16), nsteps=2)
+    g3 = two.gradient()[0].cpu().numpy()
+    assert np.linalg.norm(g3 - g1) <= 1e-13 * np.linalg.norm(g1)
