@@ -18,6 +18,8 @@ call computes misfit and gradient of every shot (FP64 reductions on the GPU).
 """
 from __future__ import annotations
 
+import weakref
+
 import math
 
 import numpy as np
@@ -94,7 +96,12 @@ class FWIMisfit:
         self.imaging_period = imaging_period
         self.plan_kw = plan_kw
         self._fn = None
-        self.last_plan = None
+        self._last_plan = None  # weak: a cached plan may hold most of the device memory
+
+    @property
+    def last_plan(self):
+        """The plan of the last call while the plan cache still holds it, else None."""
+        return self._last_plan() if self._last_plan is not None else None
 
     def _set_model(self, C_dev):
         torch = _native.require_cuda()
@@ -118,7 +125,7 @@ class FWIMisfit:
         C_dev = C.detach().to("cuda", non_blocking=True)
         dt, nsteps = self._set_model(C_dev)
         plan = plan_for(self.solver, self.shots, self.imaging_period, **self.plan_kw)
-        self.last_plan = plan
+        self._last_plan = weakref.ref(plan)
         obs = self.observed.to("cuda", non_blocking=True).to(plan.tdtype)
         plan.dobs.copy_(resample_linear(obs, self.ts_observed, self.solver.ts()))
         if want_grad:

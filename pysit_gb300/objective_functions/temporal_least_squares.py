@@ -13,6 +13,8 @@ also provides the pseudo-Hessian diagonal (:121-139).
 """
 from __future__ import annotations
 
+import weakref
+
 import numpy as np
 
 from .. import _native
@@ -50,7 +52,12 @@ class TemporalLeastSquares(ObjectiveFunctionBase):
         self.imaging_period = int(imaging_period)
         self.batched = batched
         self.plan_kwargs = plan_kwargs
-        self.last_plan = None
+        self._last_plan = None  # weak: a cached plan may hold most of the device memory
+
+    @property
+    def last_plan(self):
+        """The plan of the last batched call while the plan cache still holds it, else None."""
+        return self._last_plan() if self._last_plan is not None else None
 
     # ---- reference per-shot path ---------------------------------------------------
     def _residual(self, shot, m0, dWaveOp=None, wavefield=None):
@@ -97,7 +104,7 @@ class TemporalLeastSquares(ObjectiveFunctionBase):
         self.solver.model_parameters = m0
         plan = plan_for(self.solver, list(shots), self.imaging_period, **self.plan_kwargs)
         plan.load_observed()
-        self.last_plan = plan
+        self._last_plan = weakref.ref(plan)
         return plan
 
     def evaluate(self, shots, m0, **kwargs):
@@ -158,7 +165,7 @@ class TemporalLeastSquares(ObjectiveFunctionBase):
         if self.batched and hessian_mode in ("approximate", "levenberg"):
             self.solver.model_parameters = m0
             plan = plan_for(self.solver, list(shots), 1, **self.plan_kwargs)
-            self.last_plan = plan
+            self._last_plan = weakref.ref(plan)
             h, _ = plan.hessian(m1)
             result = m0.perturbation(data=h.cpu().numpy().reshape(-1, 1))
         else:

@@ -117,11 +117,14 @@ def cfg3(scale=1.0, nshots=8, nsteps=3000, order=8, precision="single", cfl=0.35
     return m, shots, solver, C, C0
 
 
-def cfg5(scale=1.0, nshots=128, nsteps=4000, precision="single", shots_per_launch=64, **kw):
+def cfg5(scale=1.0, nshots=128, nsteps=4000, precision="single", shots_per_launch=None, gradient_schedule="auto",
+         **kw):
     """(mesh, shots, solver, C_true, C_start) of the end-to-end FWI workload: the cfg2 model
-    and start model with 128 shots (64 per launch keeps two plans within HBM)."""
+    and start model with 128 shots.  The default schedule keeps dWaveOp in HBM with as many
+    shots per launch as fit; ``gradient_schedule="checkpoint", shots_per_launch=64`` is the
+    checkpointed configuration."""
     return cfg2(scale=scale, nshots=nshots, nsteps=nsteps, precision=precision,
-                shots_per_launch=shots_per_launch, **kw)
+                shots_per_launch=shots_per_launch, gradient_schedule=gradient_schedule, **kw)
 
 
 def run_lbfgs(m, shots, solver, C, C0, iterations=20, memory_length=10, batched=True, verbose=False):
@@ -150,7 +153,9 @@ def run_lbfgs(m, shots, solver, C, C0, iterations=20, memory_length=10, batched=
     return {"objective": [float(v) for v in hist], "alpha": [float(a) for a in alpha],
             "rel_model_error": float(np.linalg.norm(Cf - Ct) / np.linalg.norm(Ct)),
             "rel_model_error_start": float(np.linalg.norm(C0f - Ct) / np.linalg.norm(Ct)),
-            "seconds": seconds, "iterations": iterations, "shots": len(shots), "nsteps": solver.nsteps}
+            "seconds": seconds, "iterations": iterations, "shots": len(shots), "nsteps": solver.nsteps,
+            "plan": ({"schedule": objective.last_plan.gradient_schedule,
+                      "shots_per_launch": objective.last_plan.shots_per_launch} if objective.last_plan else None)}
 
 
 def cfg4(scale=1.0, nshots=256, order=6, precision="single", seed=2028, cfl=0.4):
@@ -358,6 +363,8 @@ def _main(argv=None):
     ap = argparse.ArgumentParser(prog="python -m pysit_gb300.workloads")
     ap.add_argument("workload", choices=["cfg4", "cfg5", "hessian", "gn", "steps2d", "steps3d"])
     ap.add_argument("--shots-per-launch", type=int, default=None)
+    ap.add_argument("--schedule", default="auto", choices=["checkpoint", "store", "auto"],
+                    help="cfg5 / gn: gradient schedule of the batched objective")
     ap.add_argument("--krylov", type=int, default=5, help="gn: GMRES iterations per Gauss-Newton step")
     ap.add_argument("--iterations", type=int, default=20)
     ap.add_argument("--shots", type=int, default=None, help="default 256 (cfg4), 128 (cfg5)")
@@ -384,16 +391,19 @@ def _main(argv=None):
         return
     prec = "double" if a.plain else "single"
     if a.workload == "gn":
-        m, shots, solver, C, C0 = cfg5(scale=a.scale, nshots=a.shots or 64, nsteps=a.nsteps, precision=prec)
+        m, shots, solver, C, C0 = cfg5(scale=a.scale, nshots=a.shots or 64, nsteps=a.nsteps, precision=prec,
+                                       shots_per_launch=a.shots_per_launch, gradient_schedule=a.schedule)
         out = run_gauss_newton(m, shots, solver, C, C0, iterations=a.iterations, krylov_maxiter=a.krylov,
                                batched=not a.plain, verbose=a.verbose)
         out.update(workload="Gauss-Newton on the cfg5 model", path="plain FP64" if a.plain else "batched FP32",
                    scale=a.scale)
         print(json.dumps(out))
         return
-    m, shots, solver, C, C0 = cfg5(scale=a.scale, nshots=a.shots or 128, nsteps=a.nsteps, precision=prec)
+    m, shots, solver, C, C0 = cfg5(scale=a.scale, nshots=a.shots or 128, nsteps=a.nsteps, precision=prec,
+                                   shots_per_launch=a.shots_per_launch, gradient_schedule=a.schedule)
     out = run_lbfgs(m, shots, solver, C, C0, iterations=a.iterations, batched=not a.plain, verbose=a.verbose)
-    out.update(workload=a.workload, path="plain FP64" if a.plain else "batched FP32", scale=a.scale)
+    out.update(workload=a.workload, path="plain FP64" if a.plain else "batched FP32", scale=a.scale,
+               schedule=getattr(solver, "gradient_schedule", None))
     print(json.dumps(out))
 
 
