@@ -131,3 +131,19 @@ def test_lanes_match_one_sequence(schedule):
     two.autotune(candidates=(8, 16), nsteps=2)
     g3 = two.gradient()[0].cpu().numpy()
     assert np.linalg.norm(g3 - g1) <= 1e-13 * np.linalg.norm(g1)
+
+
+def test_observed_data_resampled_on_the_device_match_the_host():
+    """load_observed resamples a device copy of the recorded traces (uploaded once); it
+    matches ReceiverSet.interpolate_data, and an in-place edit of the traces is picked up."""
+    import torch
+    m, shots, solver, C, C0 = _setup("o8")  # data recorded on the true model's time axis
+    plan = WavePlan(solver, shots)
+    dev = plan.load_observed().cpu().numpy().copy()
+    ts = solver.ts()
+    host = np.stack([s.receivers.interpolate_data(ts) for s in shots])
+    nrec = shots[0].receivers.receiver_count
+    np.testing.assert_allclose(dev[:, :, :nrec], host, rtol=0, atol=1e-13 * np.abs(host).max())
+    shots[1].receivers.data *= 2.0
+    dev2 = plan.load_observed().cpu().numpy()
+    np.testing.assert_allclose(dev2[1, :, :nrec], 2 * host[1], rtol=0, atol=1e-13 * np.abs(host).max())
