@@ -41,9 +41,11 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "FWI gradient shots/s, batched adjoint vs plain, 1xGB300 at <=1e-3 rel err; Gcell/s"
-# DRAM bytes (read + write) per launch of each 2D step, from an ncu capture of the
-# same kernels (profiles/); None where no capture backs a number
-TRAFFIC = {"forward": None, "recompute": None, "adjoint": None}
+# DRAM bytes (read + write) per shot of a launch of each 2D step (interior + PML-shell kernels),
+# from ncu captures of the same kernels at 22 shots per launch and task length 16
+# (profiles/wave2d_steps_cfg2_22shots_dram.md); a launch's traffic is this times its shots (the
+# kernels' traffic grows in proportion to the shots).  None where no capture backs a number.
+TRAFFIC_PER_SHOT = {"forward": None, "recompute": 192.0e6 / 22, "adjoint": 326.5e6 / 22}
 
 
 def _peaks():
@@ -302,6 +304,7 @@ def main():
                        "kernel_launches_per_step": plan.launches() // nrep}
     if plan.status():
         raise RuntimeError("device status flags set during the kernel timing")
+    shots_per_launch = plan.shots_per_launch
     del plan
     torch.cuda.empty_cache()
     if world > 1:
@@ -341,7 +344,11 @@ def main():
             "e2e": {"value": world * args.shots / t_e2e, "unit": "shots/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
             "roofline": {"bound": "hbm", "achieved": dom["achieved_gbs"], "peak": peak, "unit": "GB/s",
-                         "frac": dom["achieved_gbs"] / peak, "traffic": TRAFFIC.get(dom_name), "peak_kind": peak_kind,
+                         "frac": dom["achieved_gbs"] / peak,
+                         "traffic": (TRAFFIC_PER_SHOT[dom_name] * shots_per_launch
+                                     if TRAFFIC_PER_SHOT.get(dom_name) else None),
+                         "traffic_note": "ncu capture at 22 shots per launch, task length 16, scaled by shots",
+                         "peak_kind": peak_kind,
                          "kernel": f"2D {dom_name} step (interior + PML-shell kernels)",
                          "bytes_per_launch": dom["bytes_per_launch"], "launch_ms": dom["launch_ms"],
                          "modes": {k: {"launch_ms": v["launch_ms"], "achieved_gbs": v["achieved_gbs"],

@@ -35,7 +35,7 @@ from scipy.ndimage import gaussian_filter
 
 from . import core, solvers
 
-__all__ = ["layered_model", "cfg2", "cfg3", "cfg4", "cfg5", "run_lbfgs", "run_uneven_batch", "run_hessian",
+__all__ = ["layered_model", "cfg1", "run_cfg1", "cfg2", "cfg3", "cfg4", "cfg5", "run_lbfgs", "run_uneven_batch", "run_hessian",
            "run_gauss_newton", "run_steps"]
 
 
@@ -55,6 +55,57 @@ def layered_model(shape, nlayers, vmin, vmax, sigma_cells, amp, seed, clip=(1500
 def _steps_T(C0, deltas, cfl, nsteps):
     dt = cfl * min(deltas) / float(np.abs(C0).max())
     return (nsteps - 0.5) * dt
+
+
+def cfg1(precision="double"):
+    """(mesh, shots, solver, C_true, C_start) of the small CPU-sized case: 121 x 61 nodes at
+    10 m with 10-cell PML (amplitude 180 = 3 c_max ln(1e3) / (2 L)), order 4, a Gaussian
+    horizontal reflector (1500 m/s, +15 % at 350 m depth, 20 m wide), one 10 Hz Ricker source at
+    the surface centre, 121 surface receivers, T = 1.2 s at CFL 0.5 (414 steps on the true model,
+    360 on the start model); the gradient is
+    taken at the constant 1500 m/s model."""
+    pml = core.PML(100.0, 180.0)
+    d = core.RectangularDomain((0.0, 1200.0, pml, pml), (0.0, 600.0, pml, pml))
+    m = core.CartesianMesh(d, 121, 61)
+    z = m.mesh_coords()[-1]
+    C = 1500.0 * (1 + 0.15 * np.exp(-(z - 350.0) ** 2 / (2 * 20.0 ** 2)))
+    C0 = 1500.0 * np.ones_like(C)
+    shots = core.equispaced_acquisition(m, core.RickerWavelet(10.0), sources=1, receivers="max",
+                                        source_depth=0.0, receiver_depth=0.0)
+    solver = solvers.ConstantDensityAcousticWave(m, spatial_accuracy_order=4, trange=(0.0, 1.2),
+                                                 kernel_implementation="cuda", precision=precision,
+                                                 cfl_safety=0.5)
+    return m, shots, solver, C, C0
+
+
+def run_cfg1(repeats=20):
+    """Gradient of the small case through the batched plan (FP64) and through the plain
+    per-step loop (FP64), each the mean of `repeats` calls after a warm-up."""
+    import time
+
+    import torch
+
+    from .modeling import generate_seismic_data
+    from .objective_functions import TemporalLeastSquares
+
+    m, shots, solver, C, C0 = cfg1()
+    generate_seismic_data(shots, solver, solver.ModelParameters(m, {"C": C}))
+    m0 = solver.ModelParameters(m, {"C": C0})
+    out = {"grid": [int(v) for v in m.shape(include_bc=True, as_grid=True)]}
+    for name, batched, reps in (("batched", True, repeats), ("plain", False, max(1, repeats // 10))):
+        obj = TemporalLeastSquares(solver, batched=batched)
+        aux = {"objective_value": (True, None)}
+        obj.compute_gradient(shots, m0, aux)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            obj.compute_gradient(shots, m0, aux)
+        torch.cuda.synchronize()
+        t = (time.perf_counter() - t0) / reps
+        out[name] = {"seconds": t, "shots_per_s": 1.0 / t, "objective": float(aux["objective_value"][1])}
+    out["nsteps"] = int(solver.nsteps)
+    out["batched_over_plain"] = out["plain"]["seconds"] / out["batched"]["seconds"]
+    return out
 
 
 def cfg2(scale=1.0, nshots=64, nsteps=4000, order=8, precision="single", cfl=0.4, checkpoint_every=64,
@@ -361,7 +412,7 @@ def _main(argv=None):
     import json
 
     ap = argparse.ArgumentParser(prog="python -m pysit_gb300.workloads")
-    ap.add_argument("workload", choices=["cfg4", "cfg5", "hessian", "gn", "steps2d", "steps3d"])
+    ap.add_argument("workload", choices=["cfg1", "cfg4", "cfg5", "hessian", "gn", "steps2d", "steps3d"])
     ap.add_argument("--shots-per-launch", type=int, default=None)
     ap.add_argument("--schedule", default="auto", choices=["checkpoint", "store", "auto"],
                     help="cfg5 / gn: gradient schedule of the batched objective")
@@ -376,6 +427,11 @@ def _main(argv=None):
     if a.workload == "cfg4":
         out = run_uneven_batch(cfg4(scale=a.scale, nshots=a.shots or 256))
         out.update(workload="cfg4", scale=a.scale)
+        print(json.dumps(out))
+        return
+    if a.workload == "cfg1":
+        out = run_cfg1()
+        out.update(workload="cfg1: 121 x 61 at 10 m + 10 PML, order 4, FP64, 1 shot, 414 steps")
         print(json.dumps(out))
         return
     if a.workload in ("steps2d", "steps3d"):
