@@ -74,7 +74,7 @@ def cfg1(precision="double"):
                                         source_depth=0.0, receiver_depth=0.0)
     solver = solvers.ConstantDensityAcousticWave(m, spatial_accuracy_order=4, trange=(0.0, 1.2),
                                                  kernel_implementation="cuda", precision=precision,
-                                                 cfl_safety=0.5)
+                                                 cfl_safety=0.5, autotune=True, gradient_schedule="auto")
     return m, shots, solver, C, C0
 
 
