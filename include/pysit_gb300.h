@@ -250,9 +250,9 @@ int pysit_plan_step_loop(pysit_plan* plan, int mode, int nsteps, void* stream);
 
 /* Autotuner, no counterpart in the reference (its kernels have no tiles): times
  * `nsteps` forward and `nsteps` adjoint steps (as pysit_plan_step_loop does) for
- * each of the `ncand` task lengths along x in `candidates` (8..4096 rows), keeps
- * the fastest, writes it to *chosen and the measured milliseconds per candidate to
- * ms[ncand] (may be NULL).  Needs a bound workspace and a model; 2D and 3D plans.
+ * each of the `ncand` task lengths along x in `candidates` (8..4096 rows), twice (the
+ * second pass in reverse order), keeps the fastest, writes it to *chosen and the
+ * better of each candidate's two times in milliseconds to ms[ncand] (may be NULL).  Needs a bound workspace and a model; 2D and 3D plans.
  * It drops the plan's captured graphs (they hold the old task tables); the
  * wavefield buffers are left in an arbitrary state, as after step_loop. */
 int pysit_plan_autotune(pysit_plan* plan, const int* candidates, int ncand, int nsteps, int* chosen,

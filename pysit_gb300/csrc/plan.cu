@@ -1314,19 +1314,26 @@ struct PlanT final : public pysit_plan {
         int best = cand[0];
         float best_ms = 1e30f;
         int rc = PYSIT_OK;
+        // two passes over the candidates, the second in reverse order; each keeps its faster time
+        std::vector<float> t(ncand, 1e30f);
+        for (int pass = 0; pass < 2 && rc == PYSIT_OK; ++pass)
+            for (int i = 0; i < ncand && rc == PYSIT_OK; ++i) {
+                const int c = pass == 0 ? i : ncand - 1 - i;
+                if ((rc = use_tile(cand[c], s))) break;
+                // the sweeps a gradient runs: forward (in recompute mode when dWaveOp is kept) and adjoint
+                const int fmode = store_all ? kRecomp : kFwd;
+                if ((rc = step_loop(fmode, 2, s))) break;  // warm-up
+                cudaEventRecord(e0, s);
+                if ((rc = step_loop(fmode, n, s)) || (!fwd_only && (rc = step_loop(kAdj, n, s)))) break;
+                cudaEventRecord(e1, s);
+                if (cudaEventSynchronize(e1) != cudaSuccess) { rc = cuda_status(cudaGetLastError(), "autotune"); break; }
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                t[c] = std::min(t[c], ms);
+            }
         for (int c = 0; c < ncand && rc == PYSIT_OK; ++c) {
-            if ((rc = use_tile(cand[c], s))) break;
-            // the sweeps a gradient runs: forward (in recompute mode when dWaveOp is kept) and adjoint
-            const int fmode = store_all ? kRecomp : kFwd;
-            if ((rc = step_loop(fmode, 2, s))) break;  // warm-up
-            cudaEventRecord(e0, s);
-            if ((rc = step_loop(fmode, n, s)) || (!fwd_only && (rc = step_loop(kAdj, n, s)))) break;
-            cudaEventRecord(e1, s);
-            if (cudaEventSynchronize(e1) != cudaSuccess) { rc = cuda_status(cudaGetLastError(), "autotune"); break; }
-            float ms = 0.f;
-            cudaEventElapsedTime(&ms, e0, e1);
-            if (ms_out) ms_out[c] = ms;
-            if (ms < best_ms) { best_ms = ms; best = cand[c]; }
+            if (ms_out) ms_out[c] = t[c];
+            if (t[c] < best_ms) { best_ms = t[c]; best = cand[c]; }
         }
         if (rc == PYSIT_OK) rc = use_tile(best, s);
         cudaEventDestroy(e0);

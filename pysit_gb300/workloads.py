@@ -313,6 +313,7 @@ def run_hessian(m, shots, solver, C, C0, repeats=2):
     solver.model_parameters = solver.ModelParameters(m, {"C": C})
     obs = WavePlan(solver, shots, forward_only=True).forward().clone()
     ts_true = solver.ts()
+    torch.cuda.empty_cache()
     solver.model_parameters = solver.ModelParameters(m, {"C": C0})
     plan = WavePlan(solver, shots)
     plan.autotune()
@@ -323,7 +324,8 @@ def run_hessian(m, shots, solver, C, C0, repeats=2):
     shape = tuple(m.shape(as_grid=True))
     rng = np.random.default_rng(2029)
     m1 = 0.01 * gaussian_filter(rng.standard_normal(shape), 4.0).reshape(-1) / np.asarray(C0).reshape(-1) ** 2
-    out = {"shots": len(shots), "grid": [int(v) for v in shape], "nsteps": int(plan.nsteps), "tile_x": int(plan.tile_x)}
+    out = {"shots": len(shots), "grid": [int(v) for v in shape], "nsteps": int(plan.nsteps), "tile_x": int(plan.tile_x),
+           "schedule": plan.gradient_schedule, "shots_per_launch": plan.shots_per_launch}
     for name, fn in (("gradient", plan.gradient), ("born", lambda: plan.born(m1)),
                      ("hessian", lambda: plan.hessian(m1))):
         fn()
@@ -415,7 +417,7 @@ def _main(argv=None):
     ap.add_argument("workload", choices=["cfg1", "cfg4", "cfg5", "hessian", "gn", "steps2d", "steps3d"])
     ap.add_argument("--shots-per-launch", type=int, default=None)
     ap.add_argument("--schedule", default="auto", choices=["checkpoint", "store", "auto"],
-                    help="cfg5 / gn: gradient schedule of the batched objective")
+                    help="cfg5 / gn / hessian: gradient schedule of the batched plans")
     ap.add_argument("--krylov", type=int, default=5, help="gn: GMRES iterations per Gauss-Newton step")
     ap.add_argument("--iterations", type=int, default=20)
     ap.add_argument("--shots", type=int, default=None, help="default 256 (cfg4), 128 (cfg5)")
@@ -440,7 +442,8 @@ def _main(argv=None):
         print(json.dumps(out))
         return
     if a.workload == "hessian":
-        m, shots, solver, C, C0 = cfg2(scale=a.scale, nshots=a.shots or 64, nsteps=a.nsteps)
+        m, shots, solver, C, C0 = cfg2(scale=a.scale, nshots=a.shots or 64, nsteps=a.nsteps,
+                                       shots_per_launch=a.shots_per_launch, gradient_schedule=a.schedule)
         out = run_hessian(m, shots, solver, C, C0)
         out.update(workload="hessian on the cfg2 model", scale=a.scale)
         print(json.dumps(out))
