@@ -912,7 +912,14 @@ struct PlanT final : public pysit_plan {
             cudaEventRecord(ev_fork, s);
             cudaStreamWaitEvent(aux, ev_fork, 0);
         }
-        if (rec) {
+#ifndef PGB_FUSED_REC
+#define PGB_FUSED_REC 1
+#endif
+        // the recorder rides as extra leading blocks of the interior kernel (they read u_k,
+        // which the step leaves alone, and exit at once); as a kernel of its own ahead of the
+        // shell kernel it held the shell back until the interior kernel's blocks retired
+        const bool fused_rec = PGB_FUSED_REC && rec && ntask2d[0] > 0;
+        if (rec && !fused_rec) {
             record_kernel<T><<<recb, bz, 0, side>>>(q);
             ++launches;
         }
@@ -921,7 +928,9 @@ struct PlanT final : public pysit_plan {
             ++launches;
         }
         if (ntask2d[0] > 0) {
-            ctr_next[0] += launch_wave2d_warp_tasks<T, RR, MODE, 0>(q, tk, ntask2d[0], nb[0], s);
+            WaveParams<T> qi = q;
+            qi.rec.blocks = fused_rec ? recb : 0;
+            ctr_next[0] += launch_wave2d_warp_tasks<T, RR, MODE, 0>(qi, tk, ntask2d[0], nb[0], s);
             ++launches;
         }
         if (fork) {

@@ -469,7 +469,7 @@ __global__ void __launch_bounds__(kWarps * 32, (MinBlocks<T, KIND>::value))
     wave2d_warp_kernel(const WaveParams<T> p, const int* __restrict__ tasks, int ntasks, int rec_blocks) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     if ((int)blockIdx.x < rec_blocks) {
-        if (MODE == kFwd) record_block(p, blockIdx.x);
+        if (MODE != kAdj) record_block(p, blockIdx.x);
         return;
     }
     using G = Ring<T, R, MODE, KIND>;
@@ -539,7 +539,7 @@ int occupancy() {
 template <typename T, int R, int MODE, int KIND>
 long long launch_wave2d_warp_tasks(const WaveParams<T>& p, const int* tasks, int ntasks, int blocks,
                                    cudaStream_t s) {
-    const int rec = MODE == kFwd && KIND == 0 ? p.rec.blocks : 0;
+    const int rec = MODE != kAdj && KIND == 0 ? p.rec.blocks : 0;
     wave2d_warp_kernel<T, R, MODE, KIND>
         <<<rec + blocks, kWarps * 32, Ring<T, R, MODE, KIND>::bytes, s>>>(p, tasks, ntasks, rec);
     // counter values the launch consumes: one per task plus one final fetch per warp

@@ -343,7 +343,8 @@ def run_hessian(m, shots, solver, C, C0, repeats=2):
     return out
 
 
-def run_steps(workload="cfg2", scale=1.0, nshots=None, nsteps=64, shots_per_launch=None, reps=32):
+def run_steps(workload="cfg2", scale=1.0, nshots=None, nsteps=64, shots_per_launch=None, reps=32,
+              schedule="checkpoint"):
     """Per-launch times of the three step kernels (forward, recompute, adjoint) of a workload's
     first shot group, each timed alone with CUDA events (pysit_plan_step_loop), with the
     algorithmic bytes of the step and Gcell/s (a benchmarking aid for profiling)."""
@@ -358,7 +359,8 @@ def run_steps(workload="cfg2", scale=1.0, nshots=None, nsteps=64, shots_per_laun
         m, shots, solver, C, C0 = cfg3(scale=scale, nshots=nshots or 1, nsteps=nsteps)
         pml_extra = (8, 8)  # Phi_x, Phi_y, Phi_z, psi in and out
     solver.model_parameters = solver.ModelParameters(m, {"C": C0})
-    plan = WavePlan(solver, shots, shots_per_launch=shots_per_launch or len(shots), gradient_schedule="checkpoint")
+    # (with the kept schedule the recompute-mode launches also record traces, as its forward sweep does)
+    plan = WavePlan(solver, shots, shots_per_launch=shots_per_launch or len(shots), gradient_schedule=schedule)
     plan.forward()
     torch.cuda.synchronize()
     n_all = int(np.prod(m.shape(include_bc=True, as_grid=True)))
@@ -367,7 +369,7 @@ def run_steps(workload="cfg2", scale=1.0, nshots=None, nsteps=64, shots_per_laun
     w = 4 if solver.precision == "single" else 8
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     out = {"workload": workload, "scale": scale, "grid": [int(v) for v in m.shape(include_bc=True, as_grid=True)],
-           "shots_per_launch": plan.shots_per_launch, "modes": {}}
+           "shots_per_launch": plan.shots_per_launch, "schedule": plan.gradient_schedule, "modes": {}}
     for mode, name, extra in ((0, "forward", 0), (1, "recompute", 1), (2, "adjoint", 3)):
         plan.step_loop(mode, 4)
         torch.cuda.synchronize()
@@ -438,7 +440,8 @@ def _main(argv=None):
         return
     if a.workload in ("steps2d", "steps3d"):
         out = run_steps("cfg2" if a.workload == "steps2d" else "cfg3", scale=a.scale, nshots=a.shots,
-                        nsteps=a.nsteps, shots_per_launch=a.shots_per_launch)
+                        nsteps=a.nsteps, shots_per_launch=a.shots_per_launch,
+                        schedule="store" if a.schedule == "store" else "checkpoint")
         print(json.dumps(out))
         return
     if a.workload == "hessian":
