@@ -22,7 +22,8 @@ No public dataset is involved: each model is generated from a named seed.
 [--nsteps N] [--plain]`` runs the FWI and prints one JSON line (objective history,
 relative L2 error of the final model, wall time); ``... cfg4`` times the uneven
 batch, grid by grid and as one group; ``... steps2d`` / ``steps3d`` time the three
-step kernels of the cfg2 / cfg3 grids alone; ``... hessian`` times the gradient, Born
+step kernels of the cfg2 / cfg3 grids alone; ``... gradient`` times the cfg2 gradient alone
+(inside an NVTX range for profilers); ``... hessian`` times the gradient, Born
 modelling and the Gauss-Newton Hessian application of the cfg2 workload; ``... gn``
 runs Gauss-Newton iterations (GMRES on the GPU Hessian) on the cfg5 model.
 """
@@ -35,7 +36,7 @@ from scipy.ndimage import gaussian_filter
 
 from . import core, solvers
 
-__all__ = ["layered_model", "cfg1", "run_cfg1", "cfg2", "cfg3", "cfg4", "cfg5", "run_lbfgs", "run_uneven_batch", "run_hessian",
+__all__ = ["layered_model", "cfg1", "run_cfg1", "run_gradient", "cfg2", "cfg3", "cfg4", "cfg5", "run_lbfgs", "run_uneven_batch", "run_hessian",
            "run_gauss_newton", "run_steps"]
 
 
@@ -343,6 +344,41 @@ def run_hessian(m, shots, solver, C, C0, repeats=2):
     return out
 
 
+def run_gradient(scale=1.0, nshots=64, nsteps=4000, shots_per_launch=None, schedule="auto", repeats=1):
+    """The 2D batched gradient alone: observed data on the true model, one warm-up gradient at
+    the start model, then `repeats` gradients inside the NVTX range "timed_gradient" (a profiler
+    can select exactly their launches).  Returns seconds per gradient and shots/s."""
+    import time
+
+    import torch
+
+    from .autograd import resample_linear
+    from .engine import WavePlan
+
+    m, shots, solver, C, C0 = cfg2(scale=scale, nshots=nshots, nsteps=nsteps, gradient_schedule=schedule)
+    solver.model_parameters = solver.ModelParameters(m, {"C": C})
+    obs = WavePlan(solver, shots, forward_only=True).forward().clone()
+    ts_true = solver.ts()
+    torch.cuda.empty_cache()
+    solver.model_parameters = solver.ModelParameters(m, {"C": C0})
+    plan = WavePlan(solver, shots, shots_per_launch=shots_per_launch)
+    plan.autotune()
+    plan.dobs.copy_(resample_linear(obs, ts_true, solver.ts()))
+    del obs
+    plan.gradient()
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push("timed_gradient")
+    t0 = time.perf_counter()
+    for _ in range(repeats):
+        plan.gradient()
+    torch.cuda.synchronize()
+    t = (time.perf_counter() - t0) / repeats
+    torch.cuda.nvtx.range_pop()
+    return {"shots": nshots, "nsteps": int(plan.nsteps), "schedule": plan.gradient_schedule,
+            "shots_per_launch": plan.shots_per_launch, "tile_x": plan.tile_x, "seconds": t,
+            "shots_per_s": nshots / t, "launches": plan.launches(), "status": plan.status()}
+
+
 def run_steps(workload="cfg2", scale=1.0, nshots=None, nsteps=64, shots_per_launch=None, reps=32,
               schedule="checkpoint"):
     """Per-launch times of the three step kernels (forward, recompute, adjoint) of a workload's
@@ -416,7 +452,7 @@ def _main(argv=None):
     import json
 
     ap = argparse.ArgumentParser(prog="python -m pysit_gb300.workloads")
-    ap.add_argument("workload", choices=["cfg1", "cfg4", "cfg5", "hessian", "gn", "steps2d", "steps3d"])
+    ap.add_argument("workload", choices=["cfg1", "cfg4", "cfg5", "gradient", "hessian", "gn", "steps2d", "steps3d"])
     ap.add_argument("--shots-per-launch", type=int, default=None)
     ap.add_argument("--schedule", default="auto", choices=["checkpoint", "store", "auto"],
                     help="cfg5 / gn / hessian: gradient schedule of the batched plans")
@@ -431,6 +467,12 @@ def _main(argv=None):
     if a.workload == "cfg4":
         out = run_uneven_batch(cfg4(scale=a.scale, nshots=a.shots or 256))
         out.update(workload="cfg4", scale=a.scale)
+        print(json.dumps(out))
+        return
+    if a.workload == "gradient":
+        out = run_gradient(scale=a.scale, nshots=a.shots or 64, nsteps=a.nsteps, shots_per_launch=a.shots_per_launch,
+                           schedule=a.schedule)
+        out.update(workload="cfg2 gradient")
         print(json.dumps(out))
         return
     if a.workload == "cfg1":
