@@ -332,7 +332,10 @@ def main():
     h2d = obs_host.numel() * obs_host.element_size() + C_host.numel() * 4
     d2h = g.numel() * 4 + 8
 
-    cells_per_grad = 3 * n_all * solver.nsteps * args.shots
+    # cell updates of one gradient: forward, recompute and adjoint sweeps (checkpointed), or
+    # forward and adjoint (dWaveOp kept)
+    sweeps = 2 if config.get("gradient_schedule") == "store" else 3
+    cells_per_grad = sweeps * n_all * solver.nsteps * args.shots
     peak, peak_kind = _peaks()
     dom_name = max(modes, key=lambda k: modes[k]["launch_ms"])  # each mode runs nsteps times per gradient
     dom = modes[dom_name]
