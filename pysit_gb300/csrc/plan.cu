@@ -333,6 +333,7 @@ struct PlanT final : public pysit_plan {
     // ---- acquisition (host) ----------------------------------------------------
     std::vector<CSRBox> src_inj, rec_inj;
     int rec_box_max = 0;              // largest receiver injection box (cells) over the shots
+    bool rec_in_shell = false;        // 2D: every receiver box lies in cells of PML-shell tasks only
     std::vector<int> rec_rows;        // [nshots*nrec+1]
     std::vector<long long> rec_off;   // internal offsets
     std::vector<double> rec_ws;       // sampling weights
@@ -450,6 +451,17 @@ struct PlanT final : public pysit_plan {
         rec_box_max = 0;
         for (auto& b : rec_inj)
             rec_box_max = std::max(rec_box_max, (b.box[1] - b.box[0]) * (b.box[3] - b.box[2]) * (b.box[5] - b.box[4]));
+        if (dim == 2) {
+            // the bounds of the interior tasks (as build_tasks2d_ draws them)
+            const int xa = pl[0] > 0 ? pl[0] + R : 1, xb = pr[0] > 0 ? nx - pr[0] - R : nx - 1;
+            const int za = ((pl[2] > 0 ? pl[2] + R : 1) + 3) / 4 * 4, zb = (pr[2] > 0 ? nz - pr[2] - R : nz - 1) / 4 * 4;
+            rec_in_shell = !rec_inj.empty();
+            for (auto& b : rec_inj) {
+                if (b.box[1] <= b.box[0] || b.box[5] <= b.box[4]) continue;  // no taps
+                const bool zout = b.box[5] <= za || b.box[4] >= zb, xout = b.box[1] <= xa || b.box[0] >= xb;
+                if (!(zout || xout || xa >= xb || za >= zb)) rec_in_shell = false;
+            }
+        }
         rc = build_recording(d);
         if (rc) return rc;
         src_amp.assign(d.src_amp, d.src_amp + (size_t)nshots * nsteps * nsrc);
@@ -933,16 +945,22 @@ struct PlanT final : public pysit_plan {
             ctr_next[0] += launch_wave2d_warp_tasks<T, RR, MODE, 0>(qi, tk, ntask2d[0], nb[0], s);
             ++launches;
         }
+        // the adjoint source adds to cells the shell kernel has written; when every receiver
+        // box lies in shell cells it follows the shell kernel on its stream, overlapping the
+        // interior kernel's tail, else it waits for both
+        const bool scatter_side = scatter && fork && rec_in_shell;
+        auto do_scatter = [&](cudaStream_t st) {
+            q.inj.on = 1;
+            const long long n = (long long)q.nshot * rec_box_max;
+            inject_scatter2d_kernel<T><<<(int)std::min<long long>((n + 255) / 256, 4096), 256, 0, st>>>(q, rec_box_max);
+            ++launches;
+        };
+        if (scatter_side) do_scatter(side);
         if (fork) {
             cudaEventRecord(ev_join, aux);
             cudaStreamWaitEvent(s, ev_join, 0);
         }
-        if (scatter) {
-            q.inj.on = 1;
-            const long long n = (long long)q.nshot * rec_box_max;
-            inject_scatter2d_kernel<T><<<(int)std::min<long long>((n + 255) / 256, 4096), 256, 0, s>>>(q, rec_box_max);
-            ++launches;
-        }
+        if (scatter && !scatter_side) do_scatter(s);
     }
 
     // One 3D step: interior kernel on s, PML-shell kernel (and the trace recorder)
