@@ -126,8 +126,12 @@ class FWIMisfit:
         dt, nsteps = self._set_model(C_dev)
         plan = plan_for(self.solver, self.shots, self.imaging_period, **self.plan_kw)
         self._last_plan = weakref.ref(plan)
-        obs = self.observed.to("cuda", non_blocking=True).to(plan.tdtype)
-        plan.dobs.copy_(resample_linear(obs, self.ts_observed, self.solver.ts()))
+        # observed traces to the device and onto the plan's time axis, a few shots at a time
+        # (bounded temporaries beside a plan that may hold most of the device memory)
+        ts = self.solver.ts()
+        for i in range(0, plan.nshots, 16):
+            obs = self.observed[i:i + 16].to("cuda", non_blocking=True).to(plan.tdtype)
+            plan.dobs[i:i + 16].copy_(resample_linear(obs, self.ts_observed, ts))
         if want_grad:
             g, rn = plan.gradient()
             # flat, x-major like PySIT's model vectors: takes the caller's shape of C
