@@ -161,3 +161,31 @@ def test_bulk_copy_2d_variant_agrees(monkeypatch, precision, tol, schedule):
     assert np.linalg.norm(b[0] - a[0]) <= tol * np.linalg.norm(a[0])
     assert np.linalg.norm(b[2] - a[2]) <= tol * np.linalg.norm(a[2])
     assert b[3] == 0
+
+
+def test_fp32_gradient_of_the_2d_workload_within_1e3_of_fp64():
+    """The bench's claim at a size the FP64 path finishes in seconds: the 2D workload at a
+    quarter of its size (288 x 96 cells + 10-cell PML, 16 shots, 1000 steps, order 8), kept
+    schedule, FP32 against FP64 (the FP64 path is held to the oracle by the pipeline tests)."""
+    import torch
+    from pysit_gb300 import workloads
+    from pysit_gb300.autograd import resample_linear
+    out = {}
+    for prec in ("double", "single"):
+        m, shots, solver, C, C0 = workloads.cfg2(scale=0.25, nshots=16, nsteps=1000, precision=prec,
+                                                 gradient_schedule="store")
+        solver.model_parameters = solver.ModelParameters(m, {"C": C})
+        obs = WavePlan(solver, shots, forward_only=True).forward().double().clone()
+        ts = solver.ts()
+        solver.model_parameters = solver.ModelParameters(m, {"C": C0})
+        plan = WavePlan(solver, shots)
+        plan.dobs.copy_(resample_linear(obs, ts, solver.ts()))
+        g, rn = plan.gradient()
+        out[prec] = (g.cpu().numpy().copy(), float(rn.item()))
+        assert plan.status() == 0
+        del plan
+        torch.cuda.empty_cache()
+    g64, r64 = out["double"]
+    g32, r32 = out["single"]
+    assert np.linalg.norm(g32 - g64) <= 1e-3 * np.linalg.norm(g64)
+    assert r32 == pytest.approx(r64, rel=1e-3)
