@@ -171,15 +171,17 @@ def test_fp32_gradient_of_the_2d_workload_within_1e3_of_fp64():
     from pysit_gb300 import workloads
     from pysit_gb300.autograd import resample_linear
     out = {}
+    obs = ts = None  # observed data of the FP64 run, used by both
     for prec in ("double", "single"):
         m, shots, solver, C, C0 = workloads.cfg2(scale=0.25, nshots=16, nsteps=1000, precision=prec,
                                                  gradient_schedule="store")
-        solver.model_parameters = solver.ModelParameters(m, {"C": C})
-        obs = WavePlan(solver, shots, forward_only=True).forward().double().clone()
-        ts = solver.ts()
+        if obs is None:
+            solver.model_parameters = solver.ModelParameters(m, {"C": C})
+            obs = WavePlan(solver, shots, forward_only=True).forward().double().clone()
+            ts = solver.ts()
         solver.model_parameters = solver.ModelParameters(m, {"C": C0})
         plan = WavePlan(solver, shots)
-        plan.dobs.copy_(resample_linear(obs, ts, solver.ts()))
+        plan.dobs.copy_(resample_linear(obs, ts, solver.ts()).to(plan.dobs.dtype))
         g, rn = plan.gradient()
         out[prec] = (g.cpu().numpy().copy(), float(rn.item()))
         assert plan.status() == 0
