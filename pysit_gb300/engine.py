@@ -27,7 +27,7 @@ _DESC_AXIS = {1: [2], 2: [0, 2], 3: [0, 1, 2]}  # mesh axis -> (x, y, z) slot of
 # mode), per (dim, order, padded grid, dtype, shots per launch, psi form, schedule); later
 # plans of the same configuration start from them
 _TUNED = {}
-TILE_CANDIDATES = {2: (8, 16, 32, 64), 3: (16, 32, 64, 128)}
+TILE_CANDIDATES = {2: (8, 16, 32, 64), 3: (8, 16, 32, 64)}
 
 
 def padded_cells(mesh, cells):

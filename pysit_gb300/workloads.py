@@ -23,7 +23,8 @@ No public dataset is involved: each model is generated from a named seed.
 relative L2 error of the final model, wall time); ``... cfg4`` times the uneven
 batch, grid by grid and as one group; ``... steps2d`` / ``steps3d`` time the three
 step kernels of the cfg2 / cfg3 grids alone; ``... gradient`` times the cfg2 gradient alone
-(inside an NVTX range for profilers); ``... hessian`` times the gradient, Born
+(inside an NVTX range for profilers), ``... gradient3d`` the cfg3 gradient; ``... hessian``
+times the gradient, Born
 modelling and the Gauss-Newton Hessian application of the cfg2 workload; ``... gn``
 runs Gauss-Newton iterations (GMRES on the GPU Hessian) on the cfg5 model.
 """
@@ -36,7 +37,7 @@ from scipy.ndimage import gaussian_filter
 
 from . import core, solvers
 
-__all__ = ["layered_model", "cfg1", "run_cfg1", "run_gradient", "cfg2", "cfg3", "cfg4", "cfg5", "run_lbfgs", "run_uneven_batch", "run_hessian",
+__all__ = ["layered_model", "cfg1", "run_cfg1", "run_gradient", "run_gradient3d", "cfg2", "cfg3", "cfg4", "cfg5", "run_lbfgs", "run_uneven_batch", "run_hessian",
            "run_gauss_newton", "run_steps"]
 
 
@@ -379,6 +380,44 @@ def run_gradient(scale=1.0, nshots=64, nsteps=4000, shots_per_launch=None, sched
             "shots_per_s": nshots / t, "launches": plan.launches(), "status": plan.status()}
 
 
+def run_gradient3d(scale=1.0, nshots=8, nsteps=3000, autotune=True):
+    """The 3D gradient (cfg3, consistent psi form, checkpointed, one shot per launch): observed
+    data on the true model, one warm-up gradient at the start model, then one timed gradient
+    (CUDA events).  Returns seconds, shots/s, Gcell/s of the three sweeps and the tuning."""
+    import time
+
+    import torch
+
+    from .autograd import resample_linear
+    from .engine import WavePlan
+
+    m, shots, solver, C, C0 = cfg3(scale=scale, nshots=nshots, nsteps=nsteps)
+    solver.model_parameters = solver.ModelParameters(m, {"C": C})
+    ts_obs = solver.ts()
+    obs = WavePlan(solver, shots, shots_per_launch=1, forward_only=True).forward().clone()
+    torch.cuda.empty_cache()
+    solver.model_parameters = solver.ModelParameters(m, {"C": C0})
+    plan = WavePlan(solver, shots, shots_per_launch=1)
+    tune = plan.autotune() if autotune else {"chosen": plan.tile_x}
+    plan.dobs.copy_(resample_linear(obs, ts_obs, solver.ts()))
+    del obs
+    plan.gradient()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0 = time.perf_counter()
+    e0.record()
+    plan.gradient()
+    e1.record()
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / 1e3
+    cells = int(np.prod(m.shape(include_bc=True, as_grid=True)))
+    return {"shots": nshots, "nsteps": int(plan.nsteps), "grid": [int(v) for v in m.shape(include_bc=True, as_grid=True)],
+            "checkpoint_every": plan.checkpoint_every, "workspace_gb": plan.workspace_bytes / 1e9,
+            "tile_x": tune["chosen"], "tune_ms": {str(k): v for k, v in tune.get("ms", {}).items()},
+            "seconds": t, "wall_s": time.perf_counter() - t0, "shots_per_s": nshots / t,
+            "gcell_per_s": 3 * cells * plan.nsteps * nshots / t / 1e9, "status": plan.status()}
+
+
 def run_steps(workload="cfg2", scale=1.0, nshots=None, nsteps=64, shots_per_launch=None, reps=32,
               schedule="checkpoint"):
     """Per-launch times of the three step kernels (forward, recompute, adjoint) of a workload's
@@ -452,7 +491,8 @@ def _main(argv=None):
     import json
 
     ap = argparse.ArgumentParser(prog="python -m pysit_gb300.workloads")
-    ap.add_argument("workload", choices=["cfg1", "cfg4", "cfg5", "gradient", "hessian", "gn", "steps2d", "steps3d"])
+    ap.add_argument("workload", choices=["cfg1", "cfg4", "cfg5", "gradient", "gradient3d", "hessian", "gn", "steps2d",
+                                         "steps3d"])
     ap.add_argument("--shots-per-launch", type=int, default=None)
     ap.add_argument("--schedule", default="auto", choices=["checkpoint", "store", "auto"],
                     help="cfg5 / gn / hessian: gradient schedule of the batched plans")
@@ -473,6 +513,11 @@ def _main(argv=None):
         out = run_gradient(scale=a.scale, nshots=a.shots or 64, nsteps=a.nsteps, shots_per_launch=a.shots_per_launch,
                            schedule=a.schedule)
         out.update(workload="cfg2 gradient")
+        print(json.dumps(out))
+        return
+    if a.workload == "gradient3d":
+        out = run_gradient3d(scale=a.scale, nshots=a.shots or 8, nsteps=a.nsteps if a.nsteps != 4000 else 3000)
+        out.update(workload="cfg3 gradient")
         print(json.dumps(out))
         return
     if a.workload == "cfg1":
