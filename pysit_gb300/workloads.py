@@ -211,7 +211,7 @@ def run_lbfgs(m, shots, solver, C, C0, iterations=20, memory_length=10, batched=
                       "shots_per_launch": objective.last_plan.shots_per_launch} if objective.last_plan else None)}
 
 
-def cfg4(scale=1.0, nshots=256, order=6, precision="single", seed=2028, cfl=0.4):
+def cfg4(scale=1.0, nshots=256, order=6, precision="single", seed=2028, cfl=0.4, gradient_schedule="checkpoint"):
     """The uneven batch: a list of three grids, each (mesh, shots, solver, C, C0, record_steps).
 
     One model (the cfg2 model at 12.5 m) sampled every 4th / 2nd / 1st cell; shots split as
@@ -244,7 +244,8 @@ def cfg4(scale=1.0, nshots=256, order=6, precision="single", seed=2028, cfl=0.4)
             shots.append(core.Shot(src, rec))
         solver = solvers.ConstantDensityAcousticWave(m, spatial_accuracy_order=order, trange=(0.0, T),
                                                      kernel_implementation="cuda", precision=precision,
-                                                     cfl_safety=cfl, checkpoint_every=64, autotune=True)
+                                                     cfl_safety=cfl, checkpoint_every=64, autotune=True,
+                                                     gradient_schedule=gradient_schedule)
         record = rng.integers(nsteps // 2, nsteps + 1, size=ns)
         out.append((m, shots, solver, C.reshape(-1, 1), C0.reshape(-1, 1), record))
     return out
@@ -259,8 +260,17 @@ def run_uneven_batch(grids, repeats=2):
 
     from .engine import PlanGroup, WavePlan
 
-    plans = []
-    for m, shots, solver, C, C0, record in grids:
+    # plans are built largest first (cells x steps x shots): with an 'auto' schedule the grid
+    # with the most work gets first claim on the memory that keeping dWaveOp needs
+    def work(g):
+        m, shots, solver, C, C0, record = g
+        solver.model_parameters = solver.ModelParameters(m, {"C": C0})
+        return int(np.prod(m.shape(include_bc=True, as_grid=True))) * solver.nsteps * len(shots)
+
+    order = sorted(range(len(grids)), key=lambda i: -work(grids[i]))
+    built = {}
+    for i in order:
+        m, shots, solver, C, C0, record = grids[i]
         solver.model_parameters = solver.ModelParameters(m, {"C": C})
         obs_plan = WavePlan(solver, shots, forward_only=True)
         obs = obs_plan.forward().clone()
@@ -275,7 +285,8 @@ def run_uneven_batch(grids, repeats=2):
         p.dobs.copy_(resample_linear(obs, ts_true, solver.ts()))
         del obs
         torch.cuda.empty_cache()
-        plans.append(p)
+        built[i] = p
+    plans = [built[i] for i in range(len(grids))]
     nshots = sum(len(g[1]) for g in grids)
     group = PlanGroup(plans)
     for p in plans:
@@ -296,7 +307,8 @@ def run_uneven_batch(grids, repeats=2):
     status = [p.status() for p in plans]
     return {"shots": nshots, "grids": [[int(s) for s in g[0].shape(as_grid=True)] for g in grids],
             "shots_per_grid": [len(g[1]) for g in grids], "nsteps": [int(p.nsteps) for p in plans],
-            "tile_x": [int(p.tile_x) for p in plans],
+            "tile_x": [int(p.tile_x) for p in plans], "schedules": [p.gradient_schedule for p in plans],
+            "shots_per_launch": [int(p.shots_per_launch) for p in plans],
             "sequential_s": t_seq, "group_s": t_grp, "shots_per_s_sequential": nshots / t_seq,
             "shots_per_s_group": nshots / t_grp, "group_speedup": t_seq / t_grp, "status": status}
 
@@ -505,7 +517,7 @@ def _main(argv=None):
     ap.add_argument("--verbose", action="store_true")
     a = ap.parse_args(argv)
     if a.workload == "cfg4":
-        out = run_uneven_batch(cfg4(scale=a.scale, nshots=a.shots or 256))
+        out = run_uneven_batch(cfg4(scale=a.scale, nshots=a.shots or 256, gradient_schedule=a.schedule))
         out.update(workload="cfg4", scale=a.scale)
         print(json.dumps(out))
         return
