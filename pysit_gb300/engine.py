@@ -251,7 +251,7 @@ class WavePlan:
             return "checkpoint"
         lanes = self.lanes  # lanes are not split further: two half-size lanes measured slower in 2D
         per_lane = -(-self.nshots // lanes)           # shots of the largest lane
-        glane = min(gmax // lanes, per_lane)
+        glane = max(1, min(gmax // lanes, per_lane))
         launches = -(-per_lane // glane)
         G = -(-per_lane // launches)
         while G > 1 and self._workspace_for(lib, d, G, True, lanes) > budget:
