@@ -113,3 +113,31 @@ def test_cuda_path_has_no_cpu_fallback(monkeypatch):
     monkeypatch.setattr(torch.cuda, "is_available", lambda: False)
     with pytest.raises(_native.PysitCudaError):
         _native.require_cuda()
+
+
+def test_observed_data_fingerprint_sees_in_place_edits():
+    """The device copy of the recorded traces is reused while every shot holds the same array
+    with the same sampled values; an in-place edit of the array changes its fingerprint."""
+    from pysit_gb300.engine import _fingerprint
+    rng = np.random.default_rng(0)
+    a = rng.standard_normal((4000, 1152))
+    fp = _fingerprint(a)
+    assert _fingerprint(a) == fp
+    a *= 2.0
+    assert _fingerprint(a) != fp
+    b = a.copy()
+    b[-1, 5] += 1.0          # last row
+    assert _fingerprint(b) != _fingerprint(a)
+    c = a.copy()
+    c.reshape(-1)[4099 * 7] += 1.0   # a sampled element
+    assert _fingerprint(c) != _fingerprint(a)
+
+
+def test_solver_rejects_unknown_gradient_schedule():
+    d = api.RectangularDomain((0.0, 100.0, api.PML(20.0, 100.0), api.PML(20.0, 100.0)),
+                              (0.0, 100.0, api.PML(20.0, 100.0), api.PML(20.0, 100.0)))
+    m = api.CartesianMesh(d, 11, 11)
+    with pytest.raises(ValueError):
+        api.ConstantDensityAcousticWave(m, kernel_implementation="cuda", gradient_schedule="fast")
+    s = api.ConstantDensityAcousticWave(m, kernel_implementation="cuda", gradient_schedule="auto")
+    assert s.gradient_schedule == "auto"
