@@ -323,9 +323,9 @@ struct PlanT final : public pysit_plan {
     int ntask2d[2] = {0, 0};     // tasks of each kind
     std::vector<int> tasks3d;    // [ntasks][6] block tasks of the 3D sweep: interior first, then shell
     int ntask3d[2] = {0, 0};
-    int blocks2d[3][2] = {{1, 1}, {1, 1}, {1, 1}};  // resident task blocks per mode and kind (whole GPU)
+    int blocks2d[4][2] = {{1, 1}, {1, 1}, {1, 1}, {1, 1}};  // resident task blocks per mode and kind (whole GPU)
     unsigned long long ctr_next[2] = {0, 0};  // task-counter values the next 2D launch starts at
-    double shell_frac[3] = {0.0, 0.0, 0.0};  // 2D, per mode: share of the resident blocks given to the
+    double shell_frac[4] = {0.0, 0.0, 0.0, 0.0};  // 2D, per mode: share of the resident blocks given to the
                                  // PML-shell kernel (0: each kernel is sized for the whole GPU and they
                                  // overlap only where one runs out)
     cudaStream_t aux = nullptr;  // second stream of the 2D step (shell kernel beside the interior one)
@@ -810,7 +810,7 @@ struct PlanT final : public pysit_plan {
         if (dim == 2) {
             wave2d_prepare();
             wave2d_warp_prepare();
-            for (int m = 0; m < 3; ++m)
+            for (int m = 0; m < 4; ++m)
                 for (int k = 0; k < 2; ++k) blocks2d[m][k] = wave2d_warp_blocks((int)sizeof(T), order, m, k);
         }
         if (dim >= 2) {
@@ -1010,6 +1010,7 @@ struct PlanT final : public pysit_plan {
         if (dim == 2 && warp2d) {                                              \
             if (mode == kFwd) launch2d<RR, kFwd>(p, s);                        \
             else if (mode == kRecomp) launch2d<RR, kRecomp>(p, s);             \
+            else if (mode == kBorn) launch2d<RR, kBorn>(p, s);                 \
             else launch2d<RR, kAdj>(p, s);                                     \
         } else if (dim == 2) {                                                 \
             if (mode == kFwd) launch_wave2d<T, RR, kFwd>(p, bz, s);            \
@@ -1202,9 +1203,15 @@ struct PlanT final : public pysit_plan {
             set_inject(p1, true, g0, k, nullptr);  // valid tables, switched off: u1 has no source
             p1.inj.on = 0;
             set_recording(p1, g0, gn, tr + (long long)k * nrec);
-            launch(p1, kFwd, s);
-            born_source_kernel<T><<<nb, 128, 0, s>>>(p1, dim, at<T>(off.m1), dw);
-            ++launches;
+            if (dim == 2 && warp2d) {  // the Born source read inside the u1 step
+                p1.dw_in = dw;
+                p1.m1 = at<T>(off.m1);
+                launch(p1, kBorn, s);
+            } else {
+                launch(p1, kFwd, s);
+                born_source_kernel<T><<<nb, 128, 0, s>>>(p1, dim, at<T>(off.m1), dw);
+                ++launches;
+            }
             advance(u0);
             advance(u1);
         }

@@ -73,6 +73,7 @@ enum StepMode : int {
     kFwd = 0,     // forward step; records traces of u_k
     kRecomp = 1,  // forward recompute; writes the imaging operand dWaveOp_k
     kAdj = 2,     // adjoint step driven by the residual; accumulates ic += q_k * dWaveOp_k
+    kBorn = 3,    // 2D: scattered-field step with the Born source -m1 dWaveOp0_k inside the stencil
 };
 
 // Injection operator of one step: per shot a box of cells [x0,x1) x [y0,y1) x [z0,z1)
@@ -136,6 +137,8 @@ struct WaveParams {
     const T* dw_in;          // kAdj: imaging operand of this step
     T* ic;                   // kAdj: imaging accumulator (shot 0 base)
     int image;               // kAdj: accumulate this step
+    const T* m1;             // kBorn: edge-padded model perturbation (internal layout, shared by the shots);
+                             // dw_in holds dWaveOp0_k
     int* err;                // device error word (PGB_ERR_* bits), may be NULL
     int psi_c2;              // 3D: 1 = C^2 multiplies sigma_x sigma_y sigma_z psi (the reference), 0 = not
     int nan_check;           // kRecomp: flag non-finite u_{k+1} as kFwd does (a forward sweep that keeps dWaveOp)

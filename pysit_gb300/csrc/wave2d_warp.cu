@@ -1,16 +1,20 @@
 // Batched 2D leapfrog step: persistent warps fed by per-warp shared-memory row
-// rings (forward, recompute, adjoint).
+// rings (forward, recompute, adjoint, Born scattered field).
 //
 // Same maths as the reference step cda_time_scalar_2D (pysit/solvers/
 // constant_density_acoustic/time/scalar/constant_density_acoustic_time_scalar_2D.h:88-179)
 // with the fusions of the batched pipeline:
-//   kFwd    (trace recording of u_k runs as a kernel of its own beside these);
+//   kFwd    (with kRecomp and kBorn: leading blocks of the interior kernel record the
+//           traces of u_k);
 //   kRecomp the imaging operand dWaveOp_k (constant_density_acoustic_base.py:24-40)
 //           from the stencil's own bracket F: C^2 F where the step and mesh
 //           sigmas agree, plus the sigma differences elsewhere (the right PML,
 //           whose step profile is read one node further out, _2D.h:143-157);
 //   kAdj    the time-reversed adjoint step with ic += q_k * dWaveOp_k fused
-//           (temporal_modeling.py:312-365).
+//           (temporal_modeling.py:312-365);
+//   kBorn   the scattered field u1 of linearised modelling, its source -m1 dWaveOp0_k
+//           read from the stage like the adjoint's operands and added inside the bracket
+//           (linear_forward_model, temporal_modeling.py:520-535).
 //
 // Work decomposition: a table of warp tasks (x0, x1, zs, ze, kind) covers the
 // padded grid of one shot once.  The warps of the launch are persistent: each
@@ -93,11 +97,11 @@ struct Ring {
     // rows per iteration: the FP32 interior sweeps two rows at a time (the per-row
     // bookkeeping is shared, and the 2R+2 rows of the window are read once)
     static constexpr int RB = sizeof(T) == 4 && KIND == 0 ? PGB_RING_RB : 1;
-    static constexpr int AR = MODE == kAdj && PGB_RING_AHEAD > 2 ? PGB_RING_AHEAD - 1 : PGB_RING_AHEAD;
+    static constexpr int AR = (MODE == kAdj || MODE == kBorn) && PGB_RING_AHEAD > 2 ? PGB_RING_AHEAD - 1 : PGB_RING_AHEAD;
     static constexpr int A = (AR + RB - 1) / RB < 2 ? 2 : (AR + RB - 1) / RB;  // iterations in flight
     static constexpr int NU = 2 * R + RB * A;                    // x-ring slots
     static constexpr bool PML = KIND == 1;
-    static constexpr int NPF = MODE == kAdj ? 4 : 2;             // centre fields per row
+    static constexpr int NPF = MODE == kAdj || MODE == kBorn ? 4 : 2;  // centre fields per row
     static constexpr int PST = RB * (NPF * SEG + (PML ? WS : 0));  // stage (elements)
     // u ring, Phi_x ring (same slot stride, centre at +HZ, so one row offset serves both), stages
     static constexpr int ELEMS = NU * WS * (PML ? 2 : 1) + A * PST;
@@ -180,11 +184,12 @@ __device__ __forceinline__ void sweep(const WaveParams<T>& p, unsigned char* wsm
     const long long sh = (long long)shot * p.fstride;
     T* uprev = p.u_prev + sh;
     const bool img = MODE == kAdj && p.image;
+    const bool ext = img || MODE == kBorn;  // fields 3 and 4 (dWaveOp, ic or m1) ride in the stage
     auto rowoff = [&](int x) { return (long long)(x + kHalo) * p.ldz + kOZ; };
     const int ncen = (ze - zs + G::AL - 1) / G::AL * G::AL;
     const uint32_t bu = (uint32_t)(ncen + 2 * HZ) * TB;
     const uint32_t bc = (uint32_t)ncen * TB;
-    const uint32_t brow = bu + 2 * bc + (img ? 2 * bc : 0) + (PML ? bc + bu : 0);  // bytes per row
+    const uint32_t brow = bu + 2 * bc + (ext ? 2 * bc : 0) + (PML ? bc + bu : 0);  // bytes per row
     auto bytes_it = [&](int it) { return (uint32_t)min(RB, niter - RB * it) * brow; };
 
     // One bulk copy per lane and iteration: lane c copies row r = c % RB of field
@@ -192,19 +197,22 @@ __device__ __forceinline__ void sweep(const WaveParams<T>& p, unsigned char* wsm
     // destination: x-ring slot or stage).
     //   0 u_k -> u ring; 1 u_{k-1}, 2 C^2 -> stage; [3 dWaveOp, 4 ic -> stage];
     //   [PML: Phi_x -> Phi_x ring; Phi_z (halo) -> stage]
-    const int nfield = 3 + (img ? 2 : 0) + (PML ? 2 : 0);
+    const int nfield = 3 + (ext ? 2 : 0) + (PML ? 2 : 0);
     const int ncp = nfield * RB;
     const int cf = lane / RB, cr = lane - cf * RB;
     const T* csrc = nullptr;  // element of row cr (x-ring fields: row cr + R)
     uint32_t cdst = 0, cstep = 0, cbytes = 0;
     bool cring = false;
     {
-        const int cpml = 3 + (img ? 2 : 0);
+        const int cpml = 3 + (ext ? 2 : 0);
         const uint32_t w0 = smem_u32(wsm);
         if (cf == 0) {
             csrc = p.u_cur + sh + rowoff(cr + R) + zs - HZ; cdst = w0 + OFF_U; cstep = SLOT; cbytes = bu; cring = true;
-        } else if (cf == 1 || cf == 2 || (img && (cf == 3 || cf == 4))) {
-            const T* f = cf == 1 ? (const T*)uprev : cf == 2 ? p.c2 : cf == 3 ? p.dw_in + sh : (const T*)p.ic + sh;
+        } else if (cf == 1 || cf == 2 || (ext && (cf == 3 || cf == 4))) {
+            const T* f = cf == 1   ? (const T*)uprev
+                         : cf == 2 ? p.c2
+                         : cf == 3 ? p.dw_in + sh
+                                   : (MODE == kBorn ? p.m1 : (const T*)p.ic + sh);
             csrc = f + rowoff(cr) + zs;
             cdst = w0 + OFF_P + ((cf - 1) * RB + cr) * SEG * TB; cstep = STG; cbytes = bc;
         } else if (PML && cf == cpml) {
@@ -309,7 +317,7 @@ __device__ __forceinline__ void sweep(const WaveParams<T>& p, unsigned char* wsm
             const Vec<T, V> um = lds<T, V>(reinterpret_cast<const T*>(sb + (0 * RB + r) * SEG * TB));
             const Vec<T, V> cc = lds<T, V>(reinterpret_cast<const T*>(sb + (1 * RB + r) * SEG * TB));
             Vec<T, V> dwi, ici;
-            if (MODE == kAdj && img) {
+            if ((MODE == kAdj && img) || MODE == kBorn) {  // for kBorn: dWaveOp0 and m1
                 dwi = lds<T, V>(reinterpret_cast<const T*>(sb + (2 * RB + r) * SEG * TB));
                 ici = lds<T, V>(reinterpret_cast<const T*>(sb + (3 * RB + r) * SEG * TB));
             }
@@ -352,6 +360,7 @@ __device__ __forceinline__ void sweep(const WaveParams<T>& p, unsigned char* wsm
                     F.x += inject_rhs(p.inj, bx, shot, xr, zl + v0);
                     F.y += inject_rhs(p.inj, bx, shot, xr, zl + v0 + 1);
                 }
+                if (MODE == kBorn) F = O::sub(F, O::mul(pr(ici), pr(dwi)));  // rhs = -m1 dWaveOp0
                 const P uo = pr(um), c2 = pr(cc);
                 // interior tasks never touch the outer (Dirichlet) ring: no masks there
                 const bool ok0 = !PML || (xok && zok[v0]), ok1 = !PML || (xok && zok[v0 + 1]);
@@ -416,7 +425,7 @@ __device__ __forceinline__ void sweep(const WaveParams<T>& p, unsigned char* wsm
                     ico.v[v0 + 1] = ic.y;
                 }
             }
-            if (MODE == kFwd || (MODE == kRecomp && p.nan_check)) {  // a NaN or Inf anywhere in the lane's cells survives the sum
+            if (MODE == kFwd || MODE == kBorn || (MODE == kRecomp && p.nan_check)) {  // a NaN or Inf anywhere in the lane's cells survives the sum
                 T sum = T(0);
 #pragma unroll
                 for (int v = 0; v < V; ++v) sum += un.v[v];
@@ -521,8 +530,8 @@ void prep_one() {
 }
 template <typename T, int R>
 void prep_warp() {
-    prep_one<T, R, kFwd, 0>(); prep_one<T, R, kRecomp, 0>(); prep_one<T, R, kAdj, 0>();
-    prep_one<T, R, kFwd, 1>(); prep_one<T, R, kRecomp, 1>(); prep_one<T, R, kAdj, 1>();
+    prep_one<T, R, kFwd, 0>(); prep_one<T, R, kRecomp, 0>(); prep_one<T, R, kAdj, 0>(); prep_one<T, R, kBorn, 0>();
+    prep_one<T, R, kFwd, 1>(); prep_one<T, R, kRecomp, 1>(); prep_one<T, R, kAdj, 1>(); prep_one<T, R, kBorn, 1>();
 }
 
 template <typename T, int R, int MODE, int KIND>
@@ -562,9 +571,11 @@ int wave2d_warp_blocks(int dtype_bytes, int order, int mode, int kind) {
     int occ = 1;
 #define PGB_OCC(TT, RR)                                                                          \
     occ = kind == 0 ? (mode == kFwd ? occupancy<TT, RR, kFwd, 0>()                               \
-                       : mode == kRecomp ? occupancy<TT, RR, kRecomp, 0>() : occupancy<TT, RR, kAdj, 0>()) \
+                       : mode == kRecomp ? occupancy<TT, RR, kRecomp, 0>()                       \
+                       : mode == kAdj ? occupancy<TT, RR, kAdj, 0>() : occupancy<TT, RR, kBorn, 0>()) \
                     : (mode == kFwd ? occupancy<TT, RR, kFwd, 1>()                               \
-                       : mode == kRecomp ? occupancy<TT, RR, kRecomp, 1>() : occupancy<TT, RR, kAdj, 1>())
+                       : mode == kRecomp ? occupancy<TT, RR, kRecomp, 1>()                       \
+                       : mode == kAdj ? occupancy<TT, RR, kAdj, 1>() : occupancy<TT, RR, kBorn, 1>())
     if (dtype_bytes == 4) {
         switch (R) { case 1: PGB_OCC(float, 1); break; case 2: PGB_OCC(float, 2); break;
                      case 3: PGB_OCC(float, 3); break; default: PGB_OCC(float, 4); break; }
@@ -589,7 +600,9 @@ int wave2d_warp_seg(int dtype_bytes, int order, int pml) {
     template long long launch_wave2d_warp_tasks<T, R, kRecomp, K>(const WaveParams<T>&, const int*, int, int,    \
                                                                   cudaStream_t);                                 \
     template long long launch_wave2d_warp_tasks<T, R, kAdj, K>(const WaveParams<T>&, const int*, int, int,       \
-                                                               cudaStream_t);
+                                                               cudaStream_t);                                    \
+    template long long launch_wave2d_warp_tasks<T, R, kBorn, K>(const WaveParams<T>&, const int*, int, int,      \
+                                                                cudaStream_t);
 #define PGB_INSTW(T, R) PGB_INSTW1(T, R, 0) PGB_INSTW1(T, R, 1)
 PGB_INSTW(float, 1)
 PGB_INSTW(float, 2)
