@@ -26,6 +26,7 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <set>
 #include <tuple>
 #include <vector>
 
@@ -372,6 +373,7 @@ struct PlanT final : public pysit_plan {
         int64_t launches = 0;
     };
     std::map<GraphKey, GraphRec> graphs;
+    std::set<GraphKey> seen;  // run sequences used once so far: eager; captured on their second use
     int64_t launches = 0;
 
     ~PlanT() override {
@@ -788,6 +790,7 @@ struct PlanT final : public pysit_plan {
         for (auto& kv : graphs)
             if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
         graphs.clear();
+        seen.clear();
         ws = static_cast<char*>(w);
         PGB_CHECK_CUDA(cudaMemsetAsync(ws, 0, ws_need, s));
         int rc;
@@ -1395,6 +1398,7 @@ struct PlanT final : public pysit_plan {
         for (auto& kv : graphs)
             if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
         graphs.clear();
+        seen.clear();
         return PYSIT_OK;
     }
 
@@ -1476,6 +1480,15 @@ struct PlanT final : public pysit_plan {
         }
         GraphKey key{kind, a, b, c, d};
         auto it = graphs.find(key);
+        if (it == graphs.end() && seen.insert(key).second) {
+            // first use: launched as it is enqueued (a graph pays off from the second use on;
+            // an optimiser's line search often calls a plan only once or twice)
+            launches = 0;
+            enqueue(s);
+            PGB_CHECK_CUDA(cudaGetLastError());
+            last_launches = launches;
+            return PYSIT_OK;
+        }
         if (it == graphs.end()) {
             launches = 0;
             cudaGraph_t graph = nullptr;
@@ -1572,6 +1585,7 @@ struct LanesPlan final : public pysit_plan {
         }
     };
     std::map<Key, std::pair<cudaGraphExec_t, int64_t>> graphs;
+    std::set<Key> seen;
 
     ~LanesPlan() override {
         for (auto& kv : graphs)
@@ -1646,6 +1660,7 @@ struct LanesPlan final : public pysit_plan {
         for (auto& kv : graphs)
             if (kv.second.first) cudaGraphExecDestroy(kv.second.first);
         graphs.clear();
+        seen.clear();
         ws = static_cast<char*>(w);
         for (int c = 0; c < lanes(); ++c) {
             int rc = kids[c]->bind(ws + kid_off[c], kids[c]->ws_need, s);
@@ -1720,6 +1735,12 @@ struct LanesPlan final : public pysit_plan {
         }
         Key key{kind, a, b, c, d};
         auto it = graphs.find(key);
+        if (it == graphs.end() && seen.insert(key).second) {  // first use: eager, as PlanT::run
+            enqueue(s);
+            PGB_CHECK_CUDA(cudaGetLastError());
+            last_launches = kid_launches() + 1;
+            return PYSIT_OK;
+        }
         if (it == graphs.end()) {
             cudaGraph_t graph = nullptr;
             PGB_CHECK_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
@@ -1816,6 +1837,7 @@ struct LanesPlan final : public pysit_plan {
         for (auto& kv : graphs)
             if (kv.second.first) cudaGraphExecDestroy(kv.second.first);
         graphs.clear();
+        seen.clear();
         return rc;
     }
     int tuning(int* tile, double* share) const override { return kids[0]->tuning(tile, share); }
