@@ -1,4 +1,4 @@
-"""Descent-loop driver shared by the optimizers (mirror of pysit.optimization.OptimizationBase).
+"""Descent loop shared by the optimizers (mirror of pysit.optimization.OptimizationBase).
 
 Behaviour followed (pysit/optimization/optimization.py):
   * ``__call__(shots, initial_value, iteration_parameters, line_search='backtrack',
