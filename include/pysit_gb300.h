@@ -30,6 +30,7 @@ extern "C" {
 #define PYSIT_ECUDA      -2  /* CUDA runtime error */
 #define PYSIT_ENONFINITE -3  /* NaN/Inf found in a wavefield (unstable CFL) */
 #define PYSIT_ESTATE     -4  /* call out of order (e.g. no workspace bound) */
+#define PYSIT_EHOST      -5  /* host-side failure inside the library (a host allocation) */
 
 #define PYSIT_F32 0
 #define PYSIT_F64 1

@@ -17,6 +17,7 @@ PYSIT_EINVAL = -1
 PYSIT_ECUDA = -2
 PYSIT_ENONFINITE = -3
 PYSIT_ESTATE = -4
+PYSIT_EHOST = -5
 PYSIT_F32 = 0
 PYSIT_F64 = 1
 

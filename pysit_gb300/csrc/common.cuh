@@ -44,6 +44,13 @@ __host__ __device__ constexpr double d2tap(int R, int m) { return d2w(R, m < 0 ?
 // ---------------------------------------------------------------------------
 void set_error(const char* fmt, ...);
 int cuda_status(cudaError_t e, const char* what);
+// Called from a catch (...) handler: records the exception in flight and returns PYSIT_EHOST,
+// so that no C++ exception leaves an extern "C" entry point.
+int host_exception(const char* where) noexcept;
+
+// Closes every extern "C" entry point written as a function-try-block.
+#define PGB_API_CATCH(name) \
+    catch (...) { return ::pgb::host_exception(name); }
 
 #define PGB_CHECK_CUDA(call)                                         \
     do {                                                             \

@@ -2,6 +2,8 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <exception>
+#include <new>
 
 #include "common.cuh"
 
@@ -22,6 +24,19 @@ int cuda_status(cudaError_t e, const char* what) {
     set_error("CUDA error %d (%s: %s) in %s", (int)e, cudaGetErrorName(e), cudaGetErrorString(e),
               what);
     return PYSIT_ECUDA;
+}
+
+int host_exception(const char* where) noexcept {
+    try {
+        throw;
+    } catch (const std::bad_alloc&) {
+        set_error("%s: host memory allocation failed", where);
+    } catch (const std::exception& e) {
+        set_error("%s: %s", where, e.what());
+    } catch (...) {
+        set_error("%s: unexpected C++ exception", where);
+    }
+    return PYSIT_EHOST;
 }
 
 }  // namespace pgb

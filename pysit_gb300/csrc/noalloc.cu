@@ -89,7 +89,7 @@ int scratch_address(double** out) {
 using namespace pgb;
 
 extern "C" int pysit_misfit_per_shot_noalloc(int dtype, const void* dobs, const void* dsim, int nshots,
-                                             int64_t per_shot, void* resid, double* rnorm2, void* stream) {
+                                             int64_t per_shot, void* resid, double* rnorm2, void* stream) try {
     PGB_REQUIRE(dtype == PYSIT_F32 || dtype == PYSIT_F64, "dtype must be PYSIT_F32 or PYSIT_F64 (got %d)", dtype);
     PGB_REQUIRE(nshots >= 1 && nshots <= kMaxShots,
                 "nshots must be in [1, %d]: the fixed scratch holds %d shots (got %d)", kMaxShots, kMaxShots,
@@ -111,4 +111,4 @@ extern "C" int pysit_misfit_per_shot_noalloc(int dtype, const void* dobs, const 
     na_finish<<<(nshots + 7) / 8, 256, 0, s>>>(partials, nshots, rnorm2);
     PGB_CHECK_CUDA(cudaGetLastError());
     return PYSIT_OK;
-}
+} PGB_API_CATCH("pysit_misfit_per_shot_noalloc")

@@ -35,6 +35,20 @@
 namespace pgb {
 namespace {
 
+// Runs `enqueue` while `cap` captures a graph.  A C++ exception thrown meanwhile ends the
+// capture (dropping the partial graph) before it propagates, so the stream stays usable.
+template <typename F>
+void capture_into(cudaStream_t cap, F&& enqueue) {
+    try {
+        enqueue();
+    } catch (...) {
+        cudaGraph_t partial = nullptr;
+        cudaStreamEndCapture(cap, &partial);
+        if (partial) cudaGraphDestroy(partial);
+        throw;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // small kernels
 // ---------------------------------------------------------------------------
@@ -1493,7 +1507,7 @@ struct PlanT final : public pysit_plan {
             launches = 0;
             cudaGraph_t graph = nullptr;
             PGB_CHECK_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
-            enqueue(cap);
+            capture_into(cap, [&] { enqueue(cap); });
             cudaError_t e = cudaStreamEndCapture(cap, &graph);
             if (e != cudaSuccess) return cuda_status(e, "cudaStreamEndCapture");
             GraphRec rec;
@@ -1744,7 +1758,7 @@ struct LanesPlan final : public pysit_plan {
         if (it == graphs.end()) {
             cudaGraph_t graph = nullptr;
             PGB_CHECK_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
-            enqueue(cap);
+            capture_into(cap, [&] { enqueue(cap); });
             cudaError_t e = cudaStreamEndCapture(cap, &graph);
             if (e != cudaSuccess) return cuda_status(e, "cudaStreamEndCapture");
             cudaGraphExec_t exec = nullptr;
@@ -1848,7 +1862,7 @@ struct LanesPlan final : public pysit_plan {
 
 using namespace pgb;
 
-extern "C" int pysit_plan_create(const pysit_plan_desc* d, pysit_plan** out) {
+extern "C" int pysit_plan_create(const pysit_plan_desc* d, pysit_plan** out) try {
     PGB_REQUIRE(d && out, "NULL argument");
     *out = nullptr;
     PGB_REQUIRE(d->dim >= 1 && d->dim <= 3, "dim must be 1, 2 or 3");
@@ -1893,87 +1907,87 @@ extern "C" int pysit_plan_create(const pysit_plan_desc* d, pysit_plan** out) {
     if (rc) return rc;
     *out = p.release();
     return PYSIT_OK;
-}
+} PGB_API_CATCH("pysit_plan_create")
 
-extern "C" int pysit_plan_destroy(pysit_plan* p) {
+extern "C" int pysit_plan_destroy(pysit_plan* p) try {
     delete p;
     return PYSIT_OK;
-}
+} PGB_API_CATCH("pysit_plan_destroy")
 
-extern "C" int pysit_plan_workspace_bytes(const pysit_plan* p, uint64_t* bytes) {
+extern "C" int pysit_plan_workspace_bytes(const pysit_plan* p, uint64_t* bytes) try {
     PGB_REQUIRE(p && bytes, "NULL argument");
     return p->workspace_bytes(bytes);
-}
+} PGB_API_CATCH("pysit_plan_workspace_bytes")
 
-extern "C" int pysit_plan_bind_workspace(pysit_plan* p, void* ws, uint64_t bytes, void* stream) {
+extern "C" int pysit_plan_bind_workspace(pysit_plan* p, void* ws, uint64_t bytes, void* stream) try {
     PGB_REQUIRE(p, "NULL plan");
     return p->bind(ws, bytes, (cudaStream_t)stream);
-}
+} PGB_API_CATCH("pysit_plan_bind_workspace")
 
-extern "C" int pysit_plan_set_model(pysit_plan* p, const double* C, void* stream) {
+extern "C" int pysit_plan_set_model(pysit_plan* p, const double* C, void* stream) try {
     PGB_REQUIRE(p, "NULL plan");
     return p->set_model(C, (cudaStream_t)stream);
-}
+} PGB_API_CATCH("pysit_plan_set_model")
 
-extern "C" int pysit_plan_forward(pysit_plan* p, void* traces, void* stream) {
+extern "C" int pysit_plan_forward(pysit_plan* p, void* traces, void* stream) try {
     PGB_REQUIRE(p, "NULL plan");
     return p->forward(traces, (cudaStream_t)stream);
-}
+} PGB_API_CATCH("pysit_plan_forward")
 
 extern "C" int pysit_plan_gradient(pysit_plan* p, const void* dobs, double* grad, double* rnorm2,
-                                   void* traces, void* stream) {
+                                   void* traces, void* stream) try {
     PGB_REQUIRE(p, "NULL plan");
     return p->gradient(dobs, grad, rnorm2, traces, (cudaStream_t)stream, true, false);
-}
+} PGB_API_CATCH("pysit_plan_gradient")
 
 extern "C" int pysit_plan_migrate(pysit_plan* p, const void* operand, double* image, double* norm2,
-                                  void* stream) {
+                                  void* stream) try {
     PGB_REQUIRE(p, "NULL plan");
     return p->gradient(operand, image, norm2, nullptr, (cudaStream_t)stream, true, true);
-}
+} PGB_API_CATCH("pysit_plan_migrate")
 
 extern "C" int pysit_plan_misfit(pysit_plan* p, const void* dobs, double* rnorm2, void* traces,
-                                 void* stream) {
+                                 void* stream) try {
     PGB_REQUIRE(p, "NULL plan");
     return p->gradient(dobs, nullptr, rnorm2, traces, (cudaStream_t)stream, false, false);
-}
+} PGB_API_CATCH("pysit_plan_misfit")
 
-extern "C" int pysit_plan_born(pysit_plan* p, const double* m1, void* traces, void* stream) {
+extern "C" int pysit_plan_born(pysit_plan* p, const double* m1, void* traces, void* stream) try {
     PGB_REQUIRE(p, "NULL plan");
     return p->born(m1, traces, (cudaStream_t)stream);
-}
+} PGB_API_CATCH("pysit_plan_born")
 
-extern "C" int pysit_plan_hessian(pysit_plan* p, const double* m1, double* out, double* d1norm2, void* stream) {
+extern "C" int pysit_plan_hessian(pysit_plan* p, const double* m1, double* out, double* d1norm2, void* stream) try {
     PGB_REQUIRE(p, "NULL plan");
     return p->hessian(m1, out, d1norm2, (cudaStream_t)stream);
-}
+} PGB_API_CATCH("pysit_plan_hessian")
 
-extern "C" int pysit_plan_status(pysit_plan* p, int* flags, void* stream) {
+extern "C" int pysit_plan_status(pysit_plan* p, int* flags, void* stream) try {
     PGB_REQUIRE(p && flags, "NULL argument");
     return p->status(flags, (cudaStream_t)stream);
-}
+} PGB_API_CATCH("pysit_plan_status")
 
-extern "C" int pysit_plan_last_launch_count(const pysit_plan* p, int64_t* n) {
+extern "C" int pysit_plan_last_launch_count(const pysit_plan* p, int64_t* n) try {
     PGB_REQUIRE(p && n, "NULL argument");
     *n = p->last_launches;
     return PYSIT_OK;
-}
+} PGB_API_CATCH("pysit_plan_last_launch_count")
 
-extern "C" int pysit_plan_step_loop(pysit_plan* p, int mode, int nsteps, void* stream) {
+extern "C" int pysit_plan_step_loop(pysit_plan* p, int mode, int nsteps, void* stream) try {
     PGB_REQUIRE(p, "NULL plan");
     return p->step_loop(mode, nsteps, (cudaStream_t)stream);
-}
+} PGB_API_CATCH("pysit_plan_step_loop")
 
-extern "C" int pysit_plan_get_tuning(const pysit_plan* p, int* tile_x, double* shell_share) {
+extern "C" int pysit_plan_get_tuning(const pysit_plan* p, int* tile_x, double* shell_share) try {
     PGB_REQUIRE(p, "NULL plan");
     return p->tuning(tile_x, shell_share);
-}
+} PGB_API_CATCH("pysit_plan_get_tuning")
 
 extern "C" int pysit_plan_autotune(pysit_plan* p, const int* candidates, int ncand, int nsteps, int* chosen,
-                                   double* ms, void* stream) {
+                                   double* ms, void* stream) try {
     PGB_REQUIRE(p, "NULL plan");
     return p->autotune(candidates, ncand, nsteps, chosen, ms, (cudaStream_t)stream);
-}
+} PGB_API_CATCH("pysit_plan_autotune")
 
 // ---- plan groups ------------------------------------------------------------------------
 struct pysit_group {
@@ -1993,7 +2007,7 @@ struct pysit_group {
     }
 };
 
-extern "C" int pysit_group_create(pysit_plan* const* plans, int nplans, pysit_group** out) {
+extern "C" int pysit_group_create(pysit_plan* const* plans, int nplans, pysit_group** out) try {
     PGB_REQUIRE(plans && out && nplans >= 1, "need at least one plan and an output");
     for (int i = 0; i < nplans; ++i) PGB_REQUIRE(plans[i], "NULL plan %d", i);
     std::unique_ptr<pysit_group> g(new pysit_group());
@@ -2010,15 +2024,15 @@ extern "C" int pysit_group_create(pysit_plan* const* plans, int nplans, pysit_gr
     }
     *out = g.release();
     return PYSIT_OK;
-}
+} PGB_API_CATCH("pysit_group_create")
 
-extern "C" int pysit_group_destroy(pysit_group* g) {
+extern "C" int pysit_group_destroy(pysit_group* g) try {
     delete g;
     return PYSIT_OK;
-}
+} PGB_API_CATCH("pysit_group_destroy")
 
 extern "C" int pysit_group_gradient(pysit_group* g, const void* const* dobs, double* const* grad,
-                                    double* const* rnorm2, void* stream) {
+                                    double* const* rnorm2, void* stream) try {
     PGB_REQUIRE(g && dobs && grad && rnorm2, "NULL argument");
     const int n = (int)g->plans.size();
     std::vector<const void*> key;
@@ -2028,12 +2042,14 @@ extern "C" int pysit_group_gradient(pysit_group* g, const void* const* dobs, dou
         PGB_CHECK_CUDA(cudaStreamBeginCapture(g->cap, cudaStreamCaptureModeThreadLocal));
         cudaEventRecord(g->root, g->cap);
         int rc = PYSIT_OK;
-        for (int i = 0; i < n && rc == PYSIT_OK; ++i) {
-            cudaStreamWaitEvent(g->streams[i], g->root, 0);
-            rc = g->plans[i]->enqueue_grad_raw(dobs[i], grad[i], rnorm2[i], g->streams[i]);
-            cudaEventRecord(g->done[i], g->streams[i]);
-            cudaStreamWaitEvent(g->cap, g->done[i], 0);
-        }
+        capture_into(g->cap, [&] {
+            for (int i = 0; i < n && rc == PYSIT_OK; ++i) {
+                cudaStreamWaitEvent(g->streams[i], g->root, 0);
+                rc = g->plans[i]->enqueue_grad_raw(dobs[i], grad[i], rnorm2[i], g->streams[i]);
+                cudaEventRecord(g->done[i], g->streams[i]);
+                cudaStreamWaitEvent(g->cap, g->done[i], 0);
+            }
+        });
         cudaGraph_t graph = nullptr;
         cudaError_t e = cudaStreamEndCapture(g->cap, &graph);
         if (rc) {
@@ -2049,4 +2065,4 @@ extern "C" int pysit_group_gradient(pysit_group* g, const void* const* dobs, dou
     }
     PGB_CHECK_CUDA(cudaGraphLaunch(it->second, (cudaStream_t)stream));
     return PYSIT_OK;
-}
+} PGB_API_CATCH("pysit_group_gradient")
