@@ -37,6 +37,15 @@ def resample_linear(data, ts_src, ts_new):
     ts_src = np.asarray(ts_src, dtype=float)
     ts_new = np.asarray(ts_new, dtype=float)
     n = len(ts_src)
+    if n < 2:
+        # no interval to interpolate on: a single sample is kept at its own time only, as in
+        # core.acquisition.linear_interpolate
+        out = data.new_zeros((data.shape[0], len(ts_new)) + tuple(data.shape[2:]))
+        hit = np.nonzero(ts_new == ts_src[0])[0] if n == 1 else np.zeros(0, dtype=np.int64)
+        if len(hit):
+            idx_t = torch.as_tensor(hit, device=data.device)
+            out.index_copy_(1, idx_t, data[:, :1].expand(-1, len(hit), *data.shape[2:]).contiguous())
+        return out
     idx = np.clip(np.searchsorted(ts_src, ts_new, side="left"), 1, n - 1)
     lo = idx - 1
     frac = (ts_new - ts_src[lo]) / (ts_src[idx] - ts_src[lo])

@@ -410,7 +410,8 @@ struct PlanT final : public pysit_plan {
         if (dim == 1) { nx = 1; ny = 1; }
         if (dim == 2) ny = 1;
         dx = d.delta[0]; dy = d.delta[1]; dz = d.delta[2];
-        dt = d.dt; nsteps = d.nsteps; p_img = d.imaging_period; S = d.checkpoint_every;
+        dt = d.dt; nsteps = d.nsteps; p_img = d.imaging_period;
+        S = std::min(d.checkpoint_every, d.nsteps);  // an interval past the record is one segment
         nshots = d.nshots; G = std::min(d.shots_per_launch, d.nshots); nsrc = d.nsrc; nrec = d.nrec;
         use_graph = d.use_graph;
         psi_consistent = d.psi_consistent ? 1 : 0;

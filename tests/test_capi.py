@@ -129,7 +129,7 @@ def test_plan_rejects_bad_taps(lib):
 
 def test_plan_workspace_scales_with_checkpoint_interval(lib):
     sizes = []
-    for S in (1, 7, 50):
+    for S in (1, 7, 50, 10 ** 6):
         keep = []
         d = _desc(keep=keep)
         d.checkpoint_every = S
@@ -141,6 +141,8 @@ def test_plan_workspace_scales_with_checkpoint_interval(lib):
         lib.pysit_plan_destroy(h)
     # replay grows with S, checkpoints shrink with it: S=7 is the cheapest of the three
     assert sizes[1] < sizes[0] and sizes[1] < sizes[2]
+    # an interval past the record (50 steps) is one segment of the whole record
+    assert sizes[3] == sizes[2]
 
 
 def test_workspace_of_the_schedules(lib):
