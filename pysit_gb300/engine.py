@@ -13,6 +13,7 @@ from __future__ import annotations
 
 import ctypes as C
 import math
+import weakref
 
 import numpy as np
 
@@ -437,12 +438,44 @@ class PlanGroup:
         return [(p.grad, p.rnorm2) for p in self.plans]
 
 
-# recorded traces of the last shot list on the device: (arrays it was built from, dtype, nrec) ->
-# (tensor [nshots, nt_obs, nrec], ts_obs, arrays, fingerprints); one entry.  An entry is reused
-# while every shot still holds the same array with the same fingerprint (a sample of its
-# values): assign a new array to receivers.data, or pass the data to load_observed, after
-# editing recorded traces in place.
-_OBSERVED = {}
+class _ObservedCache:
+    """The recorded traces of the last shot list on the device: one entry, keyed by the
+    receivers' data arrays, the dtype and nrec.  The entry is reused while every shot still
+    holds the same array with the same fingerprint (a sample of its values): assign a new
+    array to receivers.data, or pass the data to load_observed, after editing recorded traces
+    in place.  The arrays are held weakly: when one of them is freed, the device copy goes
+    with it."""
+
+    def __init__(self):
+        self._entry = None  # (key, value, [weakref of array], [fingerprint])
+
+    def get(self, key, arrays):
+        e = self._entry
+        if e is None or e[0] != key:
+            return None
+        if all(w() is a and fp == _fingerprint(a) for w, fp, a in zip(e[2], e[3], arrays)):
+            return e[1]
+        return None
+
+    def put(self, key, value, arrays):
+        self.clear()
+        try:
+            refs = [weakref.ref(a) for a in arrays]
+        except TypeError:  # data that cannot be held weakly is not cached
+            return
+        for a in {id(a): a for a in arrays}.values():
+            weakref.finalize(a, self._drop, refs)
+        self._entry = (key, value, refs, [_fingerprint(a) for a in arrays])
+
+    def _drop(self, refs):
+        if self._entry is not None and self._entry[2] is refs:
+            self._entry = None
+
+    def clear(self):
+        self._entry = None
+
+
+_OBSERVED = _ObservedCache()
 
 
 def _fingerprint(a):
@@ -468,9 +501,10 @@ def _observed_on_device(shots, tdtype, nrec):
     if any(r.ts is not ts0 and not np.array_equal(r.ts, ts0) for r in recv[1:]):
         return None
     key = (tuple(id(r.data) for r in recv), str(tdtype), nrec, len(ts0))
-    hit = _OBSERVED.get(key)
-    if hit is not None and all(a is r.data and fp == _fingerprint(r.data) for a, fp, r in zip(hit[2], hit[3], recv)):
-        return hit[0], hit[1]
+    arrays = [r.data for r in recv]
+    hit = _OBSERVED.get(key, arrays)
+    if hit is not None:
+        return hit
     _OBSERVED.clear()
     elem = 8 if tdtype == torch.float64 else 4
     need = len(recv) * len(ts0) * nrec * elem
@@ -481,7 +515,7 @@ def _observed_on_device(shots, tdtype, nrec):
         host[i, :, :r.data.shape[1]] = r.data
     raw = torch.from_numpy(host).pin_memory().to("cuda", non_blocking=True)
     ts_obs = np.asarray(ts0, dtype=float).copy()
-    _OBSERVED[key] = (raw, ts_obs, [r.data for r in recv], [_fingerprint(r.data) for r in recv])
+    _OBSERVED.put(key, (raw, ts_obs), arrays)
     return raw, ts_obs
 
 

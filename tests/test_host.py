@@ -141,3 +141,27 @@ def test_solver_rejects_unknown_gradient_schedule():
         api.ConstantDensityAcousticWave(m, kernel_implementation="cuda", gradient_schedule="fast")
     s = api.ConstantDensityAcousticWave(m, kernel_implementation="cuda", gradient_schedule="auto")
     assert s.gradient_schedule == "auto"
+
+
+def test_observed_cache_follows_the_data_arrays():
+    """The device copy of recorded traces is found again for the same arrays with the same values,
+    missed after an in-place edit, and released when one of the arrays is freed."""
+    import gc
+    from pysit_gb300.engine import _ObservedCache
+    rng = np.random.default_rng(3)
+    a, b = rng.standard_normal((50, 4)), rng.standard_normal((50, 4))
+    cache = _ObservedCache()
+    key = (id(a), id(b))
+    payload = object()
+    cache.put(key, payload, [a, b])
+    assert cache.get(key, [a, b]) is payload
+    assert cache.get(key, [a, b.copy()]) is None
+    b[-1, 0] += 1.0  # the last row is part of the fingerprint
+    assert cache.get(key, [a, b]) is None
+    cache.put(key, payload, [a, b])
+    assert cache.get(key, [a, b]) is payload
+    del b
+    gc.collect()
+    assert cache._entry is None
+    cache.put((id(a),), payload, [[1.0, 2.0]])   # not weakly referable: not cached
+    assert cache._entry is None
