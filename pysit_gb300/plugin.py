@@ -112,6 +112,7 @@ def _make_class(pysit, dim):
         # GPU implementations shared with the standalone solver classes
         _profiles = mine._profiles
         device_model = mine.device_model
+        release_plans = mine.release_plans
         _device_sigmas = mine._device_sigmas
         time_step = mine.time_step
         _launch_step = mine._launch_step

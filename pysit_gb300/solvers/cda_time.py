@@ -280,6 +280,15 @@ class _CDATimeScalarCuda:
                                           device="cuda")
         return self._C_dev
 
+    def release_plans(self):
+        """Drop this solver's cached batched plans.  Their device workspaces (with the kept
+        dWaveOp schedule, most of the device memory) go back to the device; the next batched
+        call builds a new plan."""
+        self._plans.clear()
+        import torch
+        if torch.cuda.is_available() and torch.cuda.is_initialized():
+            torch.cuda.empty_cache()
+
     # ---- solver data -----------------------------------------------------------
     def SolverData(self, *args, **kwargs):
         """Host (numpy) ring, the reference-compatible solver state."""

@@ -165,3 +165,10 @@ def test_observed_cache_follows_the_data_arrays():
     assert cache._entry is None
     cache.put((id(a),), payload, [[1.0, 2.0]])   # not weakly referable: not cached
     assert cache._entry is None
+
+
+def test_release_plans_empties_the_plan_cache():
+    m, shots, solver, C, C0 = problems.build(api, "o6")
+    solver._plans["key"] = object()
+    solver.release_plans()
+    assert solver._plans == {}

@@ -27,6 +27,9 @@ def test_reference_factory_resolves_cuda(pysit, name, dim, order):
     s = pysit.ConstantDensityAcousticWave(m, spatial_accuracy_order=order, kernel_implementation="cuda")
     assert type(s).__name__ == f"ConstantDensityAcousticTimeScalar_{dim}D_cuda"
     assert s.supports["kernel_implementation"] == "cuda"
+    s._plans["key"] = object()
+    s.release_plans()
+    assert s._plans == {}
     # the cpp solver is still selected for 'cpp'
     c = pysit.ConstantDensityAcousticWave(m, spatial_accuracy_order=order, kernel_implementation="cpp")
     assert type(c).__name__ == f"ConstantDensityAcousticTimeScalar_{dim}D_cpp"
