@@ -17,7 +17,6 @@ import weakref
 
 import numpy as np
 
-from .. import _native
 from ..engine import plan_for
 from ..modeling.temporal_modeling import TemporalModeling
 
