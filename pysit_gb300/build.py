@@ -67,7 +67,10 @@ def build(verbose_ptxas: bool = False, jobs: int | None = None) -> str:
     os.makedirs(OBJ, exist_ok=True)
     stamp = os.path.join(OBJ, "defines.txt")
     want = " ".join(_defines())
-    have = open(stamp).read() if os.path.exists(stamp) else ""
+    have = ""
+    if os.path.exists(stamp):
+        with open(stamp) as fh:
+            have = fh.read()
     if want != have:  # other macros: every object is stale
         for f in os.listdir(OBJ):
             if f.endswith(".o"):

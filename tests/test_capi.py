@@ -13,7 +13,8 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def _declared():
-    txt = open(os.path.join(ROOT, "include", "pysit_gb300.h")).read()
+    with open(os.path.join(ROOT, "include", "pysit_gb300.h")) as f:
+        txt = f.read()
     txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
     return sorted(set(re.findall(r"\b(pysit_[a-z0-9_]+)\s*\(", txt)))
 
