@@ -182,9 +182,9 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     config = {"workload": "cfg2: 2D batched FWI gradient, 1152x384 @12.5m + 40 PML, order 8, 64 shots, "
-                          "1152 receivers, 8 Hz Ricker, 4000 steps, checkpoints every 64",
+                          "1152 receivers, 8 Hz Ricker, 4000 steps",
               "grid_padded": [int(1152 * args.scale) + 80, int(384 * args.scale) + 80],
-              "shots": args.shots, "nsteps": args.nsteps, "order": 8, "checkpoint_every": 64,
+              "shots": args.shots, "nsteps": args.nsteps, "order": 8,
               "parallelism": f"replicas{world}" if world > 1 else "single",
               "l2": "inputs larger than L2 (working set > 129 MB per step)"}
 
@@ -261,9 +261,8 @@ def main():
     config["gradient_schedule"] = plan.gradient_schedule
     config["shots_per_launch"] = plan.shots_per_launch
     config["lanes"] = plan.lanes
-    if plan.gradient_schedule == "store":
-        config["workload"] = config["workload"].replace(", checkpoints every 64", "")
-        config.pop("checkpoint_every", None)
+    if plan.gradient_schedule == "checkpoint":
+        config["checkpoint_every"] = plan.checkpoint_every
     for _ in range(args.warmup):
         plan.gradient()
     torch.cuda.synchronize()
