@@ -57,11 +57,21 @@ static const double D2W[5][5] = {
  * and float, mirroring the two reference template instantiations. */
 #define DEFINE_ORACLE(T, SUF)                                                          \
                                                                                        \
-static T d1_##SUF(const T* v, ptrdiff_t idx, ptrdiff_t s, int pos, int n, int R,       \
-                  T del)                                                               \
+static inline __attribute__((always_inline))                                          \
+T d1_##SUF(const T* v, ptrdiff_t idx, ptrdiff_t s, int pos, int n, const int R, T del) \
 {                                                                                      \
-    /* taps summed from -R to +R, out-of-range taps are zero */                        \
+    /* taps summed from -R to +R, out-of-range taps are zero; a cell R or more from    \
+     * both ends takes every tap, so its loop drops the range test and sums the same   \
+     * terms in the same order */                                                      \
     T acc = 0;                                                                         \
+    if (pos >= R && pos < n - R) {                                                     \
+        for (int m = -R; m <= R; ++m) {                                                \
+            if (m == 0) continue;                                                      \
+            T w = (T)(m > 0 ? D1W[R][m] : -D1W[R][-m]);                                \
+            acc += w * v[idx + (ptrdiff_t)m * s];                                      \
+        }                                                                              \
+        return acc / del;                                                              \
+    }                                                                                  \
     for (int m = -R; m <= R; ++m) {                                                    \
         if (m == 0) continue;                                                          \
         int p = pos + m;                                                               \
@@ -72,10 +82,17 @@ static T d1_##SUF(const T* v, ptrdiff_t idx, ptrdiff_t s, int pos, int n, int R,
     return acc / del;                                                                  \
 }                                                                                      \
                                                                                        \
-static T d2_##SUF(const T* v, ptrdiff_t idx, ptrdiff_t s, int pos, int n, int R,       \
-                  T del2)                                                              \
+static inline __attribute__((always_inline))                                          \
+T d2_##SUF(const T* v, ptrdiff_t idx, ptrdiff_t s, int pos, int n, const int R, T del2) \
 {                                                                                      \
     T acc = 0;                                                                         \
+    if (pos >= R && pos < n - R) {                                                     \
+        for (int m = -R; m <= R; ++m) {                                                \
+            T w = (T)D2W[R][m < 0 ? -m : m];                                           \
+            acc += w * v[idx + (ptrdiff_t)m * s];                                      \
+        }                                                                              \
+        return acc / del2;                                                             \
+    }                                                                                  \
     for (int m = -R; m <= R; ++m) {                                                    \
         int p = pos + m;                                                               \
         if (p < 0 || p >= n) continue;                                                 \
@@ -123,15 +140,16 @@ int oracle_cda1d_step_##SUF(int order, const T* km1_u, const T* k_phiz, const T*
     return 0;                                                                          \
 }                                                                                      \
                                                                                        \
-int oracle_cda2d_step_##SUF(int order, const T* km1_u, const T* k_phix,                \
-                            const T* k_phiz, const T* k_u, const T* C, const T* rhs,   \
-                            const T* xl, int nxl, const T* xr, int nxr,                \
-                            const T* zl, int nzl, const T* zr, int nzr,                \
-                            double dt, double dx, double dz, int nx, int nz,           \
-                            T* kp1_phix, T* kp1_phiz, T* kp1_u)                        \
+/* the step body, inlined once per stencil radius R (1..4) so that the tap loops   \
+ * unroll; the public entry below picks the instance */                               \
+static inline __attribute__((always_inline))                                          \
+void step2d_##SUF(const int R, const T* km1_u, const T* k_phix,                       \
+                  const T* k_phiz, const T* k_u, const T* C, const T* rhs,             \
+                  const T* xl, int nxl, const T* xr, int nxr,                          \
+                  const T* zl, int nzl, const T* zr, int nzr,                          \
+                  double dt, double dx, double dz, int nx, int nz,                     \
+                  T* kp1_phix, T* kp1_phiz, T* kp1_u)                                  \
 {                                                                                      \
-    int R = order / 2;                                                                 \
-    if (order < 2 || order > 8 || (order & 1) || nx < 3 || nz < 3) return -1;          \
     T dt2 = (T)(dt * dt);                                                              \
     T tdx = (T)dx, tdx2 = tdx * tdx, tdz = (T)dz, tdz2 = tdz * tdz;                    \
     ptrdiff_t xs = nz;                                                                 \
@@ -168,23 +186,44 @@ int oracle_cda2d_step_##SUF(int order, const T* km1_u, const T* k_phix,         
             }                                                                          \
         }                                                                              \
     }                                                                                  \
+}                                                                                      \
+                                                                                       \
+int oracle_cda2d_step_##SUF(int order, const T* km1_u, const T* k_phix,                \
+                            const T* k_phiz, const T* k_u, const T* C, const T* rhs,   \
+                            const T* xl, int nxl, const T* xr, int nxr,                \
+                            const T* zl, int nzl, const T* zr, int nzr,                \
+                            double dt, double dx, double dz, int nx, int nz,           \
+                            T* kp1_phix, T* kp1_phiz, T* kp1_u)                        \
+{                                                                                      \
+    if (order < 2 || order > 8 || (order & 1) || nx < 3 || nz < 3) return -1;          \
+    switch (order / 2) {                                                               \
+    case 1: step2d_##SUF(1, km1_u, k_phix, k_phiz, k_u, C, rhs, xl, nxl, xr, nxr, zl,  \
+                         nzl, zr, nzr, dt, dx, dz, nx, nz, kp1_phix, kp1_phiz, kp1_u); \
+            break;                                                                     \
+    case 2: step2d_##SUF(2, km1_u, k_phix, k_phiz, k_u, C, rhs, xl, nxl, xr, nxr, zl,  \
+                         nzl, zr, nzr, dt, dx, dz, nx, nz, kp1_phix, kp1_phiz, kp1_u); \
+            break;                                                                     \
+    case 3: step2d_##SUF(3, km1_u, k_phix, k_phiz, k_u, C, rhs, xl, nxl, xr, nxr, zl,  \
+                         nzl, zr, nzr, dt, dx, dz, nx, nz, kp1_phix, kp1_phiz, kp1_u); \
+            break;                                                                     \
+    default: step2d_##SUF(4, km1_u, k_phix, k_phiz, k_u, C, rhs, xl, nxl, xr, nxr, zl, \
+                          nzl, zr, nzr, dt, dx, dz, nx, nz, kp1_phix, kp1_phiz,        \
+                          kp1_u);                                                      \
+    }                                                                                  \
     return 0;                                                                          \
 }                                                                                      \
                                                                                        \
-int oracle_cda3d_step_##SUF(int order, const T* km1_u, const T* k_phix,                \
-                            const T* k_phiy, const T* k_phiz, const T* k_psi,          \
-                            const T* k_u, const T* C, const T* rhs,                    \
-                            const T* xl, int nxl, const T* xr, int nxr,                \
-                            const T* yl, int nyl, const T* yr, int nyr,                \
-                            const T* zl, int nzl, const T* zr, int nzr,                \
-                            double dt, double dx, double dy, double dz,                \
-                            int nx, int ny, int nz,                                    \
-                            T* kp1_phix, T* kp1_phiy, T* kp1_phiz, T* kp1_psi,         \
-                            T* kp1_u)                                                  \
+static inline __attribute__((always_inline))                                          \
+void step3d_##SUF(const int R, const T* km1_u, const T* k_phix,                       \
+                  const T* k_phiy, const T* k_phiz, const T* k_psi,                    \
+                  const T* k_u, const T* C, const T* rhs,                              \
+                  const T* xl, int nxl, const T* xr, int nxr,                          \
+                  const T* yl, int nyl, const T* yr, int nyr,                          \
+                  const T* zl, int nzl, const T* zr, int nzr,                          \
+                  double dt, double dx, double dy, double dz,                          \
+                  int nx, int ny, int nz,                                              \
+                  T* kp1_phix, T* kp1_phiy, T* kp1_phiz, T* kp1_psi, T* kp1_u)         \
 {                                                                                      \
-    int R = order / 2;                                                                 \
-    if (order < 2 || order > 8 || (order & 1) || nx < 3 || ny < 3 || nz < 3)           \
-        return -1;                                                                     \
     T dt2 = (T)(dt * dt);                                                              \
     T tdx = (T)dx, tdx2 = tdx * tdx, tdy = (T)dy, tdy2 = tdy * tdy;                    \
     T tdz = (T)dz, tdz2 = tdz * tdz;                                                   \
@@ -239,6 +278,39 @@ int oracle_cda3d_step_##SUF(int order, const T* km1_u, const T* k_phix,         
             kp1_u[idx] = dt2 * c2 * (rhs[idx] + lap + dphixdx + dphiydy + dphizdz)     \
                          - (um - 2.0 * uc);                                            \
         }                                                                              \
+    }                                                                                  \
+}                                                                                      \
+                                                                                       \
+int oracle_cda3d_step_##SUF(int order, const T* km1_u, const T* k_phix,                \
+                            const T* k_phiy, const T* k_phiz, const T* k_psi,          \
+                            const T* k_u, const T* C, const T* rhs,                    \
+                            const T* xl, int nxl, const T* xr, int nxr,                \
+                            const T* yl, int nyl, const T* yr, int nyr,                \
+                            const T* zl, int nzl, const T* zr, int nzr,                \
+                            double dt, double dx, double dy, double dz,                \
+                            int nx, int ny, int nz,                                    \
+                            T* kp1_phix, T* kp1_phiy, T* kp1_phiz, T* kp1_psi,         \
+                            T* kp1_u)                                                  \
+{                                                                                      \
+    if (order < 2 || order > 8 || (order & 1) || nx < 3 || ny < 3 || nz < 3)           \
+        return -1;                                                                     \
+    switch (order / 2) {                                                               \
+    case 1: step3d_##SUF(1, km1_u, k_phix, k_phiy, k_phiz, k_psi, k_u, C, rhs, xl, nxl, \
+                         xr, nxr, yl, nyl, yr, nyr, zl, nzl, zr, nzr, dt, dx, dy, dz,  \
+                         nx, ny, nz, kp1_phix, kp1_phiy, kp1_phiz, kp1_psi, kp1_u);    \
+            break;                                                                     \
+    case 2: step3d_##SUF(2, km1_u, k_phix, k_phiy, k_phiz, k_psi, k_u, C, rhs, xl, nxl, \
+                         xr, nxr, yl, nyl, yr, nyr, zl, nzl, zr, nzr, dt, dx, dy, dz,  \
+                         nx, ny, nz, kp1_phix, kp1_phiy, kp1_phiz, kp1_psi, kp1_u);    \
+            break;                                                                     \
+    case 3: step3d_##SUF(3, km1_u, k_phix, k_phiy, k_phiz, k_psi, k_u, C, rhs, xl, nxl, \
+                         xr, nxr, yl, nyl, yr, nyr, zl, nzl, zr, nzr, dt, dx, dy, dz,  \
+                         nx, ny, nz, kp1_phix, kp1_phiy, kp1_phiz, kp1_psi, kp1_u);    \
+            break;                                                                     \
+    default: step3d_##SUF(4, km1_u, k_phix, k_phiy, k_phiz, k_psi, k_u, C, rhs, xl,    \
+                          nxl, xr, nxr, yl, nyl, yr, nyr, zl, nzl, zr, nzr, dt, dx,    \
+                          dy, dz, nx, ny, nz, kp1_phix, kp1_phiy, kp1_phiz, kp1_psi,   \
+                          kp1_u);                                                      \
     }                                                                                  \
     return 0;                                                                          \
 }

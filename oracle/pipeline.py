@@ -61,11 +61,13 @@ def step(kind, dim, order, km1_u, k_aux, k_u, Cpad, rhs, profiles, dt, deltas, s
     cast = lambda a: np.ascontiguousarray(a, dtype=dt_)  # noqa: E731
     km1_u, k_u, Cpad, rhs = cast(km1_u), cast(k_u), cast(Cpad), cast(rhs)
     prof = [(cast(l), cast(r)) for l, r in profiles]
-    out_u = np.zeros_like(k_u)
+    # the oracle's steps write every output cell; the reference's OpenMP variants get zeroed outputs
+    new = np.empty_like if kind == "oracle" else np.zeros_like
+    out_u = new(k_u)
     extra = [C.c_int(1 if omp else 0)] if kind == "ref" else []
     if dim == 1:
         phz = cast(k_aux["Phiz"])
-        o_phz = np.zeros_like(phz)
+        o_phz = new(phz)
         f = getattr(L, f"{pfx}_cda1d_step_{suf}")
         rc = f(C.c_int(order), _p(km1_u), _p(phz), _p(k_u), _p(Cpad), _p(rhs),
                _p(prof[0][0]), C.c_int(len(prof[0][0])), _p(prof[0][1]), C.c_int(len(prof[0][1])),
@@ -73,7 +75,7 @@ def step(kind, dim, order, km1_u, k_aux, k_u, Cpad, rhs, profiles, dt, deltas, s
         aux = {"Phiz": o_phz}
     elif dim == 2:
         phx, phz = cast(k_aux["Phix"]), cast(k_aux["Phiz"])
-        o_phx, o_phz = np.zeros_like(phx), np.zeros_like(phz)
+        o_phx, o_phz = new(phx), new(phz)
         f = getattr(L, f"{pfx}_cda2d_step_{suf}")
         rc = f(C.c_int(order), _p(km1_u), _p(phx), _p(phz), _p(k_u), _p(Cpad), _p(rhs),
                _p(prof[0][0]), C.c_int(len(prof[0][0])), _p(prof[0][1]), C.c_int(len(prof[0][1])),
@@ -83,7 +85,7 @@ def step(kind, dim, order, km1_u, k_aux, k_u, Cpad, rhs, profiles, dt, deltas, s
         aux = {"Phix": o_phx, "Phiz": o_phz}
     else:
         phx, phy, phz, psi = (cast(k_aux[n]) for n in ("Phix", "Phiy", "Phiz", "psi"))
-        outs = [np.zeros_like(phx) for _ in range(4)]
+        outs = [new(phx) for _ in range(4)]
         f = getattr(L, f"{pfx}_cda3d_step_{suf}")
         rc = f(C.c_int(order), _p(km1_u), _p(phx), _p(phy), _p(phz), _p(psi), _p(k_u), _p(Cpad), _p(rhs),
                _p(prof[0][0]), C.c_int(len(prof[0][0])), _p(prof[0][1]), C.c_int(len(prof[0][1])),
@@ -107,9 +109,14 @@ def set_psi_consistent(on):
     lib("oracle").oracle_set_psi_consistent(C.c_int(1 if on else 0))
 
 
-def dwaveop(P, um, uc, up, psi):
-    """(u+ - 2u + u-)/dt^2 + S1 (u+ - u-)/(2dt) + S2 u (+ S3 psi in 3D), mesh sigma maps."""
-    dim, dt = P["dim"], P["dt"]
+def _dwaveop_sigma(P):
+    """S1, S2, S3 of dwaveop on the full grid, built once per problem: the reference keeps the
+    same sums and products as the solver's operator_components (sxPsz, sxsz, ...;
+    pysit/solvers/constant_density_acoustic/time/scalar/constant_density_acoustic_time_scalar_2D.py:51-65)."""
+    c = P.get("_dwaveop_sigma")
+    if c is not None and c[0] is P["sigmaps"]:
+        return c[1:]
+    dim = P["dim"]
     g = [np.asarray(s, float) for s in P["sigmaps"]]
     shape = P["shape"]
     if dim == 1:
@@ -127,6 +134,14 @@ def dwaveop(P, um, uc, up, psi):
         s1 = (full * (sx + sy + sz)).reshape(-1)
         s2 = (full * (sx * sy + sx * sz + sy * sz)).reshape(-1)
         s3 = (full * (sx * sy * sz)).reshape(-1)
+    P["_dwaveop_sigma"] = (P["sigmaps"], s1, s2, s3)
+    return s1, s2, s3
+
+
+def dwaveop(P, um, uc, up, psi):
+    """(u+ - 2u + u-)/dt^2 + S1 (u+ - u-)/(2dt) + S2 u (+ S3 psi in 3D), mesh sigma maps."""
+    dt = P["dt"]
+    s1, s2, s3 = _dwaveop_sigma(P)
     out = (up - 2 * uc + um) / dt ** 2 + s1 * (up - um) / (2.0 * dt) + s2 * uc
     if s3 is not None:
         out = out + s3 * psi
@@ -150,8 +165,8 @@ def forward(P, want_dwaveop=False, imaging_period=1, kind="oracle", dtype=np.flo
         up, aux_n = step(kind, dim, P["order"], um, aux, uc, P["C"], rhs, P["profiles"], P["dt"], P["deltas"],
                          P["shape"])
         if want_dwaveop and k % imaging_period == 0:
-            dws.append(dwaveop(P, um.astype(float), uc.astype(float), up.astype(float),
-                               aux["psi"].astype(float) if dim == 3 else None))
+            dws.append(dwaveop(P, um.astype(float, copy=False), uc.astype(float, copy=False), up.astype(float, copy=False),
+                               aux["psi"].astype(float, copy=False) if dim == 3 else None))
         if k == P["nsteps"] - 1:
             break
         um, uc, aux = uc, up, aux_n
@@ -183,8 +198,8 @@ def adjoint_image(P, resid, dws, imaging_period=1, kind="oracle", dtype=np.float
         qp, aux_n = step(kind, dim, P["order"], qm, aux, qc, P["C"], rhs, P["profiles"], P["dt"], P["deltas"],
                          P["shape"])
         if want_dwaveop and k % imaging_period == 0:
-            dwa.append(dwaveop(P, qm.astype(float), qc.astype(float), qp.astype(float),
-                               aux["psi"].astype(float) if dim == 3 else None))
+            dwa.append(dwaveop(P, qm.astype(float, copy=False), qc.astype(float, copy=False), qp.astype(float, copy=False),
+                               aux["psi"].astype(float, copy=False) if dim == 3 else None))
         if k == 0:
             break
         qm, qc, aux = qc, qp, aux_n
@@ -222,8 +237,8 @@ def born(P, m1, kind="oracle", dtype=np.float64, want_dwaveop1=False):
         up, aux_n = step(kind, dim, P["order"], um, aux, uc, P["C"], rhs, P["profiles"], P["dt"], P["deltas"],
                          P["shape"])
         if want_dwaveop1:
-            dw1.append(dwaveop(P, um.astype(float), uc.astype(float), up.astype(float),
-                               aux["psi"].astype(float) if dim == 3 else None))
+            dw1.append(dwaveop(P, um.astype(float, copy=False), uc.astype(float, copy=False), up.astype(float, copy=False),
+                               aux["psi"].astype(float, copy=False) if dim == 3 else None))
         if k == P["nsteps"] - 1:
             break
         um, uc, aux = uc, up, aux_n
