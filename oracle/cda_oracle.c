@@ -8,7 +8,7 @@
  *
  * Parity pin: tests/test_oracle_pin.py compares these functions with the
  * reference's own templates (compiled from pysit/solvers/constant_density_acoustic/
- * time/scalar/*.h into oracle/_ref by oracle/Makefile) on random inputs, and
+ * time/scalar/ headers into oracle/_ref by oracle/Makefile) on random inputs, and
  * tests/golden/ holds traces and gradients produced by the reference package.
  *
  * Semantics restated (reference file:line, paths inside the pysit project):
