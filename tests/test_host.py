@@ -172,3 +172,46 @@ def test_release_plans_empties_the_plan_cache():
     solver._plans["key"] = object()
     solver.release_plans()
     assert solver._plans == {}
+
+
+def _schedule_case(monkeypatch, nshots, free_gb, per_shot_gb, fixed=None, base_gb=1.0, nsteps=4000, nrec=1152):
+    """WavePlan._choose_schedule with a fake device (free memory) and a linear workspace model."""
+    import types
+    from pysit_gb300 import _native
+    from pysit_gb300.engine import WavePlan
+    GB = 1 << 30
+    fake_torch = types.SimpleNamespace(float64="f64", float32="f32",
+                                       cuda=types.SimpleNamespace(mem_get_info=lambda: (int(free_gb * GB), 0)))
+    monkeypatch.setattr(_native, "require_cuda", lambda: fake_torch)
+    calls = []
+
+    def workspace(lib, d, G, store, lanes=1):
+        calls.append((G, store, lanes))
+        return int((base_gb + G * per_shot_gb) * GB)
+    plan = types.SimpleNamespace(nshots=nshots, nsteps=nsteps, tdtype="f32", shots_per_launch=fixed or nshots,
+                                 lanes=1, _workspace_for=workspace)
+    sched = WavePlan._choose_schedule(plan, None, None, fixed is not None, nrec)
+    return sched, plan.shots_per_launch, calls
+
+
+def test_auto_schedule_takes_the_largest_balanced_launch(monkeypatch):
+    # 64 shots of 9.5 GB each on 280 GB free: 27 would fit, so three balanced launches of 22
+    sched, G, _ = _schedule_case(monkeypatch, 64, 280.0, 9.5)
+    assert (sched, G) == ("store", 22)
+    # 128 shots of the same size: five launches, ceil(128 / 5) = 26 (the end-to-end FWI's launch)
+    sched, G, _ = _schedule_case(monkeypatch, 128, 280.0, 9.5)
+    assert (sched, G) == ("store", 26)
+    # few shots that all fit: one launch of all of them
+    sched, G, _ = _schedule_case(monkeypatch, 8, 280.0, 9.5)
+    assert (sched, G) == ("store", 8)
+
+
+def test_auto_schedule_falls_back_to_checkpoints(monkeypatch):
+    # fewer than 16 shots per launch would fit: the checkpointed schedule
+    sched, _, _ = _schedule_case(monkeypatch, 64, 120.0, 9.5)
+    assert sched == "checkpoint"
+    # a fixed launch size is kept and decides alone
+    sched, G, calls = _schedule_case(monkeypatch, 64, 280.0, 9.5, fixed=32)
+    assert (sched, G) == ("checkpoint", 32) and calls == [(32, True, 1)]
+    sched, G, _ = _schedule_case(monkeypatch, 64, 280.0, 9.5, fixed=8)
+    assert (sched, G) == ("store", 8)
