@@ -215,3 +215,32 @@ def test_auto_schedule_falls_back_to_checkpoints(monkeypatch):
     assert (sched, G) == ("checkpoint", 32) and calls == [(32, True, 1)]
     sched, G, _ = _schedule_case(monkeypatch, 64, 280.0, 9.5, fixed=8)
     assert (sched, G) == ("store", 8)
+
+
+def test_misfit_backward_maps_the_m_gradient_to_velocity(monkeypatch):
+    """MisfitFunction's backward turns the gradient g in m = C**-2 (cell-volume inner product)
+    into dJ/dC = g * dV * (-2 C**-3): checked on a misfit whose value is dV * sum(g * C**-2)."""
+    import types
+    import torch
+    from pysit_gb300 import _native, autograd
+    monkeypatch.setattr(_native, "require_cuda", lambda: torch)
+    rng = np.random.default_rng(4)
+    deltas = (12.5, 10.0)
+    dV = float(np.prod(deltas))
+    g = torch.as_tensor(rng.standard_normal((6, 5)), dtype=torch.float64)
+
+    class Obj:
+        solver = types.SimpleNamespace(mesh=types.SimpleNamespace(deltas=deltas))
+
+        def _run(self, C, want_grad):
+            J = dV * (g * C.detach().double() ** -2).sum()
+            return J.to(C.dtype), (g.clone() if want_grad else None)
+
+    C0 = torch.as_tensor(1500.0 + 500.0 * rng.random((6, 5)), dtype=torch.float64)
+    C = C0.clone().requires_grad_()
+    J = autograd._make_function().apply(C, Obj())
+    J.backward()
+    Cr = C0.clone().requires_grad_()
+    (dV * (g * Cr ** -2).sum()).backward()
+    torch.testing.assert_close(C.grad, Cr.grad, rtol=1e-13, atol=0)
+    assert float(J.detach()) == pytest.approx(float(dV * (g * C0 ** -2).sum()), rel=1e-15)
