@@ -244,3 +244,33 @@ def test_misfit_backward_maps_the_m_gradient_to_velocity(monkeypatch):
     (dV * (g * Cr ** -2).sum()).backward()
     torch.testing.assert_close(C.grad, Cr.grad, rtol=1e-13, atol=0)
     assert float(J.detach()) == pytest.approx(float(dV * (g * C0 ** -2).sum()), rel=1e-15)
+
+
+@pytest.mark.parametrize("n_src", [1, 2, 7])
+def test_resampling_arithmetic_equals_host_interpolation(monkeypatch, n_src):
+    """The device resampler's arithmetic, run here on CPU tensors, against linear_interpolate
+    (a single sample is kept at its own time only)."""
+    import torch
+    from pysit_gb300 import _native
+    from pysit_gb300.autograd import resample_linear
+    monkeypatch.setattr(_native, "require_cuda", lambda: torch)
+    rng = np.random.default_rng(n_src)
+    ts_src = 0.004 * np.arange(n_src) + 0.002
+    ts_new = np.concatenate([[-0.003, 0.0, ts_src[0]], 0.0035 * np.arange(1, 9), [ts_src[-1], 0.2]])
+    data = rng.standard_normal((3, n_src, 5))
+    want = np.stack([api.linear_interpolate(ts_src, d, ts_new) for d in data])
+    got = resample_linear(torch.as_tensor(data), ts_src, ts_new).numpy()
+    np.testing.assert_allclose(got, want, rtol=1e-13, atol=1e-15)
+
+
+def test_device_edge_padding_equals_numpy(monkeypatch):
+    import torch
+    from pysit_gb300 import _native
+    from pysit_gb300.autograd import _edge_pad
+    monkeypatch.setattr(_native, "require_cuda", lambda: torch)
+    for name in ("o6", "dirichlet", "3d", "1d"):
+        m, *_ = problems.build(api, name)
+        shape = tuple(m.shape(as_grid=True))
+        a = np.random.default_rng(0).standard_normal(shape)
+        pads = [(m.parameters[k].lbc.n, m.parameters[k].rbc.n) for k in range(m.dim)]
+        np.testing.assert_array_equal(_edge_pad(torch.as_tensor(a), m).numpy(), np.pad(a, pads, mode="edge"))
