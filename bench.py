@@ -48,6 +48,16 @@ METRIC = "FWI gradient shots/s, batched adjoint vs plain, 1xGB300 at <=1e-3 rel 
 TRAFFIC_PER_SHOT = {"forward": None, "recompute": 192.0e6 / 22, "adjoint": 326.5e6 / 22}
 
 
+def max_over_ranks(values, device):
+    """Element-wise maximum of per-rank timings over every rank of the process group: the
+    slowest replica sets the time of a multi-GPU step."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.cpu().tolist()]
+
+
 def _peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -306,10 +316,6 @@ def main():
     shots_per_launch = plan.shots_per_launch
     del plan
     torch.cuda.empty_cache()
-    if world > 1:
-        tt = torch.tensor([t_grad], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_grad = float(tt.item())
 
     # ---- e2e: public autograd API, host inputs each step ----------------------------
     fwi = FWIMisfit(solver, shots, obs_host, ts_obs, checkpoint_every=solver.checkpoint_every,
@@ -319,6 +325,8 @@ def main():
         x = C_host.clone().requires_grad_()
         fwi(x).backward()
     torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         x = C_host.clone().requires_grad_()
@@ -328,6 +336,8 @@ def main():
         _ = float(J.item())
     torch.cuda.synchronize()
     t_e2e = (time.perf_counter() - t0) / args.steps
+    if world > 1:
+        t_grad, t_e2e = max_over_ranks([t_grad, t_e2e], "cuda")
     h2d = obs_host.numel() * obs_host.element_size() + C_host.numel() * 4
     d2h = g.numel() * 4 + 8
 
