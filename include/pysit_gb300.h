@@ -37,7 +37,9 @@ extern "C" {
 
 /* Message describing the last error on the calling thread ("" if none). */
 const char* pysit_cuda_last_error(void);
-/* Library ABI version (major*1000 + minor). */
+/* ABI version of this header (major*1000 + minor); pysit_cuda_version() returns the
+ * library's, so a client can check that the two match. */
+#define PYSIT_ABI_VERSION 1000
 int pysit_cuda_version(void);
 
 /* ------------------------------------------------------------------------

@@ -43,4 +43,4 @@ int host_exception(const char* where) noexcept {
 
 extern "C" const char* pysit_cuda_last_error(void) { return pgb::g_msg; }
 
-extern "C" int pysit_cuda_version(void) { return 1000; }
+extern "C" int pysit_cuda_version(void) { return PYSIT_ABI_VERSION; }

@@ -48,6 +48,7 @@ int main(void) {
         printf("create failed %d: %s\n", rc, pysit_cuda_last_error());
         return 1;
     }
+    if (pysit_cuda_version() != PYSIT_ABI_VERSION) return 5;
     if (pysit_plan_workspace_bytes(plan, &bytes) != PYSIT_OK || bytes == 0) return 2;
     /* a run before a workspace is bound is an error, not a crash */
     if (pysit_plan_forward(plan, NULL, NULL) != PYSIT_EINVAL) return 3;

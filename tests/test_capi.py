@@ -35,7 +35,9 @@ def test_every_declared_symbol_is_exported(lib):
 
 
 def test_version_and_empty_error(lib):
-    assert lib.pysit_cuda_version() >= 1000
+    with open(os.path.join(ROOT, "include", "pysit_gb300.h")) as f:
+        header = int(re.search(r"#define PYSIT_ABI_VERSION (\d+)", f.read()).group(1))
+    assert lib.pysit_cuda_version() == header >= 1000
     assert isinstance(lib.pysit_cuda_last_error(), bytes)
 
 
