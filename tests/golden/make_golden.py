@@ -6,6 +6,7 @@ Run in a container that has the reference tree (default /root/reference) after
     python tests/golden/make_golden.py            # all problems of tests/problems.py
     python tests/golden/make_golden.py lbfgs:o2   # the reference's LBFGS run on problem o2
     python tests/golden/make_golden.py born:o2    # Born modelling and Hessian applications on o2
+    python tests/golden/make_golden.py period:o6:2  # the gradient with imaging every 2 steps
 
 For every problem it stores (compressed .npz): the traces of every shot
 modelled on the true model by the reference's own ``generate_seismic_data``
@@ -71,6 +72,21 @@ def run(name):
     np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
     print(f"{name}: shots={len(shots)} nsteps_true={nsteps_true} nsteps0={nsteps0} "
           f"|grad|={np.linalg.norm(out['grad']):.6e} objective={out['objective']:.6e}")
+
+
+def run_period(name, period):
+    """compute_gradient with imaging every `period` steps (temporal_least_squares.py:16-25,
+    forward_model / migrate_shot with imaging_period, temporal_modeling.py:146-148, 313-365)."""
+    pysit = pysit_live.import_pysit()
+    m, shots, solver, C, C0 = problems.build(pysit, name, kernel="cpp")
+    pysit.generate_seismic_data(shots, solver, solver.ModelParameters(m, {"C": C}))
+    obj = pysit.TemporalLeastSquares(solver, imaging_period=period)
+    aux = {"objective_value": (True, None)}
+    grad = obj.compute_gradient(shots, solver.ModelParameters(m, {"C": C0}), aux)
+    out = dict(grad=grad.data.reshape(-1), objective=aux["objective_value"][1], period=period,
+               nsteps0=solver.nsteps)
+    np.savez_compressed(os.path.join(HERE, f"period{period}_{name}.npz"), **out)
+    print(f"period{period}_{name}: |grad|={np.linalg.norm(out['grad']):.6e} objective={out['objective']:.6e}")
 
 
 LBFGS_ITERS = 5
@@ -160,5 +176,8 @@ if __name__ == "__main__":
             run_lbfgs(n.split(":", 1)[1])
         elif n.startswith("born:"):
             run_born(n.split(":", 1)[1])
+        elif n.startswith("period:"):
+            _, prob, per = n.split(":")
+            run_period(prob, int(per))
         else:
             run(n)

@@ -83,12 +83,18 @@ def test_fp32_batched_gradient_within_tolerance(name, golden):
     assert _rel(grad.data, g["grad"]) < 1e-3
 
 
-@pytest.mark.parametrize("p", [2, 3])
-def test_imaging_period_matches_oracle(p, golden):
-    g = golden("o6")
-    m, shots, solver, C, C0 = _setup("o6", g)
+@pytest.mark.parametrize("name,p", [("o6", 2), ("o6", 3), ("3d", 2)])
+def test_imaging_period_matches_reference(name, p, golden):
+    """Imaging every p steps: the reference's own gradient (tests/golden/period<p>_<name>.npz)
+    and the oracle's."""
+    g = golden(name)
+    m, shots, solver, C, C0 = _setup(name, g)
+    aux = {"objective_value": (True, None)}
     grad = api.TemporalLeastSquares(solver, imaging_period=p).compute_gradient(
-        shots, solver.ModelParameters(m, {"C": C0}))
+        shots, solver.ModelParameters(m, {"C": C0}), aux)
+    gp = golden(f"period{p}_{name}")
+    assert _rel(grad.data, gp["grad"]) < 1e-9
+    assert aux["objective_value"][1] == pytest.approx(float(gp["objective"]), rel=1e-10)
     Ps = [problems.oracle_problem(solver, s) for s in shots]
     dobs = [s.receivers.interpolate_data(solver.ts()) for s in shots]
     ref, _ = pipeline.gradient(Ps, dobs, imaging_period=p)

@@ -118,3 +118,21 @@ def test_oracle_rejects_bad_arguments():
     z = np.zeros(10)
     with pytest.raises(ValueError):
         pipeline.step("oracle", 1, 5, z, {"Phiz": z}, z, z + 1, z, [(z[:0], z[:0])], 1e-3, [1.0], [10])
+
+
+@pytest.mark.parametrize("name,period", [("o6", 2), ("o6", 3), ("3d", 2)])
+def test_oracle_imaging_period_matches_reference_golden(name, period, golden):
+    """The gradient with imaging every `period` steps against the reference's own run
+    (TemporalLeastSquares(solver, imaging_period=period), tests/golden/period<p>_<name>.npz)."""
+    g, gp = golden(name), golden(f"period{period}_{name}")
+    m, shots, solver, C, C0 = problems.build(api, name)
+    ts_true = np.arange(int(g["nsteps_true"])) * float(g["dt_true"])
+    for s, d in zip(shots, g["traces"]):
+        s.reset_time_series(ts_true)
+        s.receivers.data[:] = d
+    solver.model_parameters = solver.ModelParameters(m, {"C": C0})
+    assert solver.nsteps == int(gp["nsteps0"])
+    dobs = [s.receivers.interpolate_data(solver.ts()) for s in shots]
+    grad, r2 = pipeline.gradient([problems.oracle_problem(solver, s) for s in shots], dobs, imaging_period=period)
+    assert _rel(grad, gp["grad"]) < 1e-11
+    assert 0.5 * r2 * solver.dt == pytest.approx(float(gp["objective"]), rel=1e-12)
