@@ -7,6 +7,7 @@ Run in a container that has the reference tree (default /root/reference) after
     python tests/golden/make_golden.py lbfgs:o2   # the reference's LBFGS run on problem o2
     python tests/golden/make_golden.py born:o2    # Born modelling and Hessian applications on o2
     python tests/golden/make_golden.py period:o6:2  # the gradient with imaging every 2 steps
+    python tests/golden/make_golden.py fwd:o2     # forward_model's wavefield and dWaveOp snapshots
 
 For every problem it stores (compressed .npz): the traces of every shot
 modelled on the true model by the reference's own ``generate_seismic_data``
@@ -87,6 +88,23 @@ def run_period(name, period):
                nsteps0=solver.nsteps)
     np.savez_compressed(os.path.join(HERE, f"period{period}_{name}.npz"), **out)
     print(f"period{period}_{name}: |grad|={np.linalg.norm(out['grad']):.6e} objective={out['objective']:.6e}")
+
+
+def run_fwd(name):
+    """forward_model(shot 0, true model, imaging_period 1, ['simdata', 'wavefield', 'dWaveOp'])
+    (temporal_modeling.py:60-169): the wavefield (unpadded, before the step) and dWaveOp (padded,
+    after it) at four steps."""
+    pysit = pysit_live.import_pysit()
+    m, shots, solver, C, C0 = problems.build(pysit, name, kernel="cpp")
+    tm = pysit.TemporalModeling(solver)
+    rv = tm.forward_model(shots[0], solver.ModelParameters(m, {"C": C}), 1, ["simdata", "wavefield", "dWaveOp"])
+    n = solver.nsteps
+    ks = np.array([1, n // 3, 2 * n // 3, n - 1])
+    out = dict(steps=ks, simdata=rv["simdata"], nsteps=n, dt=solver.dt,
+               wavefield=np.stack([np.ravel(rv["wavefield"][k]) for k in ks]),
+               dwaveop=np.stack([np.ravel(rv["dWaveOp"][k]) for k in ks]))
+    np.savez_compressed(os.path.join(HERE, f"fwd_{name}.npz"), **out)
+    print(f"fwd_{name}: nsteps={n} |dWaveOp snapshots|={np.linalg.norm(out['dwaveop']):.6e}")
 
 
 LBFGS_ITERS = 5
@@ -176,6 +194,8 @@ if __name__ == "__main__":
             run_lbfgs(n.split(":", 1)[1])
         elif n.startswith("born:"):
             run_born(n.split(":", 1)[1])
+        elif n.startswith("fwd:"):
+            run_fwd(n.split(":", 1)[1])
         elif n.startswith("period:"):
             _, prob, per = n.split(":")
             run_period(prob, int(per))

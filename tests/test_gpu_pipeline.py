@@ -136,6 +136,11 @@ def test_forward_model_outputs_match_oracle(golden):
     assert len(rv["wavefield"]) == solver.nsteps
     fast = tm.forward_model(shots[0], m1, 1, ["simdata"])["simdata"]
     assert _rel(fast, sim) < 1e-11
+    # the reference's own forward_model snapshots (unpadded wavefield, padded dWaveOp)
+    f = golden("fwd_o2")
+    ks = f["steps"]
+    assert _rel(np.stack([np.ravel(rv["wavefield"][k]) for k in ks]), f["wavefield"]) < 1e-11
+    assert _rel(np.stack([np.ravel(rv["dWaveOp"][k]) for k in ks]), f["dwaveop"]) < 1e-10
 
 
 def test_time_step_on_host_solver_data_matches_oracle():

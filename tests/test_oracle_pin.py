@@ -136,3 +136,16 @@ def test_oracle_imaging_period_matches_reference_golden(name, period, golden):
     grad, r2 = pipeline.gradient([problems.oracle_problem(solver, s) for s in shots], dobs, imaging_period=period)
     assert _rel(grad, gp["grad"]) < 1e-11
     assert 0.5 * r2 * solver.dt == pytest.approx(float(gp["objective"]), rel=1e-12)
+
+
+@pytest.mark.parametrize("name", ["o2", "3d", "1d"])
+def test_oracle_dwaveop_matches_reference_forward_model(name, golden):
+    """dWaveOp (constant_density_acoustic_base.py:24-40) of the oracle's forward loop against
+    the reference's forward_model snapshots (tests/golden/fwd_<name>.npz)."""
+    f = golden(f"fwd_{name}")
+    m, shots, solver, C, C0 = problems.build(api, name)
+    solver.model_parameters = solver.ModelParameters(m, {"C": C})
+    assert solver.nsteps == int(f["nsteps"])
+    sim, dws = pipeline.forward(problems.oracle_problem(solver, shots[0]), want_dwaveop=True)
+    assert _rel(sim, f["simdata"]) < 1e-12
+    assert _rel(np.stack([dws[k] for k in f["steps"]]), f["dwaveop"]) < 1e-12
