@@ -8,6 +8,7 @@ Run in a container that has the reference tree (default /root/reference) after
     python tests/golden/make_golden.py born:o2    # Born modelling and Hessian applications on o2
     python tests/golden/make_golden.py period:o6:2  # the gradient with imaging every 2 steps
     python tests/golden/make_golden.py fwd:o2     # forward_model's wavefield and dWaveOp snapshots
+    python tests/golden/make_golden.py mig:o6     # migrate_shot of a seeded operand
 
 For every problem it stores (compressed .npz): the traces of every shot
 modelled on the true model by the reference's own ``generate_seismic_data``
@@ -107,6 +108,22 @@ def run_fwd(name):
     print(f"fwd_{name}: nsteps={n} |dWaveOp snapshots|={np.linalg.norm(out['dwaveop']):.6e}")
 
 
+def run_mig(name):
+    """migrate_shot (temporal_modeling.py:171-214) of shot 0 at the starting model for a seeded
+    data-space operand, imaging every step and every second step."""
+    pysit = pysit_live.import_pysit()
+    m, shots, solver, C, C0 = problems.build(pysit, name, kernel="cpp")
+    m0 = solver.ModelParameters(m, {"C": C0})
+    solver.model_parameters = m0
+    tm = pysit.TemporalModeling(solver)
+    op = np.random.default_rng(0).standard_normal((solver.nsteps, shots[0].receivers.receiver_count))
+    out = dict(operand=op, nsteps=solver.nsteps)
+    for p in (1, 2):
+        out[f"image_p{p}"] = np.ravel(tm.migrate_shot(shots[0], m0, op, p).data)
+    np.savez_compressed(os.path.join(HERE, f"mig_{name}.npz"), **out)
+    print(f"mig_{name}: nsteps={solver.nsteps} |image|={np.linalg.norm(out['image_p1']):.6e}")
+
+
 LBFGS_ITERS = 5
 
 
@@ -194,6 +211,8 @@ if __name__ == "__main__":
             run_lbfgs(n.split(":", 1)[1])
         elif n.startswith("born:"):
             run_born(n.split(":", 1)[1])
+        elif n.startswith("mig:"):
+            run_mig(n.split(":", 1)[1])
         elif n.startswith("fwd:"):
             run_fwd(n.split(":", 1)[1])
         elif n.startswith("period:"):

@@ -111,15 +111,20 @@ def test_schedule_variants_agree(kw, golden):
 
 
 def test_migrate_batched_equals_plain(golden):
+    """Both migration paths against each other and against the reference's migrate_shot of the
+    same operand (tests/golden/mig_o6.npz)."""
     g = golden("o6")
     m, shots, solver, C, C0 = _setup("o6", g)
     m0 = solver.ModelParameters(m, {"C": C0})
-    rng = np.random.default_rng(0)
     solver.model_parameters = m0
-    op = rng.standard_normal((solver.nsteps, shots[0].receivers.receiver_count))
+    f = golden("mig_o6")
+    op = f["operand"]
+    assert op.shape == (solver.nsteps, shots[0].receivers.receiver_count)
     a = api.TemporalModeling(solver, batched=True).migrate_shot(shots[0], m0, op, 1)
     b = api.TemporalModeling(solver, batched=False).migrate_shot(shots[0], m0, op, 1)
     assert _rel(a.data, b.data) < 1e-10
+    assert _rel(a.data, f["image_p1"]) < 1e-9
+    assert _rel(b.data, f["image_p1"]) < 1e-9
 
 
 def test_forward_model_outputs_match_oracle(golden):

@@ -149,3 +149,18 @@ def test_oracle_dwaveop_matches_reference_forward_model(name, golden):
     sim, dws = pipeline.forward(problems.oracle_problem(solver, shots[0]), want_dwaveop=True)
     assert _rel(sim, f["simdata"]) < 1e-12
     assert _rel(np.stack([dws[k] for k in f["steps"]]), f["dwaveop"]) < 1e-12
+
+
+@pytest.mark.parametrize("name", ["o6", "3d"])
+@pytest.mark.parametrize("period", [1, 2])
+def test_oracle_migration_matches_reference(name, period, golden):
+    """fold(adjoint image) of a seeded operand against the reference's migrate_shot
+    (tests/golden/mig_<name>.npz)."""
+    f = golden(f"mig_{name}")
+    m, shots, solver, C, C0 = problems.build(api, name)
+    solver.model_parameters = solver.ModelParameters(m, {"C": C0})
+    assert solver.nsteps == int(f["nsteps"])
+    P = problems.oracle_problem(solver, shots[0])
+    _, dws = pipeline.forward(P, True, period)
+    image = pipeline.fold(P, pipeline.adjoint_image(P, f["operand"], dws, period))
+    assert _rel(image, f[f"image_p{period}"]) < 1e-12
