@@ -40,7 +40,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "FWI gradient shots/s, batched adjoint vs plain, 1xGB300 at <=1e-3 rel err; Gcell/s"
+METRIC = "FWI gradient shots/s, batched adjoint vs plain, 1\u00d7GB300 at \u22641e-3 rel err; Gcell/s"
 # DRAM bytes (read + write) per shot of a launch of each 2D step (interior + PML-shell kernels),
 # from ncu captures of the same kernels at 22 shots per launch and task length 16
 # (profiles/wave2d_steps_cfg2_22shots_dram.md); a launch's traffic is this times its shots (the
