@@ -165,8 +165,9 @@ def test_bulk_copy_2d_variant_agrees(monkeypatch, precision, tol, schedule):
 
 def test_fp32_gradient_of_the_2d_workload_within_1e3_of_fp64():
     """The bench's claim at a size the FP64 path finishes in seconds: the 2D workload at a
-    quarter of its size (288 x 96 cells + 10-cell PML, 16 shots, 1000 steps, order 8), kept
-    schedule, FP32 against FP64 (the FP64 path is held to the oracle by the pipeline tests)."""
+    quarter of its size (288 x 96 cells + 10-cell PML, 16 shots, 1000 steps, order 8), FP32
+    against FP64 (the FP64 path is held to the oracle by the pipeline tests).  It runs the kept
+    schedule; the checkpointed one gives the same gradient to the last bit (tests above)."""
     import torch
     from pysit_gb300 import workloads
     from pysit_gb300.autograd import resample_linear
