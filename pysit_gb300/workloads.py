@@ -140,7 +140,10 @@ def cfg3(scale=1.0, nshots=8, nsteps=3000, order=8, precision="single", cfl=0.35
     Its PML amplitude (1e-3 reflection over 20 cells) makes the reference's 3D
     step diverge (C^2 on sigma_x sigma_y sigma_z psi, _3D.h:219), so the workload
     uses the consistent form by default; ``pml_psi="reference"`` reproduces the
-    reference's step."""
+    reference's step.  Checkpoints every sqrt(nsteps) steps (55 for 3000) unless
+    ``checkpoint_every`` is given."""
+    if checkpoint_every is None:
+        checkpoint_every = max(1, int(round(math.sqrt(nsteps))))
     nx, ny, nz = (max(12, int(round(n * scale))) for n in (400, 400, 300))
     npml = max(4, int(round(20 * scale)))
     dx = 15.0

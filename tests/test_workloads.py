@@ -46,6 +46,7 @@ def test_3d_gradient_workload_scaled():
     nx, ny, nz = m.shape(as_grid=True)
     assert (nx, ny, nz) == (40, 40, 30) and tuple(m.deltas) == (15.0, 15.0, 15.0)
     assert solver.spatial_accuracy_order == 8 and solver.dtype == np.float32
+    assert solver.checkpoint_every == 55  # sqrt(3000)
     assert len(shots) == 8 and {s.receivers.receiver_count for s in shots} == {min(100, nx) * min(100, ny)}
     assert {_ricker_hz(s) for s in shots} == {6.0}
     assert np.any(C == 4500.0) and 1500.0 <= C.min()  # the salt body at 4500 m/s
