@@ -1,7 +1,7 @@
 """Physical domain and boundary conditions (mirror of pysit.core.domain).
 
 Same public names and argument meaning as the reference:
-``RectangularDomain(*configs)`` with one ``(lbound, rbound, lbc, rbc[, unit])``
+``RectangularDomain(*axis_configs)`` with one ``(lbound, rbound, lbc, rbc[, unit])``
 tuple per axis (pysit/core/domain.py:36-134), and the boundary conditions
 ``Dirichlet()`` and ``PML(length, amplitude, ftype='quadratic', boundary='dirichlet',
 compact=False)`` (pysit/core/domain.py:154-254).  Axes are ordered (x, [y,] z)
@@ -77,16 +77,16 @@ class PML(DomainBC):
 
 
 class RectangularDomain:
-    """Rectangular domain; ``configs`` = one (lbound, rbound, lbc, rbc[, unit]) per axis."""
+    """Rectangular domain; ``axis_configs`` = one (lbound, rbound, lbc, rbc[, unit]) per axis."""
     type = "rectangular"
 
-    def __init__(self, *configs):
-        if not 1 <= len(configs) <= 3:
+    def __init__(self, *axis_configs):
+        if not 1 <= len(axis_configs) <= 3:
             raise ValueError("Domain construction must be between one and three dimensions.")
-        self.dim = len(configs)
+        self.dim = len(axis_configs)
         self.parameters = {}
         for i, key in enumerate(_AXES[self.dim]):
-            cfg = configs[i]
+            cfg = axis_configs[i]
             if len(cfg) == 4:
                 L, R, lbc, rbc = cfg
                 unit = None

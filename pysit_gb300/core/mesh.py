@@ -83,16 +83,16 @@ class CartesianMesh:
     """Structured Cartesian mesh over a RectangularDomain."""
     type = "structured-cartesian"
 
-    def __init__(self, domain, *configs):
-        if not 1 <= len(configs) <= 3:
+    def __init__(self, domain, *axis_nodes):
+        if not 1 <= len(axis_nodes) <= 3:
             raise ValueError("Mesh dimension must be between 1 and 3.")
-        if len(configs) != domain.dim:
+        if len(axis_nodes) != domain.dim:
             raise ValueError("Mesh dimension must match domain dimension.")
         self.domain = domain
         self.dim = domain.dim
         self.parameters = {}
         for i, key in enumerate(_AXES[self.dim]):
-            n = int(configs[i])
+            n = int(axis_nodes[i])
             delta = domain.parameters[i].length / (n - 1)
             p = Bunch(n=n, delta=delta)
             p.lbc = _mesh_bc(self, domain.parameters[i].lbc, i, "left", delta)
