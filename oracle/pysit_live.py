@@ -1,8 +1,8 @@
 """TEST INFRASTRUCTURE: import the unmodified reference package (PySIT) in-process.
 
 Only tests/ and tests/golden/make_golden.py use this module, as a checker.  It
-never runs on the GPU host (the reference tree is not there) and the product
-(pysit_gb300) never imports it.
+runs only where the reference tree exists, and the product (pysit_gb300) never
+imports it.
 
 What it does, without writing to the read-only reference tree:
   * adds the numpy aliases removed in numpy >= 1.24 that the reference still uses

@@ -15,8 +15,8 @@ axis to ``./shots_time/shot_<i>.<ext>`` and ``ts_<i>.<ext>`` (i from 1), and
   savemat  one MATLAB variable per file, named by the file's own path as the reference
            names it, so either side reads the other's files;
   h5py     one dataset per file, named by the file's path (needs h5py).
-The directory is replaced on every save, as the reference does.  ``path`` (a keyword of
-this build) moves it.
+The directory is replaced on every save, as the reference does.  ``path`` (a keyword the
+reference does not have) moves it.
 """
 from __future__ import annotations
 

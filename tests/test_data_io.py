@@ -1,9 +1,9 @@
 """Observed-data files: generate_seismic_data(save_method=...) and
 generate_seismic_data_from_file (pysit/modeling/data_modeling.py:59-173, 180-333).
 
-Round trips of this build's writer and reader ('pickle', 'savemat'; 'h5py' where h5py is
+Round trips of pysit_gb300's writer and reader ('pickle', 'savemat'; 'h5py' where h5py is
 installed), and the file format against the reference itself: a 'savemat' directory
-written by the reference's generate_seismic_data is read by this build, and one written
+written by the reference's generate_seismic_data is read by pysit_gb300, and one written
 here is read by the reference's generate_seismic_data_from_file (tests run where the
 reference tree is present).  Data are set on the host, so no GPU is needed.
 """
@@ -66,7 +66,7 @@ def ref():
 
 def test_savemat_files_are_exchangeable_with_the_reference(ref, tmp_path, monkeypatch):
     monkeypatch.chdir(tmp_path)
-    # reference writes (its cpp solver models the data), this build reads
+    # reference writes (its cpp solver models the data), pysit_gb300 reads
     rm, rshots, rsolver, C, C0 = problems.build(ref, "o2", kernel="cpp")
     ref.generate_seismic_data(rshots, rsolver, rsolver.ModelParameters(rm, {"C": C}), save_method="savemat")
     m, shots, solver = _shots()
@@ -74,7 +74,7 @@ def test_savemat_files_are_exchangeable_with_the_reference(ref, tmp_path, monkey
     for a, b in zip(rshots, shots):
         np.testing.assert_array_equal(b.receivers.data, a.receivers.data)
         np.testing.assert_array_equal(b.receivers.ts, a.receivers.ts)
-    # this build writes, the reference reads
+    # pysit_gb300 writes, the reference reads
     m, mine, solver = _shots(seed=5)
     save_shot_data(mine, "savemat")
     ref.generate_seismic_data_from_file(rshots, rsolver, save_method="savemat")

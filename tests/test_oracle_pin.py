@@ -2,7 +2,7 @@
 
 * the C restatement of the step (oracle/cda_oracle.c) against the reference's own
   templates compiled from its headers into oracle/_ref (skipped where the reference
-  tree is absent, i.e. on the GPU host);
+  tree is absent);
 * the oracle pipeline (forward, adjoint, gradient) plus pysit_gb300's host-side
   geometry against golden outputs of the unmodified reference (tests/golden/).
 """
