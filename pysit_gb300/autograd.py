@@ -102,6 +102,11 @@ class FWIMisfit:
         self.shots = list(shots)
         self.observed = observed  # [nshots, nt_obs, nrec] torch tensor (host pinned or device)
         self.ts_observed = np.asarray(ts_observed, dtype=float)
+        shape = tuple(observed.shape)
+        nrec = max(s.receivers.receiver_count for s in self.shots)
+        if len(shape) != 3 or shape != (len(self.shots), len(self.ts_observed), nrec):
+            raise ValueError(f"observed data of shape {shape} do not fit {len(self.shots)} shots, "
+                             f"{len(self.ts_observed)} samples and {nrec} receivers (the most of any shot)")
         self.imaging_period = imaging_period
         self.plan_kw = plan_kw
         self._fn = None

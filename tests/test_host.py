@@ -274,3 +274,16 @@ def test_device_edge_padding_equals_numpy(monkeypatch):
         a = np.random.default_rng(0).standard_normal(shape)
         pads = [(m.parameters[k].lbc.n, m.parameters[k].rbc.n) for k in range(m.dim)]
         np.testing.assert_array_equal(_edge_pad(torch.as_tensor(a), m).numpy(), np.pad(a, pads, mode="edge"))
+
+
+def test_fwi_misfit_checks_the_observed_data_shape():
+    import torch
+    from pysit_gb300.autograd import FWIMisfit
+    m, shots, solver, C, C0 = problems.build(api, "o2")
+    nrec = shots[0].receivers.receiver_count
+    ts = np.arange(50) * 1e-3
+    FWIMisfit(solver, shots, torch.zeros((len(shots), 50, nrec)), ts)
+    for bad in ((len(shots) + 1, 50, nrec), (len(shots), 49, nrec), (len(shots), 50, nrec + 1),
+                (len(shots), 50, nrec - 1), (50, nrec)):
+        with pytest.raises(ValueError):
+            FWIMisfit(solver, shots, torch.zeros(bad), ts)
