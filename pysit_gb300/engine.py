@@ -11,8 +11,11 @@ pysit/objective_functions/temporal_least_squares.py:27-198).
 """
 from __future__ import annotations
 
+import ast
 import ctypes as C
+import json
 import math
+import os
 import weakref
 
 import numpy as np
@@ -25,10 +28,67 @@ __all__ = ["WavePlan", "PlanGroup", "padded_cells", "default_checkpoint_every"]
 _DESC_AXIS = {1: [2], 2: [0, 2], 3: [0, 1, 2]}  # mesh axis -> (x, y, z) slot of the descriptor
 
 # tunings chosen by WavePlan.autotune (task length along x, 2D shell block shares per step
-# mode), per (dim, order, padded grid, dtype, shots per launch, psi form, schedule); later
-# plans of the same configuration start from them
+# mode), per (dim, order, padded grid, dtype, psi form, shots per launch, schedule, forward
+# only, lanes); later plans of the same configuration start from them.  With the environment
+# variable PYSIT_CUDA_TUNE_CACHE naming a JSON file, the table is read from that file on first
+# use and written back after every new tuning, so later processes on the machine start from it.
 _TUNED = {}
+_TUNE_FILES_READ = set()
 TILE_CANDIDATES = {2: (8, 16, 32, 64), 3: (8, 16, 32, 64)}
+
+
+def _tune_cache_file():
+    return os.environ.get("PYSIT_CUDA_TUNE_CACHE") or None
+
+
+def _read_tunings(path):
+    """Tunings stored in `path` ({} for a missing or unreadable file; bad rows are skipped)."""
+    try:
+        with open(path) as f:
+            rows = json.load(f)
+    except (OSError, ValueError):
+        return {}
+    out = {}
+    for row in rows if isinstance(rows, list) else []:
+        try:
+            key, tile, share = row
+            out[ast.literal_eval(key)] = (int(tile), tuple(float(v) for v in share))
+        except (ValueError, SyntaxError, TypeError):
+            continue
+    return out
+
+
+def _write_tunings(path, table):
+    rows = [[repr(k), v[0], list(v[1])] for k, v in table.items()]
+    tmp = f"{path}.{os.getpid()}.tmp"
+    with open(tmp, "w") as f:
+        json.dump(rows, f)
+    os.replace(tmp, path)  # readers see the old file or the new one, never a partial one
+
+
+def _plain_key(key):
+    """The tuning key with numpy scalars as Python numbers (so that its repr reads back)."""
+    if isinstance(key, tuple):
+        return tuple(_plain_key(v) for v in key)
+    return key.item() if isinstance(key, np.generic) else key
+
+
+def _tuning_get(key):
+    key = _plain_key(key)
+    path = _tune_cache_file()
+    if path and path not in _TUNE_FILES_READ:
+        _TUNE_FILES_READ.add(path)
+        for k, v in _read_tunings(path).items():
+            _TUNED.setdefault(k, v)
+    return _TUNED.get(key)
+
+
+def _tuning_put(key, value):
+    key = _plain_key(key)
+    _TUNED[key] = value
+    path = _tune_cache_file()
+    if path:
+        _write_tunings(path, {**_read_tunings(path), **_TUNED})
 
 
 def padded_cells(mesh, cells):
@@ -185,7 +245,7 @@ class WavePlan:
         self.gradient_schedule = gradient_schedule
         # the tuning key knows the launch size and schedule only now
         self._tune_key = self._tune_key + (self.shots_per_launch, gradient_schedule, self.forward_only, self.lanes)
-        tuned = _TUNED.get(self._tune_key)
+        tuned = _tuning_get(self._tune_key)
         d.tile_x = tuned[0] if tuned else 0
         for k in range(3):
             d.shell_share[k] = tuned[1][k] if tuned else 0.0
@@ -382,7 +442,7 @@ class WavePlan:
         tile, share = C.c_int(), (C.c_double * 3)()
         _native.check(_native.load().pysit_plan_get_tuning(self._h, C.byref(tile), share))
         self.shell_share = [float(v) for v in share]
-        _TUNED[self._tune_key] = (self.tile_x, tuple(self.shell_share))
+        _tuning_put(self._tune_key, (self.tile_x, tuple(self.shell_share)))
         return {"chosen": self.tile_x, "ms": dict(zip(cand, list(ms))), "shell_share": self.shell_share}
 
     def step_loop(self, mode, nsteps):
@@ -536,7 +596,7 @@ def plan_for(solver, shots, imaging_period=1, **kw):
             cache.clear()
             _native.require_cuda().cuda.empty_cache()
         p = WavePlan(solver, shots, imaging_period=imaging_period, **kw)
-        if getattr(solver, "autotune", False) and p._tune_key not in _TUNED:
+        if getattr(solver, "autotune", False) and _tuning_get(p._tune_key) is None:
             p.autotune()
         cache[key] = p
     return p

@@ -287,3 +287,29 @@ def test_fwi_misfit_checks_the_observed_data_shape():
                 (len(shots), 50, nrec - 1), (50, nrec)):
         with pytest.raises(ValueError):
             FWIMisfit(solver, shots, torch.zeros(bad), ts)
+
+
+def test_tuning_cache_file_round_trip(monkeypatch, tmp_path):
+    """PYSIT_CUDA_TUNE_CACHE: a tuning written by one process is found by the next; an
+    unreadable file is ignored; without the variable nothing is written."""
+    from pysit_gb300 import engine
+    key = (2, 8, (1232, 464), str(np.float32), 0, np.int64(22), "store", False, 1)
+    value = (16, (0.25, 0.3, 0.35))
+    path = tmp_path / "tunings.json"
+    monkeypatch.setattr(engine, "_TUNED", {})
+    monkeypatch.setattr(engine, "_TUNE_FILES_READ", set())
+    monkeypatch.delenv("PYSIT_CUDA_TUNE_CACHE", raising=False)
+    engine._tuning_put(key, value)
+    assert not path.exists() and engine._tuning_get(key) == value
+    monkeypatch.setenv("PYSIT_CUDA_TUNE_CACHE", str(path))
+    engine._tuning_put(key, value)
+    assert path.exists()
+    # a later process: empty in-memory table, same file
+    monkeypatch.setattr(engine, "_TUNED", {})
+    monkeypatch.setattr(engine, "_TUNE_FILES_READ", set())
+    assert engine._tuning_get(key) == value
+    assert engine._tuning_get(key[:-1] + (2,)) is None
+    path.write_text("not json")
+    monkeypatch.setattr(engine, "_TUNED", {})
+    monkeypatch.setattr(engine, "_TUNE_FILES_READ", set())
+    assert engine._tuning_get(key) is None
