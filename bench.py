@@ -216,6 +216,7 @@ def main():
                     help="gradient schedule: recompute from checkpoints, or keep dWaveOp in HBM")
     ap.add_argument("--lanes", type=int, default=None, help="concurrent shot lanes (default: the schedule's choice)")
     ap.add_argument("--cpu-sample", type=int, default=40)
+    ap.add_argument("--cpu-procs", type=int, default=None, help="processes of the CPU port (default: all cores)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain per-shot FP64 GPU path")
     ap.add_argument("--no-kept", action="store_true", help="skip timing the kept-dWaveOp schedule")
@@ -236,7 +237,7 @@ def main():
             return
         vals = []
         for i in range(args.warmup + args.steps):
-            cb = cpu_baseline(nsample=args.cpu_sample, scale=args.scale, nsteps_full=args.nsteps)
+            cb = cpu_baseline(nsample=args.cpu_sample, procs=args.cpu_procs, scale=args.scale, nsteps_full=args.nsteps)
             if i >= args.warmup:
                 vals.append(cb["value"])
         v = float(np.median(vals))
@@ -408,7 +409,8 @@ def main():
         plain["batched_over_plain"] = line["value"] / world / plain["value"]
         line["plain_fp64"] = plain
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(nsample=args.cpu_sample, scale=args.scale, nsteps_full=args.nsteps)
+        line["cpu_baseline"] = cpu_baseline(nsample=args.cpu_sample, procs=args.cpu_procs, scale=args.scale,
+                                            nsteps_full=args.nsteps)
     if world == 1 and config.get("gradient_schedule") == "checkpoint" and not args.no_kept:
         try:
             line["kept_schedule"] = kept_schedule_leg(solver, shots, obs_host, ts_obs, args.steps, args.warmup,

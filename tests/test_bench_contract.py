@@ -7,8 +7,8 @@ import subprocess
 import sys
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-ARGS = ["--impl", "reference", "--scale", "0.05", "--nsteps", "8", "--cpu-sample", "4", "--steps", "1",
-        "--warmup", "1"]
+ARGS = ["--impl", "reference", "--scale", "0.05", "--nsteps", "8", "--cpu-sample", "4", "--cpu-procs", "2",
+        "--steps", "1", "--warmup", "1"]
 
 
 def _run(extra_env=None):
@@ -29,7 +29,7 @@ def test_reference_arm_prints_one_json_line():
     assert d["metric"] == bench.METRIC == "FWI gradient shots/s, batched adjoint vs plain, 1\u00d7GB300 at \u22641e-3 rel err; Gcell/s"
     assert d["unit"] == "shots/s" and d["higher_is_better"] is True and d["value"] > 0
     cb = d["cpu_baseline"]
-    assert cb["value"] == d["value"] and cb["kind"] == "port" and cb["cores"] >= 1 and cb["sample"]
+    assert cb["value"] == d["value"] and cb["kind"] == "port" and cb["cores"] == 2 and cb["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": "shots/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     assert d["config"]["workload"].startswith("cfg2")
 
