@@ -102,21 +102,121 @@ def _peaks():
 # ---------------------------------------------------------------------------
 # CPU baseline: the oracle port (test infrastructure) on a bounded sample
 # ---------------------------------------------------------------------------
+_CPU_PROBLEM = {}  # per worker process: the sample problem, built once
+
+
 def _cpu_worker(args):
     scale, nsample, order = args
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    key = (scale, nsample, order)
+    if key not in _CPU_PROBLEM:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import problems
+        from pysit_gb300 import workloads
+        m, shots, solver, C, C0 = workloads.cfg2(scale=scale, nshots=1, nsteps=nsample, order=order,
+                                                 precision="double")
+        solver.model_parameters = solver.ModelParameters(m, {"C": C0})
+        _CPU_PROBLEM[key] = problems.oracle_problem(solver, shots[0])
     import pipeline
-    import problems
-    from pysit_gb300 import workloads
-    m, shots, solver, C, C0 = workloads.cfg2(scale=scale, nshots=1, nsteps=nsample, order=order,
-                                             precision="double")
-    solver.model_parameters = solver.ModelParameters(m, {"C": C0})
-    P = problems.oracle_problem(solver, shots[0])
+    P = _CPU_PROBLEM[key]
     t0 = time.perf_counter()
     sim, dws = pipeline.forward(P, want_dwaveop=True)
     pipeline.adjoint_image(P, np.random.default_rng(0).standard_normal(sim.shape) * 1e-3, dws)
     return time.perf_counter() - t0
+
+
+def _mem_available():
+    """Bytes of host memory available to new processes (MemAvailable), or None."""
+    try:
+        with open("/proc/meminfo") as f:
+            for line in f:
+                if line.startswith("MemAvailable:"):
+                    return int(line.split()[1]) * 1024
+    except OSError:
+        pass
+    return None
+
+
+class CpuBaseline:
+    """Shots/s of the CPU port of the reference pipeline (forward with the per-step dWaveOp list,
+    adjoint with imaging, FP64, oracle/cda_oracle.c): P worker processes, each one shot-gradient
+    of `nsample` of the record's `nsteps_full` steps, extrapolated to the full record.  The
+    reference's cpp kernels are serial, so shot-level processes are its own parallel model
+    (ParallelWrapShot); P is the host's cores, bounded by the RAM the reference's dWaveOp list
+    would hold for a full record (nsteps_full x padded cells x 8 B per in-flight shot,
+    temporal_modeling.py:146-148).  The pool and each worker's problem live across samples."""
+
+    def __init__(self, nsample=400, procs=None, scale=1.0, nsteps_full=4000, order=8):
+        self.nsample, self.scale, self.nsteps_full, self.order = nsample, scale, nsteps_full, order
+        nx, nz = max(16, int(round(1152 * scale))), max(12, int(round(384 * scale)))
+        npml = max(4, int(round(40 * scale)))
+        self.dwaveop_bytes = nsteps_full * (nx + 2 * npml) * (nz + 2 * npml) * 8
+        self.cores = os.cpu_count() or 1
+        mem = _mem_available()
+        self.p_ram = max(1, int(0.9 * mem // self.dwaveop_bytes)) if mem else None
+        self.mem_gb = mem / 1e9 if mem else None
+        self.procs = procs or max(1, min(self.cores, 64, self.p_ram or self.cores))
+        self.pool = mp.get_context("spawn").Pool(self.procs)
+
+    def close(self):
+        self.pool.close()
+        self.pool.join()
+
+    def sample(self, nsample=None):
+        """One sample: every process runs its shot-gradient; returns (shots/s, wall seconds)."""
+        n = nsample or self.nsample
+        t0 = time.perf_counter()
+        times = self.pool.map(_cpu_worker, [(self.scale, n, self.order)] * self.procs)
+        wall = time.perf_counter() - t0
+        per_shot = max(times) * self.nsteps_full / n
+        return self.procs / per_shot, wall
+
+    def describe(self, value, wall):
+        return dict(value=value, unit="shots/s", cores=self.procs, kind="port",
+                    sample=f"{self.procs} processes x 1 shot-gradient of {self.nsample} of {self.nsteps_full} steps "
+                           f"(forward + dWaveOp list + adjoint + imaging, FP64, oracle/cda_oracle.c), extrapolated "
+                           f"to the full record; wall {wall:.1f}s per sample",
+                    host_cores=self.cores, processes_ram_bound=self.p_ram,
+                    dwaveop_gb_per_shot=self.dwaveop_bytes / 1e9, mem_available_gb=self.mem_gb)
+
+
+def cpu_baseline(nsample=400, procs=None, scale=1.0, nsteps_full=4000, order=8):
+    """One sample of CpuBaseline, described for the bench line."""
+    cb = CpuBaseline(nsample, procs, scale, nsteps_full, order)
+    try:
+        v, wall = cb.sample()
+    finally:
+        cb.close()
+    return cb.describe(v, wall)
+
+
+def accuracy_vs_fp64(obs_host, ts_obs, scale, nshots, nsteps, nshots_check=8):
+    """The metric's accuracy on the benchmarked configuration: the FP32 and the FP64 batched
+    gradients (checkpointed as the bench runs) of `nshots_check` shots spread over the batch,
+    all record steps, from the same observed data; relative L2 errors of the FP32 gradient and
+    misfit against FP64 (the FP64 path is held to the oracle by the parity tests)."""
+    import torch
+    from pysit_gb300 import workloads
+    from pysit_gb300.autograd import resample_linear
+    from pysit_gb300.engine import WavePlan
+    idx = sorted(set(np.linspace(0, nshots - 1, min(nshots_check, nshots)).round().astype(int).tolist()))
+    out = {}
+    for prec in ("double", "single"):
+        m, shots, solver, C, C0 = workloads.cfg2(scale=scale, nshots=nshots, nsteps=nsteps, precision=prec)
+        solver.model_parameters = solver.ModelParameters(m, {"C": C0})
+        plan = WavePlan(solver, [shots[i] for i in idx], checkpoint_every=solver.checkpoint_every)
+        plan.dobs.copy_(resample_linear(obs_host[idx].cuda(), ts_obs, solver.ts()).to(plan.tdtype))
+        g, rn = plan.gradient()
+        plan.check_status()
+        out[prec] = (g.cpu().numpy().copy(), float(rn.item()))
+        del plan
+        torch.cuda.empty_cache()
+    g64, r64 = out["double"]
+    g32, r32 = out["single"]
+    return {"grad_rel_err_vs_fp64": float(np.linalg.norm(g32 - g64) / np.linalg.norm(g64)),
+            "misfit_rel_err_vs_fp64": abs(r32 - r64) / abs(r64),
+            "accuracy_check": {"shots": idx, "nsteps": nsteps, "schedule": "checkpoint", "tolerance": 1e-3,
+                               "reference": "FP64 batched gradient of the same shots and observed data"}}
 
 
 def plain_fp64_baseline(scale=1.0, nsteps_full=4000, nsample=1024, order=8):
@@ -144,22 +244,6 @@ def plain_fp64_baseline(scale=1.0, nsteps_full=4000, nsample=1024, order=8):
     per_shot = t / ns * nsteps_full
     return {"value": 1.0 / per_shot, "unit": "shots/s", "dtype": "f64",
             "sample": f"1 shot x {ns} steps of the same grid, extrapolated to {nsteps_full} steps; wall {t:.2f}s"}
-
-
-def cpu_baseline(nsample=40, procs=None, scale=1.0, nsteps_full=4000, order=8):
-    """Shots/s of the CPU port: `procs` processes, each one shot-gradient of `nsample`
-    steps (forward with the per-step dWaveOp list, adjoint with imaging, FP64),
-    extrapolated to `nsteps_full` steps."""
-    procs = procs or max(1, min(os.cpu_count() or 1, 64))
-    ctx = mp.get_context("spawn")
-    t0 = time.perf_counter()
-    with ctx.Pool(procs) as pool:
-        times = pool.map(_cpu_worker, [(scale, nsample, order)] * procs)
-    wall = time.perf_counter() - t0
-    per_shot = max(times) * nsteps_full / nsample
-    return dict(value=procs / per_shot, unit="shots/s", cores=procs, kind="port",
-                sample=f"{procs} shots x {nsample} of {nsteps_full} steps (forward+dWaveOp+adjoint+imaging, FP64, "
-                       f"oracle/cda_oracle.c one process per shot), extrapolated; wall {wall:.1f}s")
 
 
 # ---------------------------------------------------------------------------
@@ -215,11 +299,12 @@ def main():
     ap.add_argument("--schedule", default="checkpoint", choices=["checkpoint", "store", "auto"],
                     help="gradient schedule: recompute from checkpoints, or keep dWaveOp in HBM")
     ap.add_argument("--lanes", type=int, default=None, help="concurrent shot lanes (default: the schedule's choice)")
-    ap.add_argument("--cpu-sample", type=int, default=40)
+    ap.add_argument("--cpu-sample", type=int, default=400, help="record steps of the CPU sample (10 %% of 4000)")
     ap.add_argument("--cpu-procs", type=int, default=None, help="processes of the CPU port (default: all cores)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain per-shot FP64 GPU path")
     ap.add_argument("--no-kept", action="store_true", help="skip timing the kept-dWaveOp schedule")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the FP32-vs-FP64 gradient check")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -235,17 +320,26 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        vals = []
-        for i in range(args.warmup + args.steps):
-            cb = cpu_baseline(nsample=args.cpu_sample, procs=args.cpu_procs, scale=args.scale, nsteps_full=args.nsteps)
-            if i >= args.warmup:
-                vals.append(cb["value"])
+        cb = CpuBaseline(nsample=args.cpu_sample, procs=args.cpu_procs, scale=args.scale, nsteps_full=args.nsteps)
+        vals, walls = [], []
+        try:
+            for i in range(args.warmup + args.steps):
+                if i < args.warmup:  # warm-up (untimed): a short sample starts the processes and their problems
+                    cb.sample(min(args.cpu_sample, 40))
+                    continue
+                v, wall = cb.sample()
+                vals.append(v)
+                walls.append(wall)
+        finally:
+            cb.close()
         v = float(np.median(vals))
+        # a step is one bounded sample (every process one shot-gradient of cpu_sample steps): its
+        # wall time is ms_per_step; value extrapolates the sample to the full record
         line = {"metric": METRIC, "value": v, "unit": "shots/s", "n_gpus": 0, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": 1e3 * args.shots / v, "higher_is_better": True,
+                "warmup": args.warmup, "ms_per_step": 1e3 * float(np.median(walls)), "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
                 "config": config, "impl": "reference",
-                "cpu_baseline": dict(cb, value=v),
+                "cpu_baseline": cb.describe(v, float(np.median(walls))),
                 "e2e": {"value": v, "unit": "shots/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
@@ -408,6 +502,8 @@ def main():
         plain = plain_fp64_baseline(scale=args.scale, nsteps_full=args.nsteps)
         plain["batched_over_plain"] = line["value"] / world / plain["value"]
         line["plain_fp64"] = plain
+    if rank == 0 and not args.no_accuracy:  # outside the timed regions
+        line.update(accuracy_vs_fp64(obs_host, ts_obs, args.scale, args.shots, args.nsteps))
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(nsample=args.cpu_sample, procs=args.cpu_procs, scale=args.scale,
                                             nsteps_full=args.nsteps)

@@ -31,6 +31,8 @@ extern "C" {
 #define PYSIT_ENONFINITE -3  /* NaN/Inf found in a wavefield (unstable CFL) */
 #define PYSIT_ESTATE     -4  /* call out of order (e.g. no workspace bound) */
 #define PYSIT_EHOST      -5  /* host-side failure inside the library (a host allocation) */
+#define PYSIT_ETIMEOUT   -6  /* a bounded device wait expired: the results of the run are invalid
+                                (reported by the host layer from bit 0 of pysit_plan_status) */
 
 #define PYSIT_F32 0
 #define PYSIT_F64 1
@@ -39,7 +41,7 @@ extern "C" {
 const char* pysit_cuda_last_error(void);
 /* ABI version of this header (major*1000 + minor); pysit_cuda_version() returns the
  * library's, so a client can check that the two match. */
-#define PYSIT_ABI_VERSION 1000
+#define PYSIT_ABI_VERSION 1001
 int pysit_cuda_version(void);
 
 /* ------------------------------------------------------------------------
@@ -171,6 +173,18 @@ typedef struct {
                                       launch sequences run side by side on their own streams (each lane
                                       with its own buffers: lanes x the workspace of its shots); 0 or 1 =
                                       one sequence.  Results are the lanes' sums, in lane order */
+    uint32_t wait_polls;           /* 0 = a step kernel's wait for a bulk copy into shared memory makes
+                                      up to 2^22 blocking tries (far beyond any copy's latency); n > 0 =
+                                      at most n non-blocking tests before the wait counts as expired.
+                                      An expired wait sets bit 0 of the status word; the warp waits
+                                      (with the full limit) for the copies it has in flight and runs
+                                      no further task, so the run's results are invalid */
+    int wait_fault;                /* test aid, 0 in normal use.  1 = every task of the 2D step kernels
+                                      first waits (bounded: wait_polls non-blocking tests, 64 when
+                                      wait_polls is 0) on an mbarrier on which nothing ever arrives;
+                                      the wait runs out and takes the expiry path above with the
+                                      task's bulk copies in flight.  Lets a test check that path and
+                                      the status report without any GPU fault */
 } pysit_plan_desc;
 
 int pysit_plan_create(const pysit_plan_desc* desc, pysit_plan** out);
@@ -232,11 +246,18 @@ int pysit_plan_status(pysit_plan* plan, int* flags, void* stream);
  * for callers that cannot allocate device memory (applications that reserve all
  * device memory in their own pool up front, C/Fortran codes that link no
  * allocator).  Inputs dobs, dsim and output resid (may be NULL) are
- * [nshots][per_shot] arrays of `dtype`; rnorm2 (FP64, dev) receives
- * sum_i (dobs - dsim)^2 per shot.  No allocation: the reduction scratch is a
- * fixed 128 KiB device array (nshots <= 256, larger counts are rejected).  The
- * first call on a device looks its address up (make it before any stream
- * capture).  All calls share that array: calls that overlap on the GPU race.
+ * [nshots][per_shot] arrays of `dtype`; resid may be the same array as dobs or
+ * dsim (an in-place residual).  rnorm2 (FP64, dev) receives
+ * sum_i (dobs - dsim)^2 per shot over every one of the per_shot samples: unlike
+ * the plan's misfit, which stops each shot at its own record length, nothing here
+ * knows record lengths, so a caller with uneven records zeroes the samples past
+ * each shot's end in both arrays first.  No allocation: the reduction scratch is a
+ * fixed 128 KiB device array (nshots <= 256, larger counts are rejected).  Its
+ * address differs per CUDA context; the first call made in each context looks it
+ * up (make that call before any stream capture), later calls in the same context
+ * reuse it, and a new context (another one the host made current, or the one
+ * rebuilt after cudaDeviceReset) gets its own lookup.  All calls share the array:
+ * calls that overlap on the GPU race.
  * ------------------------------------------------------------------------ */
 int pysit_misfit_per_shot_noalloc(int dtype, const void* dobs, const void* dsim, int nshots,
                                   int64_t per_shot, void* resid, double* rnorm2, void* stream);

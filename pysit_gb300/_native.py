@@ -18,6 +18,7 @@ PYSIT_ECUDA = -2
 PYSIT_ENONFINITE = -3
 PYSIT_ESTATE = -4
 PYSIT_EHOST = -5
+PYSIT_ETIMEOUT = -6
 PYSIT_F32 = 0
 PYSIT_F64 = 1
 
@@ -60,6 +61,8 @@ class PlanDesc(C.Structure):
         ("forward_only", _i),
         ("shell_share", _d * 3),
         ("lanes", _i),
+        ("wait_polls", C.c_uint32),
+        ("wait_fault", _i),
     ]
 
 

@@ -153,6 +153,7 @@ class FWIMisfit:
         else:
             rn = plan.misfit()
             grad_m = None
+        plan.check_status()
         J = (0.5 * dt) * rn.reshape(())
         return J.to(C.dtype if C.dtype.is_floating_point else torch.float64), grad_m
 

@@ -5,9 +5,6 @@ parallel with nvcc (``-gencode arch=compute_103a,code=sm_103a``) and links the
 shared library in-tree (``pysit_gb300/libpysit_gb300.so``).  Object files go
 to ``pysit_gb300/_build/``.  Nothing is installed into site-packages.
 
-``PYSIT_CUDA_DEFINES`` (space-separated ``NAME=VALUE``) passes tuning macros of the
-kernels (e.g. ``PGB_SHELL_MINB=5``) as ``-D`` flags; a change of them rebuilds every
-object.
 """
 from __future__ import annotations
 
@@ -33,7 +30,9 @@ def _nvcc() -> str:
 
 
 def _defines() -> list[str]:
-    return ["-D" + d for d in os.environ.get("PYSIT_CUDA_DEFINES", "").split() if d]
+    """Extra -D flags of every translation unit (none: the kernels' macros keep their defaults).
+    The object directory records them, so a change rebuilds every object."""
+    return []
 
 
 def _flags(verbose_ptxas: bool = False) -> list[str]:

@@ -9,12 +9,17 @@
 // outputs: its only scratch is a fixed array in device memory that the library
 // holds on every GPU that loads it, until the process exits.
 //
-// Scratch: kMaxShots * kBlocksPerShot doubles (256 * 64 * 8 B = 128 KiB).  The
-// device address of the array is looked up once per device, on the first call
-// made with that device current; make that first call before any stream
-// capture.  Every call overwrites every partial sum it reads, so nothing has to
-// start at zero; but all calls share the one array, so calls that overlap on
-// the GPU (different streams, or host threads) race and give wrong results.
+// Scratch: kMaxShots * kBlocksPerShot doubles (256 * 64 * 8 B = 128 KiB).  A
+// __device__ array has one address per CUDA context, so the address is looked up
+// (cudaGetSymbolAddress) on the first call made in each context and kept with
+// that context's unique ID: a host that switches between contexts of its own, or
+// a context rebuilt after cudaDeviceReset, gets the address that belongs to it.
+// Make the first call of each context before any stream capture.  Every call
+// overwrites every partial sum it reads, so nothing has to start at zero; but all
+// calls share the one array, so calls that overlap on the GPU (different streams,
+// or host threads) race and give wrong results.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "common.cuh"
@@ -28,14 +33,11 @@ constexpr int kThreadsNA = 256;
 
 static __device__ __align__(256) double g_noalloc_partials[kMaxShots * kBlocksPerShot];
 
-std::mutex g_addr_mu;
-double* g_addr[64] = {nullptr};
-
 // stage 1: block b of shot s sums (dobs - dsim)^2 over its slice in FP64 and
-// writes one partial; optional residual written back
+// writes one partial; optional residual written back.  resid may be dobs or dsim
+// (an in-place call): each element is read before it is written, by one thread.
 template <typename T>
-__global__ void __launch_bounds__(kThreadsNA) na_partials(const T* __restrict__ dobs, const T* __restrict__ dsim,
-                                                          long long per_shot, T* __restrict__ resid,
+__global__ void __launch_bounds__(kThreadsNA) na_partials(const T* dobs, const T* dsim, long long per_shot, T* resid,
                                                           double* __restrict__ partials) {
     const int s = blockIdx.y, b = blockIdx.x;
     const T* o = dobs + (long long)s * per_shot;
@@ -68,18 +70,77 @@ __global__ void na_finish(const double* __restrict__ partials, int nshots, doubl
     if (lane == 0) out[s] = a;
 }
 
-int scratch_address(double** out) {
-    int dev = 0;
-    PGB_CHECK_CUDA(cudaGetDevice(&dev));
-    PGB_REQUIRE(dev >= 0 && dev < 64, "device ordinal %d out of range", dev);
-    std::lock_guard<std::mutex> lock(g_addr_mu);
-    if (!g_addr[dev]) {
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_partials);
-        if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress(g_noalloc_partials)");
-        g_addr[dev] = static_cast<double*>(p);
+// ---- the scratch address of the current context -------------------------------------
+// Two driver entry points, fetched through the runtime (no link against the driver
+// library): the calling thread's current context and its process-unique ID.
+using GetCurrentFn = CUresult (*)(CUcontext*);
+using GetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+
+struct CtxAddr {
+    unsigned long long id;
+    double* ptr;
+};
+constexpr int kCtxSlots = 64;  // contexts remembered at once (the oldest entry is replaced)
+
+std::mutex g_mu;
+GetCurrentFn g_get_current = nullptr;
+GetIdFn g_get_id = nullptr;
+bool g_fns_tried = false;
+CtxAddr g_cache[kCtxSlots];
+int g_cached = 0, g_next = 0;
+
+int driver_fns() {  // under g_mu
+    if (!g_fns_tried) {
+        g_fns_tried = true;
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_get_current = reinterpret_cast<GetCurrentFn>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_get_id = reinterpret_cast<GetIdFn>(f);
+        cudaGetLastError();  // a failed query leaves no sticky runtime error behind
     }
-    *out = g_addr[dev];
+    PGB_REQUIRE(g_get_current && g_get_id, "the CUDA driver offers no cuCtxGetCurrent / cuCtxGetId (CUDA >= 12 needed)");
+    return PYSIT_OK;
+}
+
+// ID of the calling thread's current context; the runtime makes the device's primary
+// context current first if no context is current yet
+int current_context(unsigned long long* id) {  // under g_mu
+    CUcontext ctx = nullptr;
+    PGB_REQUIRE(g_get_current(&ctx) == CUDA_SUCCESS, "cuCtxGetCurrent failed");
+    if (!ctx) {
+        int dev = 0;
+        PGB_CHECK_CUDA(cudaGetDevice(&dev));
+        PGB_CHECK_CUDA(cudaSetDevice(dev));  // initialises and binds the primary context
+        PGB_REQUIRE(g_get_current(&ctx) == CUDA_SUCCESS && ctx, "no CUDA context is current");
+    }
+    PGB_REQUIRE(g_get_id(ctx, id) == CUDA_SUCCESS, "cuCtxGetId failed");
+    return PYSIT_OK;
+}
+
+int scratch_address(double** out) {
+    std::lock_guard<std::mutex> lock(g_mu);
+    int rc = driver_fns();
+    if (rc) return rc;
+    unsigned long long id = 0;
+    if ((rc = current_context(&id))) return rc;
+    for (int i = 0; i < g_cached; ++i)
+        if (g_cache[i].id == id) {
+            *out = g_cache[i].ptr;
+            return PYSIT_OK;
+        }
+    // first call in this context: look the symbol up (not inside a stream capture)
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_partials);
+    if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress(g_noalloc_partials)");
+    const int slot = g_cached < kCtxSlots ? g_cached++ : g_next;
+    if (g_cached == kCtxSlots && slot == g_next) g_next = (g_next + 1) % kCtxSlots;
+    g_cache[slot] = CtxAddr{id, static_cast<double*>(p)};
+    *out = static_cast<double*>(p);
     return PYSIT_OK;
 }
 

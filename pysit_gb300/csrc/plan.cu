@@ -322,6 +322,8 @@ struct PlanT final : public pysit_plan {
     int fwd_only = 0;            // forward modelling only: no adjoint, imaging or checkpoint buffers
     int nslots = 1;              // replay slots: S (checkpointed) or ceil(nsteps / p_img) (kept)
     int tile_req = 0;            // requested task length along x (0: default)
+    unsigned wait_polls = 0;     // tries of a step kernel's bulk-copy wait (0: the kernels' default)
+    int wait_fault = 0;          // test aid: the 2D step kernels' waits run out (pysit_plan_desc.wait_fault)
     std::vector<int> shot_steps; // record length of each shot in steps (empty: all nsteps)
     size_t task_cap = 0;         // ints the task buffer holds (enough for the shortest x-chunk)
     double dx, dy, dz, dt;
@@ -333,7 +335,6 @@ struct PlanT final : public pysit_plan {
     long long fstride;  // elements per field per shot (256-byte multiple)
     int bz, tx, ntz, ntx;
     int nseg;
-    bool warp2d = true;          // 2D: warp-task sweep (true) or bulk-copy row pipeline (false)
     std::vector<int> tasks2d;    // [ntasks][5] warp tasks of the 2D sweep: interior first, then shell
     int ntask2d[2] = {0, 0};     // tasks of each kind
     std::vector<int> tasks3d;    // [ntasks][6] block tasks of the 3D sweep: interior first, then shell
@@ -418,6 +419,8 @@ struct PlanT final : public pysit_plan {
         store_all = d.store_dwaveop ? 1 : 0;
         fwd_only = d.forward_only ? 1 : 0;
         tile_req = d.tile_x > 0 ? d.tile_x : 0;
+        wait_polls = d.wait_polls;
+        wait_fault = d.wait_fault ? 1 : 0;
         for (int m = 0; m < 3; ++m)
             shell_frac[m] = d.shell_share[m] > 0 && d.shell_share[m] < 1 ? d.shell_share[m] : 0.0;
         shot_steps.clear();
@@ -488,48 +491,28 @@ struct PlanT final : public pysit_plan {
 
     void choose_tiling() {
         constexpr int V = V16<T>::N;
-        const char* e = getenv("PYSIT_CUDA_TILE");  // "bz,tx" override (tuning)
-        int ebz = 0, etx = 0;
-        bool have = e && sscanf(e, "%d,%d", &ebz, &etx) == 2 && ebz >= 32 && ebz <= 256 && ebz % 32 == 0 &&
-                    etx >= 1;
         if (dim == 2) {
-            const char* f = getenv("PYSIT_CUDA_SHELL_FRAC");  // tuning: block share of the shell kernel
-            if (f) shell_frac[0] = shell_frac[1] = shell_frac[2] = std::min(0.95, std::max(0.0, atof(f)));
-            const char* k = getenv("PYSIT_CUDA_2D");  // "tma" selects the bulk-copy pipeline
-            warp2d = !(k && strcmp(k, "tma") == 0);
-            if (warp2d) {
-                bz = wave2d_warp_threads();
-                tx = have ? etx : tile_req ? tile_req : 32;
-                build_tasks2d();
-                ntz = ntx = 1;
-                return;
-            }
-            // bulk-copy pipelined sweep: fixed 128-thread blocks, tx rows per block
-            bz = wave2d_threads();
-            tx = have ? etx : 64;
-            ntz = (nz + wave2d_tile_z((int)sizeof(T)) - 1) / wave2d_tile_z((int)sizeof(T));
-            ntx = (nx + tx - 1) / tx;
+            bz = wave2d_warp_threads();
+            tx = tile_req ? tile_req : 32;
+            build_tasks2d();
+            ntz = ntx = 1;
             return;
         }
         if (dim == 3) {
             bz = 128;  // threads of the recorder blocks
-            tx = have ? etx : tile_req ? tile_req : 64;
+            tx = tile_req ? tile_req : 64;
             build_tasks3d();
             ntz = ntx = 1;
             return;
         }
-        if (have) {
-            bz = ebz; tx = etx;
-        } else {
-            // fewest loaded elements (tile + halo) per useful cell, bz >= 64
-            double best = 1e30;
-            for (int b : {64, 128, 256}) {
-                int tiles = (nz + b * V - 1) / (b * V);
-                double cost = (double)tiles * (b * V + 2 * kHalo) / nz;
-                if (cost < best - 1e-9) { best = cost; bz = b; }
-            }
-            tx = 32;
+        // 1D: fewest loaded elements (tile + halo) per useful cell, bz >= 64
+        double best = 1e30;
+        for (int b : {64, 128, 256}) {
+            int tiles = (nz + b * V - 1) / (b * V);
+            double cost = (double)tiles * (b * V + 2 * kHalo) / nz;
+            if (cost < best - 1e-9) { best = cost; bz = b; }
         }
+        tx = 32;
         ntz = (nz + bz * V - 1) / (bz * V);
         ntx = (nx + tx - 1) / tx;
     }
@@ -620,7 +603,7 @@ struct PlanT final : public pysit_plan {
     // ints of the task table for a task length tx_try (the current table is kept)
     static constexpr int kMinTileX = 8;
     size_t task_ints(int tx_try) {
-        if (!((dim == 2 && warp2d) || dim == 3)) return 0;
+        if (dim == 1) return 0;
         const int keep = tx;
         tx = tx_try;
         size_t n;
@@ -826,7 +809,6 @@ struct PlanT final : public pysit_plan {
         PGB_CHECK_CUDA(cudaStreamSynchronize(s));
         if (!cap) PGB_CHECK_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
         if (dim == 2) {
-            wave2d_prepare();
             wave2d_warp_prepare();
             for (int m = 0; m < 4; ++m)
                 for (int k = 0; k < 2; ++k) blocks2d[m][k] = wave2d_warp_blocks((int)sizeof(T), order, m, k);
@@ -880,6 +862,8 @@ struct PlanT final : public pysit_plan {
         p.idy = T(1.0 / dy); p.idy2 = T(1.0 / (T(dy) * T(dy)));
         p.idz = T(1.0 / dz); p.idz2 = T(1.0 / (T(dz) * T(dz)));
         p.err = ws ? at<int>(off.err) : nullptr;
+        p.polls = wait_polls;
+        p.wait_fault = wait_fault;
         p.psi_c2 = psi_consistent ? 0 : 1;
         p.task_ctr = ws ? at<unsigned long long>(off.ctr) : nullptr;
         (void)g0;
@@ -1022,18 +1006,14 @@ struct PlanT final : public pysit_plan {
     }
 
     void launch(const WaveParams<T>& p, int mode, cudaStream_t s) {
-        if (!(dim == 2 && warp2d) && dim != 3) ++launches;
+        if (dim == 1) ++launches;
 #define PGB_L(RR)                                                              \
     do {                                                                       \
-        if (dim == 2 && warp2d) {                                              \
+        if (dim == 2) {                                                        \
             if (mode == kFwd) launch2d<RR, kFwd>(p, s);                        \
             else if (mode == kRecomp) launch2d<RR, kRecomp>(p, s);             \
             else if (mode == kBorn) launch2d<RR, kBorn>(p, s);                 \
             else launch2d<RR, kAdj>(p, s);                                     \
-        } else if (dim == 2) {                                                 \
-            if (mode == kFwd) launch_wave2d<T, RR, kFwd>(p, bz, s);            \
-            else if (mode == kRecomp) launch_wave2d<T, RR, kRecomp>(p, bz, s); \
-            else launch_wave2d<T, RR, kAdj>(p, bz, s);                         \
         } else if (dim == 3) {                                                 \
             if (mode == kFwd) launch3d<RR, kFwd>(p, s);                        \
             else if (mode == kRecomp) launch3d<RR, kRecomp>(p, s);             \
@@ -1221,7 +1201,7 @@ struct PlanT final : public pysit_plan {
             set_inject(p1, true, g0, k, nullptr);  // valid tables, switched off: u1 has no source
             p1.inj.on = 0;
             set_recording(p1, g0, gn, tr + (long long)k * nrec);
-            if (dim == 2 && warp2d) {  // the Born source read inside the u1 step
+            if (dim == 2) {  // the Born source read inside the u1 step
                 p1.dw_in = dw;
                 p1.m1 = at<T>(off.m1);
                 launch(p1, kBorn, s);
@@ -1354,7 +1334,7 @@ struct PlanT final : public pysit_plan {
     int autotune(const int* cand, int ncand, int n, int* chosen, double* ms_out, cudaStream_t s) override {
         PGB_REQUIRE(ws, "no workspace bound");
         PGB_REQUIRE(model_set, "pysit_plan_set_model must be called first");
-        PGB_REQUIRE((dim == 2 && warp2d) || dim == 3, "autotuning applies to the 2D and 3D task sweeps");
+        PGB_REQUIRE(dim >= 2, "autotuning applies to the 2D and 3D task sweeps");
         PGB_REQUIRE(cand && ncand >= 1 && chosen, "need at least one candidate and an output");
         PGB_REQUIRE(n >= 1, "nsteps must be >= 1");
         for (int c = 0; c < ncand; ++c)

@@ -7,7 +7,7 @@
 // Zero-extended stencils (fd_manual.hpp:5-70), Dirichlet outer ring, right PML
 // profile read at r[n_r - ((n-1) - i)] (_2D.h:143-157), psi integrated on every
 // non-ring cell in 3D.  These kernels serve the per-step API (time_step) and the
-// plain per-shot path; the batched pipeline lives in wave2d.cu / wave3d.cu.
+// plain per-shot path; the batched pipeline lives in wave2d_warp.cu / wave3d.cu.
 //
 // One thread per cell, z (the contiguous axis) on threadIdx.x.  Taps outside
 // [0, n) are skipped, which is the zero extension of the reference.

@@ -140,6 +140,8 @@ struct WaveParams {
     const T* m1;             // kBorn: edge-padded model perturbation (internal layout, shared by the shots);
                              // dw_in holds dWaveOp0_k
     int* err;                // device error word (PGB_ERR_* bits), may be NULL
+    unsigned polls;          // 0: a bulk-copy wait tries 2^22 times (each try may suspend); n: n non-blocking tests
+    int wait_fault;          // test aid: each task first waits (bounded) on a barrier nothing arrives on
     int psi_c2;              // 3D: 1 = C^2 multiplies sigma_x sigma_y sigma_z psi (the reference), 0 = not
     int nan_check;           // kRecomp: flag non-finite u_{k+1} as kFwd does (a forward sweep that keeps dWaveOp)
     // 2D persistent sweep: task counters (interior, PML shell) shared by the
@@ -183,8 +185,6 @@ __device__ __forceinline__ void record_block(const WaveParams<T>& p, int rb) {
     p.rec.traces[shot * p.rec.tr_sstride + r] = acc;
 }
 
-template <typename T, int R, int MODE>
-void launch_wave2d(const WaveParams<T>& p, int bz, cudaStream_t s);
 // persistent-warp 2D sweep fed by shared-memory row rings, one task kind per
 // kernel (0 interior, 1 PML shell); tasks = [ntasks][5] ints (x0, x1, zs, ze,
 // kind) of one shot, shared by all shots; `blocks` task blocks.  Returns the
@@ -205,9 +205,5 @@ int wave3d_rows_per_block();
 int wave3d_seg(int dtype_bytes, int kind);  // widest z-range of a task of each kind
 template <typename T, int R, int MODE>
 void launch_wave1d(const WaveParams<T>& p, int bz, cudaStream_t s);
-// one-time kernel attributes (large dynamic shared memory); call outside graph capture
-void wave2d_prepare();
-int wave2d_threads();
-int wave2d_tile_z(int dtype_bytes);
 
 }  // namespace pgb

@@ -40,8 +40,12 @@
 // caller may instead switch the injection off here and add it after the step.
 // Each lane issues at most one of a row's bulk copies (per-lane copy descriptors),
 // and the arithmetic runs on cell pairs (packed f32x2 instructions in FP32).
-// Waits are bounded: on expiry the kernel sets the plan's error word, waits (again
-// bounded) for the copies it issued, and carries on.
+// Waits are bounded (2^22 blocking tries of the stage's mbarrier, or WaveParams::polls
+// non-blocking tests when the plan sets a limit; WaveParams::wait_fault adds a wait that
+// always runs out, for tests): on expiry the
+// warp waits, with the full limit, for every copy it still has in flight, sets the
+// plan's error word, and takes no further task of the launch (it still draws them from
+// the counter, so the counter stays in step with the later launches of the run).
 #include "tma.cuh"
 #include "wave.cuh"
 
@@ -49,7 +53,8 @@ namespace pgb {
 namespace {
 
 constexpr int kWarps = 4;  // warps per block
-constexpr uint32_t kPolls = 1u << 22;
+constexpr uint32_t kPolls = 1u << 22;  // tries of a drain wait (and the default of WaveParams::polls)
+constexpr int kSpareBar = 15;          // the last of a warp's 16 mbarrier slots: never armed (test aid)
 #ifndef PGB_RING_AHEAD
 #define PGB_RING_AHEAD 4   // rows whose copies are in flight ahead of the computation
 #endif
@@ -107,7 +112,7 @@ struct Ring {
     static constexpr int ELEMS = NU * WS * (PML ? 2 : 1) + A * PST;
     static constexpr size_t per_warp = 128 + sizeof(T) * (size_t)ELEMS;  // barriers + rings
     static constexpr size_t bytes = kWarps * per_warp;
-    static_assert(A >= 2 && A <= 16, "the barrier block holds 16 mbarriers");
+    static_assert(A >= 2 && A <= 15, "the barrier block holds 16 mbarriers, the last one spare");
     static_assert(V % 2 == 0 && HZ % V == 0, "lanes hold whole pairs; halo in whole vectors");
     static_assert(per_warp % 16 == 0, "warp regions stay 16-byte aligned");
     static_assert(RB == 1 || RB == 2, "one or two rows per iteration");
@@ -253,6 +258,24 @@ __device__ __forceinline__ void sweep(const WaveParams<T>& p, unsigned char* wsm
         }
     }
 
+    // an expired wait at iteration `it`: every stage armed for iterations it .. it+A-1 may
+    // still receive bytes; wait for those phases with the full limit before leaving the task
+    auto drain = [&](int it) {
+        const int armed = min(A, nit - it);
+        for (int j = 0; j < armed; ++j) {
+            const int sj = pp.s + j < A ? pp.s + j : pp.s + j - A;
+            mbar_wait_bounded(reinterpret_cast<uint64_t*>(wsm) + sj, pp.s + j < A ? pp.ph : (pp.ph ^ 1u), kPolls);
+        }
+    };
+    // test aid (WaveParams::wait_fault): a bounded wait on the warp's spare mbarrier, on which
+    // nothing ever arrives, runs out and takes the expiry path with this task's copies in flight
+    if (p.wait_fault && !__all_sync(0xffffffffu, mbar_test_bounded(reinterpret_cast<uint64_t*>(wsm) + kSpareBar, 0u,
+                                                                  p.polls ? p.polls : 64u))) {
+        late = true;
+        drain(0);
+        return;
+    }
+
     // per-lane constants
     bool zok[V];
     T sgz[V], mgz[V];
@@ -288,7 +311,13 @@ __device__ __forceinline__ void sweep(const WaveParams<T>& p, unsigned char* wsm
     for (int it = 0; it < nit; ++it, o += (long long)RB * p.ldz) {
         const int x = x0 + RB * it;
         const int s = pp.s;
-        if (!mbar_wait_bounded(reinterpret_cast<uint64_t*>(wsm) + s, pp.ph, kPolls)) late = true;
+        const bool ok = p.polls ? mbar_test_bounded(reinterpret_cast<uint64_t*>(wsm) + s, pp.ph, p.polls)
+                                : mbar_wait_bounded(reinterpret_cast<uint64_t*>(wsm) + s, pp.ph, kPolls);
+        if (!__all_sync(0xffffffffu, ok)) {
+            late = true;
+            drain(it);
+            return;
+        }
         const unsigned char* sb = lb + OFF_P + s * STG;  // this lane in stage s
 
         // ---- the shared-memory reads of this iteration ---------------------------------
@@ -488,6 +517,7 @@ __global__ void __launch_bounds__(kWarps * 32, (MinBlocks<T, KIND>::value))
     constexpr int A = G::A;
     if (lane == 0) {
         for (int s = 0; s < A; ++s) mbar_init(&bar[s], 1);
+        if (p.wait_fault) mbar_init(&bar[kSpareBar], 1);  // one arrival expected, none ever made
         fence_mbar_init();
     }
     __syncwarp();
@@ -501,17 +531,10 @@ __global__ void __launch_bounds__(kWarps * 32, (MinBlocks<T, KIND>::value))
         if (lane == 0) t = atomicAdd(ctr, 1ull) - base;
         t = __shfl_sync(0xffffffffu, t, 0);
         if (t >= total) break;
+        if (late) continue;  // an expired wait: the remaining tasks are drawn, not run
         const int shot = (int)(t / (unsigned)ntasks);
         const int* tk = tasks + 5 * (int)(t - (unsigned long long)shot * ntasks);
         sweep<T, R, MODE, KIND>(p, wsm, pp, shot, __ldg(tk), __ldg(tk + 1), __ldg(tk + 2), __ldg(tk + 3), bad, late);
-    }
-    late = __any_sync(0xffffffffu, late);
-    if (late) {
-        // a stage whose wait expired may still have copies in flight: wait for the
-        // last phase of every stage (bounded) before the shared memory is released.
-        // pp.s is the next stage to use; stage j's last armed phase has parity
-        // pp.ph for j < pp.s and pp.ph ^ 1 otherwise
-        for (int j = 0; j < A; ++j) mbar_wait_bounded(&bar[j], j < pp.s ? pp.ph : (pp.ph ^ 1u), kPolls);
     }
     if (p.err) {
         if (MODE != kAdj && bad) atomicOr(p.err, PGB_ERR_NONFINITE);

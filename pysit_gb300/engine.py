@@ -113,7 +113,8 @@ class WavePlan:
     """Device plan of one (solver configuration, shot list)."""
 
     def __init__(self, solver, shots, imaging_period=1, checkpoint_every=None, shots_per_launch=None,
-                 use_graph=None, record_steps=None, gradient_schedule=None, forward_only=False, lanes=None):
+                 use_graph=None, record_steps=None, gradient_schedule=None, forward_only=False, lanes=None,
+                 wait_polls=0, wait_fault=False):
         """``record_steps``: optional record length of each shot in time steps (<= solver.nsteps);
         a shorter shot's residual is zero from its length on, so its misfit and gradient are those
         of a run of that length (the shots of one plan still step together).
@@ -125,7 +126,11 @@ class WavePlan:
         memory, taking as many shots per launch as fit unless shots_per_launch is fixed.
         ``forward_only`` plans model data only (no adjoint, imaging or checkpoint storage).
         ``lanes`` (default 1): the shots split into that many ranges whose launch sequences run
-        side by side on their own streams, shots_per_launch being per lane."""
+        side by side on their own streams, shots_per_launch being per lane.
+        ``wait_polls`` (default 0, the library's limit): tries of a step kernel's wait for a
+        bulk copy before it counts as expired (``check_status`` then raises).  ``wait_fault``
+        (test aid): the 2D step kernels' tasks first wait on a barrier nothing arrives on, so
+        that the wait runs out and the expiry path runs."""
         torch = _native.require_cuda()
         lib = _native.load()
         self.solver = solver
@@ -187,6 +192,8 @@ class WavePlan:
         d.nshots = self.nshots
         d.use_graph = 1 if use_graph else 0
         d.psi_consistent = 1 if getattr(solver, "pml_psi", "reference") == "consistent" else 0
+        d.wait_polls = int(wait_polls)
+        d.wait_fault = 1 if wait_fault else 0
         self._tune_key = (self.dim, solver.spatial_accuracy_order, tuple(full), str(solver.dtype),
                           d.psi_consistent)
         self.record_steps = None
@@ -456,6 +463,18 @@ class WavePlan:
         f = C.c_int()
         _native.check(_native.load().pysit_plan_status(self._h, C.byref(f), C.c_void_p(_native.stream_handle())))
         return int(f.value)
+
+    def check_status(self):
+        """Read and clear the status flags of the runs since the last read.  An expired
+        bulk-copy wait (flag 1) makes those runs' results invalid: PysitCudaError with
+        PYSIT_ETIMEOUT.  A non-finite wavefield (flag 2: the time step is unstable) is left to
+        the caller, as the reference leaves it: the flags are returned."""
+        f = self.status()
+        if f & 1:
+            raise _native.PysitCudaError(
+                _native.PYSIT_ETIMEOUT, "a step kernel's wait for a bulk copy expired: the results of the "
+                "plan's last runs are invalid")
+        return f
 
     def misfit(self, with_traces=False):
         self.set_model()

@@ -134,6 +134,7 @@ def generate_seismic_data(shots, solver, model, verbose=False, frequencies=None,
         ts = solver.ts()
         plan = plan_for(solver, shots, forward_only=True)
         traces = plan.forward().double().cpu().numpy()
+        plan.check_status()
         for i, shot in enumerate(shots):
             shot.reset_time_series(ts)
             shot.dt = solver.dt

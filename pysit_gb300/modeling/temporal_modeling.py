@@ -94,6 +94,7 @@ class TemporalModeling:
                 tr = plan.forward()
                 retval["simdata"] = tr[0, :, :shot.receivers.receiver_count].to(dtype=__import__("torch").float64) \
                     .cpu().numpy()
+                plan.check_status()
             return retval
         return self._forward_plain(shot, imaging_period, rp)
 
@@ -145,6 +146,7 @@ class TemporalModeling:
                 tr = plan.born(m1)
                 retval["simdata"] = tr[0, :, :shot.receivers.receiver_count].to(
                     dtype=__import__("torch").float64).cpu().numpy()
+                plan.check_status()
             return retval
         return self._linear_plain(shot, m1, rp, dWaveOp0)
 
@@ -217,7 +219,9 @@ class TemporalModeling:
             op = np.zeros((1, solver.nsteps, plan.nrec))
             op[0, :, :shot.receivers.receiver_count] = np.asarray(operand_simdata)
             img = plan.migrate(torch.as_tensor(op, dtype=plan.tdtype, device="cuda"))
-            return m0.perturbation(data=img.cpu().numpy().reshape(-1, 1))
+            out = m0.perturbation(data=img.cpu().numpy().reshape(-1, 1))
+            plan.check_status()
+            return out
         if dWaveOp is None:
             dWaveOp = self._forward_plain(shot, imaging_period, {"dWaveOp"}, device_outputs=True)["dWaveOp"]
         rp = ["imaging_condition"]

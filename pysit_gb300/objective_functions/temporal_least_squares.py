@@ -110,6 +110,7 @@ class TemporalLeastSquares(ObjectiveFunctionBase):
         if self.batched:
             plan = self._plan(shots, m0)
             r_norm2 = float(plan.misfit().item())
+            plan.check_status()
         else:
             r_norm2 = 0.0
             for shot in shots:
@@ -122,6 +123,7 @@ class TemporalLeastSquares(ObjectiveFunctionBase):
         if self.batched and not want_phd:
             plan = self._plan(shots, m0)
             g, rn = plan.gradient()
+            plan.check_status()
             grad = m0.perturbation(data=g.cpu().numpy().reshape(-1, 1))
             r_norm2 = float(rn.item())
             pseudo_h_diag = None
@@ -166,6 +168,7 @@ class TemporalLeastSquares(ObjectiveFunctionBase):
             plan = plan_for(self.solver, list(shots), 1, **self.plan_kwargs)
             self._last_plan = weakref.ref(plan)
             h, _ = plan.hessian(m1)
+            plan.check_status()
             result = m0.perturbation(data=h.cpu().numpy().reshape(-1, 1))
         else:
             result = m0.perturbation()

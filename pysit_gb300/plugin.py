@@ -138,13 +138,18 @@ def _patch_objective(pysit):
 
     def evaluate(self, shots, m0, **kw):
         if type(self.solver).__name__.endswith("_cuda") and not self.parallel_wrap_shot.use_parallel:
-            return 0.5 * float(_plan(self, shots, m0).misfit().item()) * self.solver.dt
+            plan = _plan(self, shots, m0)
+            rn = float(plan.misfit().item())
+            plan.check_status()
+            return 0.5 * rn * self.solver.dt
         return orig_eval(self, shots, m0, **kw)
 
     def compute_gradient(self, shots, m0, aux_info={}, **kw):
         phd = ("pseudo_hess_diag" in aux_info) and aux_info["pseudo_hess_diag"][0]
         if type(self.solver).__name__.endswith("_cuda") and not phd and not self.parallel_wrap_shot.use_parallel:
-            g, rn = _plan(self, shots, m0).gradient()
+            plan = _plan(self, shots, m0)
+            g, rn = plan.gradient()
+            plan.check_status()
             grad = m0.perturbation(data=g.cpu().numpy().reshape(-1, 1))
             r_norm2 = float(rn.item()) * self.solver.dt
             if ("residual_norm" in aux_info) and aux_info["residual_norm"][0]:

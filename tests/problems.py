@@ -36,6 +36,16 @@ SPECS = {
                   f=35.0, model="random", nsrc=(1, 1), nrec=(3, 3), sdepth=50.0, rdepth=30.0),
 }
 
+# Deep grids (GPU tests against the oracle, no fixtures): the padded z extent (433 cells in 2D,
+# 171 in 3D) splits the interior into several z-segments of the step kernels' task tables in
+# both precisions, with the sources at mid depth so that the fields cross the segment boundaries.
+DEEP_SPECS = {
+    "deep": dict(dim=2, n=(41, 401), L=(400.0, 4000.0), pml=(16, 200.0), order=8, T=0.4, cfl=0.4,
+                 f=25.0, model="layered", nsrc=2, nrec=20, sdepth=2000.0, rdepth=1800.0),
+    "deep3d": dict(dim=3, n=(15, 13, 161), L=(140.0, 120.0, 1600.0), pml=(5, 5.0), order=8, T=0.14, cfl=0.25,
+                   f=30.0, model="layered", nsrc=(1, 1), nrec=(3, 3), sdepth=800.0, rdepth=700.0),
+}
+
 
 def _models(mesh, spec):
     coords = mesh.mesh_coords()
@@ -59,7 +69,7 @@ def _models(mesh, spec):
 def build(api, name, kernel="cuda", precision="double", spec_overrides=None, **solver_kw):
     """(mesh, shots, solver, C_true, C_start) of problem `name`; spec_overrides replaces
     entries of its spec (e.g. the PML), solver_kw go to the solver."""
-    spec = dict(SPECS[name], **(spec_overrides or {}))
+    spec = dict({**SPECS, **DEEP_SPECS}[name], **(spec_overrides or {}))
     cells, amp = spec["pml"]
     dim = spec["dim"]
     deltas = [L / (n - 1) for L, n in zip(spec["L"], spec["n"])]

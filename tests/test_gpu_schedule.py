@@ -149,20 +149,6 @@ def test_observed_data_resampled_on_the_device_match_the_host():
     np.testing.assert_allclose(dev2[1, :, :nrec], 2 * host[1], rtol=0, atol=1e-13 * np.abs(host).max())
 
 
-@pytest.mark.parametrize("precision,tol", [("double", 1e-12), ("single", 1e-4)])
-@pytest.mark.parametrize("schedule", ["checkpoint", "store"])
-def test_bulk_copy_2d_variant_agrees(monkeypatch, precision, tol, schedule):
-    """The bulk-copy pipelined 2D sweep (PYSIT_CUDA_2D=tma, kernels of wave2d.cu) against the
-    default warp-task sweep: same traces and gradient up to rounding."""
-    m, shots, solver, C, C0 = _setup("o8", precision)
-    a = _grad(solver, shots, schedule, checkpoint_every=6)
-    monkeypatch.setenv("PYSIT_CUDA_2D", "tma")
-    b = _grad(solver, shots, schedule, checkpoint_every=6)
-    assert np.linalg.norm(b[0] - a[0]) <= tol * np.linalg.norm(a[0])
-    assert np.linalg.norm(b[2] - a[2]) <= tol * np.linalg.norm(a[2])
-    assert b[3] == 0
-
-
 def test_fp32_gradient_of_the_2d_workload_within_1e3_of_fp64():
     """The bench's claim at a size the FP64 path finishes in seconds: the 2D workload at a
     quarter of its size (288 x 96 cells + 10-cell PML, 16 shots, 1000 steps, order 8), FP32
