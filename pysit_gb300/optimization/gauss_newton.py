@@ -1,15 +1,15 @@
-"""Gauss-Newton with a Krylov inner solve (mirror of pysit.optimization.GaussNewton,
-pysit/optimization/gauss_newton.py:15-85).
+"""Gauss-Newton with PySIT's interface (pysit/optimization/gauss_newton.py:15-85).
 
-Each iteration solves H d = -g with GMRES (``krylov.gmres``, pyamg's convention, one
-cycle of up to ``krylov_maxiter`` iterations) where H v is
-``objective.apply_hessian(shots, m0, v, **objective_arguments)`` - on the GPU the batched
-Gauss-Newton Hessian of all shots in one plan call per Krylov iteration - then takes a
-line-search step along d with alpha0 = 1.
+The direction d solves the Gauss-Newton system H d = -g approximately with GMRES
+(``krylov.gmres``: one cycle of at most ``krylov_maxiter`` iterations), where H v is
+``objective.apply_hessian(shots, m0, v)`` - on the GPU the batched Hessian of all shots,
+one plan call per Krylov iteration.  The line search starts from the full Newton step
+(length 1).  ``krylov_residuals`` holds |H d - (-g)| per Krylov iteration of the last
+iteration.
 
-Deviation: the reference's matvec builds ``m0.perturbation(data=x)`` but passes the raw
-array to apply_hessian (:57-60), whose Born modelling then calls ``with_padding`` on it;
-here the perturbation is passed.
+Difference from the reference: its Hessian product passes the raw Krylov vector to
+apply_hessian, whose Born modelling needs a model perturbation (:57-60); here the vector
+is wrapped as one.
 """
 from __future__ import annotations
 
@@ -26,33 +26,23 @@ class GaussNewton(OptimizationBase):
     def __init__(self, objective, krylov_maxiter=50, *args, **kwargs):
         super().__init__(objective, *args, **kwargs)
         self.krylov_maxiter = krylov_maxiter
+        self.krylov_residuals = []
 
-    def _select_step(self, shots, current_objective_value, gradient, iteration, objective_arguments, **kwargs):
+    def search_direction(self, shots, gradient, iteration, objective_arguments):
         m0 = self.base_model
-        rhs = -1 * np.asarray(gradient.asarray(), dtype=float).reshape(-1)
 
-        def matvec(x):
-            m1 = m0.perturbation(data=np.asarray(x, dtype=float).reshape(-1, 1))
-            h = self.objective_function.apply_hessian(shots, self.base_model, m1, **objective_arguments)
+        def hessian_times(v):
+            h = self.objective_function.apply_hessian(shots, m0, m0.perturbation(data=np.reshape(v, (-1, 1))),
+                                                      **objective_arguments)
             return np.asarray(h.data, dtype=float).reshape(-1)
 
-        resid = []
-        d, info = gmres(matvec, rhs, maxiter=self.krylov_maxiter, residuals=resid)
-        self.krylov_residuals = list(resid)  # ||H d - (-g)|| per Krylov iteration, last outer iteration
-        direction = m0.perturbation(data=d.reshape(-1, 1))
-        if info < 0:
-            self._print("CG Failure")
-        if info == 0:
-            self._print("CG Converge")
-        if info > 0:
-            self._print("CG ran {0} iterations".format(info))
+        rhs = -np.asarray(gradient.asarray(), dtype=float).reshape(-1)
+        residuals = []
+        d, info = gmres(hessian_times, rhs, maxiter=self.krylov_maxiter, residuals=residuals)
+        self.krylov_residuals = residuals
+        outcome = "converged" if info == 0 else ("broke down" if info < 0 else f"stopped after {info} iterations")
+        self._log(f"  Krylov solve {outcome}, residual {residuals[-1] if residuals else None}")
+        return m0.perturbation(data=d.reshape(-1, 1))
 
-        alpha = self.select_alpha(shots, gradient, direction, objective_arguments,
-                                  current_objective_value=current_objective_value,
-                                  alpha0_kwargs={"reset": iteration == 0}, **kwargs)
-        self._print("  alpha {0}".format(alpha))
-        self.store_history("alpha", iteration, alpha)
-        return alpha * direction
-
-    def _compute_alpha0(self, phi0, grad0, reset=False, upscale_factor=None, **kwargs):
+    def trial_length(self, value, gradient, iteration):
         return 1.0

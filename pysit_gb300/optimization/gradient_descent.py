@@ -1,11 +1,10 @@
-"""Steepest descent with a line search (mirror of pysit.optimization.GradientDescent,
-pysit/optimization/gradient_descent.py:13-57): direction -g; the backtracking line
-search starts from f / (|g| * prod(deltas))**2 on the first iteration and from the
-previous step length / 0.7 afterwards."""
+"""Steepest descent with PySIT's interface (pysit/optimization/gradient_descent.py:13-57):
+the direction is -g; the line search starts from f / (|g| prod(deltas))^2 at iteration 0
+and from the previous accepted length / 0.7 afterwards (a little longer than the last
+step, so that the step can grow again)."""
 from __future__ import annotations
 
-import numpy as np
-
+from .line_search import Backtracking
 from .optimization import OptimizationBase
 
 __all__ = ["GradientDescent"]
@@ -13,20 +12,10 @@ __all__ = ["GradientDescent"]
 
 class GradientDescent(OptimizationBase):
 
-    def __init__(self, objective, *args, **kwargs):
-        super().__init__(objective, *args, **kwargs)
-        self.prev_alpha = None
+    def search_direction(self, shots, gradient, iteration, objective_arguments):
+        return -1 * gradient
 
-    def _select_step(self, shots, current_objective_value, gradient, iteration, objective_arguments, **kwargs):
-        direction = -1 * gradient
-        alpha = self.select_alpha(shots, gradient, direction, objective_arguments,
-                                  current_objective_value=current_objective_value,
-                                  alpha0_kwargs={"reset": iteration == 0}, **kwargs)
-        self._print("  alpha {0}".format(alpha))
-        self.store_history("alpha", iteration, alpha)
-        return alpha * direction
-
-    def _compute_alpha0(self, phi0, grad0, reset=False, upscale_factor=None, **kwargs):
-        if reset or self.prev_alpha is None:
-            return phi0 / (grad0.norm() * np.prod(self.solver.mesh.deltas)) ** 2
-        return self.prev_alpha / upscale_factor
+    def trial_length(self, value, gradient, iteration):
+        if iteration == 0 or self.prev_alpha is None:
+            return self._scaled_first_length(value, gradient)
+        return self.prev_alpha / Backtracking.trial_growth

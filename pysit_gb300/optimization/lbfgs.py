@@ -1,90 +1,84 @@
-"""Limited-memory BFGS (mirror of pysit.optimization.LBFGS, pysit/optimization/lbfgs.py:13-124).
+"""Limited-memory BFGS with PySIT's interface (pysit/optimization/lbfgs.py:13-124).
 
-The search direction is the two-loop recursion of Nocedal & Wright (Algorithm
-7.4) over the stored pairs (s, y, rho), with the initial scaling
-gamma = <s, y> / <y, y> of the newest pair (1 before any pair exists).  As in
-the reference, a pair is completed one iteration late, when the next gradient
-is known:
-  s_k = m_{k+1} - m_k  (the difference of the models actually used, after any
-        post-processing of ``base_model += step``, in the linear form m = C**-2),
-  y_k = g_{k+1} - g_k,  rho_k = 1 / <y_k, s_k>,
-with the model-space inner product (cell volume weighted).  The step length
-comes from the line search; the backtracking line search starts from
-alpha_0 = f / (|g| * prod(deltas))**2 on the first step after a memory reset,
-and from 1 afterwards.
+The direction is -H_k g_k with H_k the L-BFGS inverse-Hessian approximation applied by the
+two-loop recursion of Nocedal & Wright (Numerical Optimization, 2nd ed., Algorithm 7.4):
+over the m newest curvature pairs (s_i, y_i), rho_i = 1 / <y_i, s_i>, with the initial
+matrix gamma_k I, gamma_k = <s, y> / <y, y> of the newest pair (1 while there is none).
+A pair is known one iteration after its step:
+  s_k = m_{k+1} - m_k  (the models the iterations actually used, in PySIT's linear form
+        m = C**-2),
+  y_k = g_{k+1} - g_k,
+with the model-space inner product (cell-volume weighted).  The line search starts from
+f / (|g| prod(deltas))^2 on the first step after the memory is cleared (at every call of
+``inner_loop`` unless ``reset_on_new_inner_loop_call`` is False) and from 1 afterwards.
 """
 from __future__ import annotations
 
 import copy
 from collections import deque
-
-import numpy as np
+from dataclasses import dataclass
 
 from .optimization import OptimizationBase
 
-__all__ = ["LBFGS"]
+__all__ = ["LBFGS", "two_loop"]
+
+
+@dataclass
+class CurvaturePair:
+    s: object     # model difference (ModelPerturbation)
+    y: object     # gradient difference (ModelPerturbation)
+    rho: float    # 1 / <y, s>
+
+
+def two_loop(gradient, pairs, gamma):
+    """H g for the L-BFGS matrix of `pairs` (oldest first) with H0 = gamma I."""
+    q = copy.deepcopy(gradient)
+    coeffs = []
+    for p in reversed(pairs):            # newest to oldest
+        a = p.rho * p.s.inner_product(q)
+        q -= a * p.y
+        coeffs.append(a)
+    r = gamma * q
+    for p, a in zip(pairs, reversed(coeffs)):  # oldest to newest
+        b = p.rho * p.y.inner_product(r)
+        r += (a - b) * p.s
+    return r
 
 
 class LBFGS(OptimizationBase):
 
     def __init__(self, objective, memory_length=None, reset_on_new_inner_loop_call=True, *args, **kwargs):
         super().__init__(objective, *args, **kwargs)
-        self.prev_alpha = None
-        self.prev_model = None
-        self.memory_length = memory_length  # None: unbounded
+        self.memory_length = memory_length  # None: every pair is kept
         self.reset_on_new_inner_loop_call = reset_on_new_inner_loop_call
-        self._reset_memory()
+        self.clear_memory()
 
-    def _reset_memory(self):
-        # entries [rho, s, y]; the newest holds [None, None, -g_k] until g_{k+1} is known
-        self.memory = deque([], maxlen=self.memory_length)
-        self._reset_line_search = True
-        self.prev_model = None
+    def clear_memory(self):
+        self.memory = deque(maxlen=self.memory_length)  # CurvaturePair, oldest first
+        self._last = None     # (model, gradient) of the previous iteration: half of the next pair
+        self._fresh = True    # the next line search starts from the scaled first length
 
     def inner_loop(self, *args, **kwargs):
         if self.reset_on_new_inner_loop_call:
-            self._reset_memory()
+            self.clear_memory()
         super().inner_loop(*args, **kwargs)
 
-    def _select_step(self, shots, current_objective_value, gradient, iteration, objective_arguments, **kwargs):
-        mem = self.memory
-        q = copy.deepcopy(gradient)
-        x_k = copy.deepcopy(self.base_model)
-
+    def search_direction(self, shots, gradient, iteration, objective_arguments):
+        model = copy.deepcopy(self.base_model)
+        if self._last is not None:
+            m_prev, g_prev = self._last
+            s = model - m_prev
+            y = gradient - g_prev
+            self.memory.append(CurvaturePair(s=s, y=y, rho=1.0 / y.inner_product(s)))
         gamma = 1.0
-        if len(mem) > 0:
-            newest = mem[-1]
-            newest[2] += gradient                       # y = g_k - g_{k-1}
-            newest[1] = x_k - self.prev_model            # s = m_k - m_{k-1}
-            newest[0] = 1.0 / newest[2].inner_product(newest[1])
-            gamma = newest[1].inner_product(newest[2]) / newest[2].inner_product(newest[2])
+        if self.memory:
+            p = self.memory[-1]
+            gamma = p.s.inner_product(p.y) / p.y.inner_product(p.y)
+        self._last = (model, copy.deepcopy(gradient))
+        return -1.0 * two_loop(gradient, list(self.memory), gamma)
 
-        # first loop, newest to oldest
-        alphas = []
-        for rho, s, y in reversed(mem):
-            a = rho * s.inner_product(q)
-            q -= a * y
-            alphas.append(a)
-        alphas.reverse()
-        # second loop, oldest to newest
-        r = gamma * q
-        for a, (rho, s, y) in zip(alphas, mem):
-            b = rho * y.inner_product(r)
-            r += (a - b) * s
-        direction = -1.0 * r
+    def trial_length(self, value, gradient, iteration):
+        return self._scaled_first_length(value, gradient) if self._fresh else 1.0
 
-        a0kw = {"reset": self._reset_line_search}
-        self._reset_line_search = False
-        alpha = self.select_alpha(shots, gradient, direction, objective_arguments,
-                                  current_objective_value=current_objective_value, alpha0_kwargs=a0kw, **kwargs)
-        self._print("  alpha {0}".format(alpha))
-        self.store_history("alpha", iteration, alpha)
-
-        self.prev_model = x_k
-        mem.append([None, None, copy.deepcopy(-1 * gradient)])
-        return alpha * direction
-
-    def _compute_alpha0(self, phi0, grad0, reset=False, *args, **kwargs):
-        if reset:
-            return phi0 / (grad0.norm() * np.prod(self.solver.mesh.deltas)) ** 2
-        return 1.0
+    def step_taken(self, length, direction):
+        self._fresh = False
