@@ -26,9 +26,24 @@ import sys
 import types
 import warnings
 
-REFERENCE_ROOT = os.environ.get("PYSIT_REFERENCE_ROOT", "/root/reference")
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _REF_DIR = os.path.join(_HERE, "_ref")
+
+
+def _reference_root():
+    """The reference tree: PYSIT_REFERENCE_ROOT, else the tree that oracle/Makefile built
+    oracle/_ref from (recorded in _ref/reference_root.txt), else None."""
+    env = os.environ.get("PYSIT_REFERENCE_ROOT")
+    if env:
+        return env
+    try:
+        with open(os.path.join(_REF_DIR, "reference_root.txt")) as f:
+            return f.read().strip() or None
+    except OSError:
+        return None
+
+
+REFERENCE_ROOT = _reference_root() or ""
 _SWIG_FULLNAME = ("pysit.solvers.constant_density_acoustic.time.scalar."
                   "_constant_density_acoustic_time_scalar_cpp")
 

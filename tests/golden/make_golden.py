@@ -1,7 +1,7 @@
 """Generate the golden fixtures of tests/golden/ by running the unmodified reference.
 
-Run in a container that has the reference tree (default /root/reference) after
-``make -C oracle`` built its SWIG module into oracle/_ref:
+Run where the reference tree exists, after ``make -C oracle`` built its SWIG module into
+oracle/_ref (the tree is PYSIT_REFERENCE_ROOT or the one oracle/Makefile used):
 
     python tests/golden/make_golden.py            # all problems of tests/problems.py
     python tests/golden/make_golden.py lbfgs:o2   # the reference's LBFGS run on problem o2
