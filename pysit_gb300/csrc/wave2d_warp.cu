@@ -61,6 +61,9 @@ constexpr int kSpareBar = 15;          // the last of a warp's 16 mbarrier slots
 #ifndef PGB_RING_RB
 #define PGB_RING_RB 2      // rows per iteration of the FP32 interior sweep
 #endif
+#ifndef PGB_SHELL_RB
+#define PGB_SHELL_RB 1     // rows per iteration of the FP32 PML-shell sweep
+#endif
 
 template <typename T, int N> struct VecT;
 template <> struct VecT<float, 4> { using type = float4; };
@@ -101,7 +104,7 @@ struct Ring {
     static constexpr int WS = SEG + 2 * HZ;                      // slot with halo (elements)
     // rows per iteration: the FP32 interior sweeps two rows at a time (the per-row
     // bookkeeping is shared, and the 2R+2 rows of the window are read once)
-    static constexpr int RB = sizeof(T) == 4 && KIND == 0 ? PGB_RING_RB : 1;
+    static constexpr int RB = sizeof(T) == 4 ? (KIND == 0 ? PGB_RING_RB : PGB_SHELL_RB) : 1;
     static constexpr int AR = (MODE == kAdj || MODE == kBorn) && PGB_RING_AHEAD > 2 ? PGB_RING_AHEAD - 1 : PGB_RING_AHEAD;
     static constexpr int A = (AR + RB - 1) / RB < 2 ? 2 : (AR + RB - 1) / RB;  // iterations in flight
     static constexpr int NU = 2 * R + RB * A;                    // x-ring slots
@@ -160,6 +163,15 @@ template <typename T> __device__ __forceinline__ T rcp_(T x);
 // FP64 keeps the exact division of the reference
 template <> __device__ __forceinline__ float rcp_(float x) { return __fdividef(1.0f, x); }
 template <> __device__ __forceinline__ double rcp_(double x) { return 1.0 / x; }
+
+// Waits (full limit) for the `armed` stages from stage s on (phase parity ph, flipped past
+// the ring's end): the drain after an expired wait.
+__device__ __noinline__ void drain_stages(unsigned char* wsm, int s, uint32_t ph, int A, int armed) {
+    for (int j = 0; j < armed; ++j) {
+        const int sj = s + j < A ? s + j : s + j - A;
+        mbar_wait_bounded(reinterpret_cast<uint64_t*>(wsm) + sj, s + j < A ? ph : (ph ^ 1u), kPolls);
+    }
+}
 
 template <typename T, int R, int MODE, int KIND>
 __device__ __forceinline__ void sweep(const WaveParams<T>& p, unsigned char* wsm, Pipe& pp, const int shot,
@@ -258,23 +270,10 @@ __device__ __forceinline__ void sweep(const WaveParams<T>& p, unsigned char* wsm
         }
     }
 
-    // an expired wait at iteration `it`: every stage armed for iterations it .. it+A-1 may
-    // still receive bytes; wait for those phases with the full limit before leaving the task
-    auto drain = [&](int it) {
-        const int armed = min(A, nit - it);
-        for (int j = 0; j < armed; ++j) {
-            const int sj = pp.s + j < A ? pp.s + j : pp.s + j - A;
-            mbar_wait_bounded(reinterpret_cast<uint64_t*>(wsm) + sj, pp.s + j < A ? pp.ph : (pp.ph ^ 1u), kPolls);
-        }
-    };
     // test aid (WaveParams::wait_fault): a bounded wait on the warp's spare mbarrier, on which
     // nothing ever arrives, runs out and takes the expiry path with this task's copies in flight
-    if (p.wait_fault && !__all_sync(0xffffffffu, mbar_test_bounded(reinterpret_cast<uint64_t*>(wsm) + kSpareBar, 0u,
-                                                                  p.polls ? p.polls : 64u))) {
-        late = true;
-        drain(0);
-        return;
-    }
+    bool expired = p.wait_fault && !__all_sync(0xffffffffu, mbar_test_bounded(reinterpret_cast<uint64_t*>(wsm) + kSpareBar,
+                                                                               0u, p.polls ? p.polls : 64u));
 
     // per-lane constants
     bool zok[V];
@@ -308,15 +307,15 @@ __device__ __forceinline__ void sweep(const WaveParams<T>& p, unsigned char* wsm
     // sigma_x (and the mesh sigma_x) of the shell rows, loaded one iteration ahead
     T sx_n = PML ? __ldg(p.sgx + x0) : T(0);
     T mx_n = PML && MODE == kRecomp ? __ldg(p.mgx + x0) : T(0);
-    for (int it = 0; it < nit; ++it, o += (long long)RB * p.ldz) {
+    int it = 0;
+    for (; it < (expired ? 0 : nit); ++it, o += (long long)RB * p.ldz) {
         const int x = x0 + RB * it;
         const int s = pp.s;
         const bool ok = p.polls ? mbar_test_bounded(reinterpret_cast<uint64_t*>(wsm) + s, pp.ph, p.polls)
                                 : mbar_wait_bounded(reinterpret_cast<uint64_t*>(wsm) + s, pp.ph, kPolls);
         if (!__all_sync(0xffffffffu, ok)) {
-            late = true;
-            drain(it);
-            return;
+            expired = true;
+            break;
         }
         const unsigned char* sb = lb + OFF_P + s * STG;  // this lane in stage s
 
@@ -489,6 +488,12 @@ __device__ __forceinline__ void sweep(const WaveParams<T>& p, unsigned char* wsm
         }
         nxs += RB;
         if (nxs >= NU) nxs -= NU;
+    }
+    if (expired) {
+        // every stage armed for iterations it .. it+A-1 may still receive bytes: wait for those
+        // phases with the full limit before the warp leaves its tasks
+        late = true;
+        drain_stages(wsm, pp.s, pp.ph, A, min(A, nit - it));
     }
 }
 

@@ -302,7 +302,7 @@ class WavePlan:
 
     def _choose_schedule(self, lib, d, fixed_launch, nrec):
         """'store' with the largest balanced launch that fits in free device memory (at least
-        16 shots or all of them), else 'checkpoint'."""
+        8 shots or all of them), else 'checkpoint' with the largest balanced launch that fits."""
         torch = _native.require_cuda()
         free = torch.cuda.mem_get_info()[0]
         elem = 8 if self.tdtype == torch.float64 else 4
@@ -311,22 +311,31 @@ class WavePlan:
         G = self.shots_per_launch
         if fixed_launch:
             return "store" if self._workspace_for(lib, d, G, True, self.lanes) <= budget else "checkpoint"
-        b1 = self._workspace_for(lib, d, 1, True)
-        per = self._workspace_for(lib, d, 2, True) - b1
-        gmax = self.nshots if per <= 0 else int((budget - (b1 - per)) // per)
-        gmax = min(gmax, self.nshots)
-        if gmax < min(16, self.nshots):
-            return "checkpoint"
         lanes = self.lanes  # lanes are not split further: two half-size lanes measured slower in 2D
         per_lane = -(-self.nshots // lanes)           # shots of the largest lane
-        glane = max(1, min(gmax // lanes, per_lane))
-        launches = -(-per_lane // glane)
-        G = -(-per_lane // launches)
-        while G > 1 and self._workspace_for(lib, d, G, True, lanes) > budget:
-            G -= 1
-        self.shots_per_launch = G
-        self.lanes = lanes
-        return "store"
+
+        def fit(store):
+            """Largest balanced launch of this schedule within the budget (0: none fits)."""
+            b1 = self._workspace_for(lib, d, 1, store)
+            per = self._workspace_for(lib, d, 2, store) - b1
+            gmax = self.nshots if per <= 0 else int((budget - (b1 - per)) // per)
+            gmax = min(gmax, self.nshots)
+            if gmax < 1:
+                return 0
+            glane = max(1, min(gmax // lanes, per_lane))
+            g = -(-per_lane // -(-per_lane // glane))
+            while g > 1 and self._workspace_for(lib, d, g, store, lanes) > budget:
+                g -= 1
+            return g
+
+        g = fit(True)
+        if g >= min(8, self.nshots):
+            self.shots_per_launch = g
+            return "store"
+        # checkpointed: the largest launch that fits (one shot at least; the plan reports a
+        # workspace the device lacks when even that does not fit)
+        self.shots_per_launch = max(1, fit(False))
+        return "checkpoint"
 
     # ---------------------------------------------------------------------------
     def set_model(self):

@@ -174,7 +174,8 @@ def test_release_plans_empties_the_plan_cache():
     assert solver._plans == {}
 
 
-def _schedule_case(monkeypatch, nshots, free_gb, per_shot_gb, fixed=None, base_gb=1.0, nsteps=4000, nrec=1152):
+def _schedule_case(monkeypatch, nshots, free_gb, per_shot_gb, fixed=None, base_gb=1.0, nsteps=4000, nrec=1152,
+                   ckpt_per_shot_gb=None):
     """WavePlan._choose_schedule with a fake device (free memory) and a linear workspace model."""
     import types
     from pysit_gb300 import _native
@@ -187,7 +188,8 @@ def _schedule_case(monkeypatch, nshots, free_gb, per_shot_gb, fixed=None, base_g
 
     def workspace(lib, d, G, store, lanes=1):
         calls.append((G, store, lanes))
-        return int((base_gb + G * per_shot_gb) * GB)
+        per = per_shot_gb if store or ckpt_per_shot_gb is None else ckpt_per_shot_gb
+        return int((base_gb + G * per) * GB)
     plan = types.SimpleNamespace(nshots=nshots, nsteps=nsteps, tdtype="f32", shots_per_launch=fixed or nshots,
                                  lanes=1, _workspace_for=workspace)
     sched = WavePlan._choose_schedule(plan, None, None, fixed is not None, nrec)
@@ -207,9 +209,14 @@ def test_auto_schedule_takes_the_largest_balanced_launch(monkeypatch):
 
 
 def test_auto_schedule_falls_back_to_checkpoints(monkeypatch):
-    # fewer than 16 shots per launch would fit: the checkpointed schedule
-    sched, _, _ = _schedule_case(monkeypatch, 64, 120.0, 9.5)
-    assert sched == "checkpoint"
+    # fewer than 8 shots per launch would keep dWaveOp: the checkpointed schedule, with the
+    # largest balanced launch whose checkpoints fit (21 of 2.5 GB fit beside the traces in 60 GB:
+    # four launches of 16)
+    sched, G, _ = _schedule_case(monkeypatch, 64, 60.0, 9.5, ckpt_per_shot_gb=2.5)
+    assert (sched, G) == ("checkpoint", 16)
+    # 11 shots keep dWaveOp in 120 GB: enough for the kept schedule
+    sched, G, _ = _schedule_case(monkeypatch, 64, 120.0, 9.5)
+    assert (sched, G) == ("store", 11)
     # a fixed launch size is kept and decides alone
     sched, G, calls = _schedule_case(monkeypatch, 64, 280.0, 9.5, fixed=32)
     assert (sched, G) == ("checkpoint", 32) and calls == [(32, True, 1)]
