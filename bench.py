@@ -496,7 +496,8 @@ def main():
                          "forward_graph": {"launch_ms": fwd_launch_ms, "achieved_gbs": achieved,
                                            "gcell_per_s": fwd_gcells}},
             "gpu_launches": launches, "misfit_rnorm2": rn, "clocks": clocks,
-            "autotune": {"tile_x": tuned_grad["chosen"], "ms": {str(k): v for k, v in tuned_grad["ms"].items()},
+            "autotune": {"tile_x": tuned_grad["chosen"], "tile_z": tuned_grad["chosen_z"],
+                         "ms": {str(k): v for k, v in tuned_grad["ms"].items()},
                          "shell_share": tuned_grad.get("shell_share"), "forward_plan_tile_x": tuned["chosen"]}}
     if rank == 0 and not args.no_plain:
         plain = plain_fp64_baseline(scale=args.scale, nsteps_full=args.nsteps)

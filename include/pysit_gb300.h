@@ -185,6 +185,10 @@ typedef struct {
                                       the wait runs out and takes the expiry path above with the
                                       task's bulk copies in flight.  Lets a test check that path and
                                       the status report without any GPU fault */
+    int tile_z;                    /* 2D/3D: z extent of an interior task at most, in cells (a multiple of
+                                      4, >= 16); 0 = the kernel's full width (32 lanes x the lane vector:
+                                      128 cells in FP32, 64 in FP64).  Narrower tasks leave lanes idle but
+                                      make more tasks; pysit_plan_autotune_tiles chooses it by timing */
 } pysit_plan_desc;
 
 int pysit_plan_create(const pysit_plan_desc* desc, pysit_plan** out);
@@ -281,6 +285,15 @@ int pysit_plan_step_loop(pysit_plan* plan, int mode, int nsteps, void* stream);
  * wavefield buffers are left in an arbitrary state, as after step_loop. */
 int pysit_plan_autotune(pysit_plan* plan, const int* candidates, int ncand, int nsteps, int* chosen,
                         double* ms, void* stream);
+/* The autotuner over both tile dimensions, no counterpart in the reference: as
+ * pysit_plan_autotune for every pair of a task length along x in cand_x[ncx] (8..4096) and a
+ * z extent of the interior tasks in cand_z[ncz] (0 = the full width, else >= 16 cells);
+ * writes the fastest pair to *chosen_x / *chosen_z and the better of each pair's two times
+ * to ms[ix * ncz + iz] (may be NULL). */
+int pysit_plan_autotune_tiles(pysit_plan* plan, const int* cand_x, int ncx, const int* cand_z, int ncz,
+                              int nsteps, int* chosen_x, int* chosen_z, double* ms, void* stream);
+/* The plan's current task length along x and z extent of its interior tasks (0: full width). */
+int pysit_plan_get_tiles(const pysit_plan* plan, int* tile_x, int* tile_z);
 /* The plan's current tuning: task length along x and the three 2D shell block shares
  * (pysit_plan_desc.shell_share).  Either output may be NULL. */
 int pysit_plan_get_tuning(const pysit_plan* plan, int* tile_x, double* shell_share);

@@ -254,7 +254,8 @@ def run_gradient3d(scale=1.0, nshots=8, nsteps=3000, autotune=True):
     cells = int(np.prod(m.shape(include_bc=True, as_grid=True)))
     return {"shots": nshots, "nsteps": int(plan.nsteps), "grid": [int(v) for v in m.shape(include_bc=True, as_grid=True)],
             "checkpoint_every": plan.checkpoint_every, "workspace_gb": plan.workspace_bytes / 1e9,
-            "tile_x": tune["chosen"], "tune_ms": {str(k): v for k, v in tune.get("ms", {}).items()},
+            "tile_x": tune["chosen"], "tile_z": tune.get("chosen_z"),
+            "tune_ms": {str(k): v for k, v in tune.get("ms", {}).items()},
             "seconds": t, "wall_s": time.perf_counter() - t0, "shots_per_s": nshots / t,
             "gcell_per_s": 3 * cells * plan.nsteps * nshots / t / 1e9, "status": plan.status()}
 

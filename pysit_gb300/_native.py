@@ -63,6 +63,7 @@ class PlanDesc(C.Structure):
         ("lanes", _i),
         ("wait_polls", C.c_uint32),
         ("wait_fault", _i),
+        ("tile_z", _i),
     ]
 
 
@@ -95,6 +96,9 @@ _PROTOS = {
     "pysit_plan_last_launch_count": (_i, [_vp, C.POINTER(C.c_int64)]),
     "pysit_plan_step_loop": (_i, [_vp, _i, _i, _vp]),
     "pysit_plan_autotune": (_i, [_vp, C.POINTER(_i), _i, _i, C.POINTER(_i), C.POINTER(C.c_double), _vp]),
+    "pysit_plan_autotune_tiles": (_i, [_vp, C.POINTER(_i), _i, C.POINTER(_i), _i, _i, C.POINTER(_i), C.POINTER(_i),
+                                       C.POINTER(C.c_double), _vp]),
+    "pysit_plan_get_tiles": (_i, [_vp, C.POINTER(_i), C.POINTER(_i)]),
     "pysit_group_create": (_i, [C.POINTER(_vp), _i, C.POINTER(_vp)]),
     "pysit_group_destroy": (_i, [_vp]),
     "pysit_group_gradient": (_i, [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp), _vp]),

@@ -303,6 +303,10 @@ struct pysit_plan {
     virtual int step_loop(int mode, int nsteps, cudaStream_t s) = 0;
     virtual int autotune(const int* cand, int ncand, int nsteps, int* chosen, double* ms, cudaStream_t s) = 0;
     virtual int tuning(int* tile, double* share) const = 0;
+    // autotune over task lengths along x and z extents of the interior tasks (0: full width)
+    virtual int autotune2(const int* cx, int ncx, const int* cz, int ncz, int nsteps, int* chosen_x,
+                          int* chosen_z, double* ms, cudaStream_t s) = 0;
+    virtual int tiles(int* tile_x, int* tile_z) const = 0;
     // enqueue misfit + gradient on s without graph handling (for a group's capture)
     virtual int enqueue_grad_raw(const void* dobs, double* grad, double* rnorm2, cudaStream_t s) = 0;
     // linearised modelling / Gauss-Newton Hessian application for a model perturbation
@@ -322,6 +326,7 @@ struct PlanT final : public pysit_plan {
     int fwd_only = 0;            // forward modelling only: no adjoint, imaging or checkpoint buffers
     int nslots = 1;              // replay slots: S (checkpointed) or ceil(nsteps / p_img) (kept)
     int tile_req = 0;            // requested task length along x (0: default)
+    int tz = 0;                  // z extent of an interior task at most (0: the kernel's full width)
     unsigned wait_polls = 0;     // tries of a step kernel's bulk-copy wait (0: the kernels' default)
     int wait_fault = 0;          // test aid: the 2D step kernels' waits run out (pysit_plan_desc.wait_fault)
     std::vector<int> shot_steps; // record length of each shot in steps (empty: all nsteps)
@@ -419,6 +424,8 @@ struct PlanT final : public pysit_plan {
         store_all = d.store_dwaveop ? 1 : 0;
         fwd_only = d.forward_only ? 1 : 0;
         tile_req = d.tile_x > 0 ? d.tile_x : 0;
+        PGB_REQUIRE(d.tile_z == 0 || d.tile_z >= kMinTileZ, "tile_z %d below %d cells", d.tile_z, kMinTileZ);
+        tz = d.tile_z > 0 ? d.tile_z / 4 * 4 : 0;
         wait_polls = d.wait_polls;
         wait_fault = d.wait_fault ? 1 : 0;
         for (int m = 0; m < 3; ++m)
@@ -529,7 +536,9 @@ struct PlanT final : public pysit_plan {
     void add_tasks(int xa, int xb, int za, int zb, int kind) {
         if (xb <= xa || zb <= za) return;
         std::vector<std::pair<int, int>> zs;
-        split(za, zb, wave2d_warp_seg((int)sizeof(T), order, kind), zs);
+        int w = wave2d_warp_seg((int)sizeof(T), order, kind);
+        if (kind == 0 && tz > 0) w = std::min(w, tz);
+        split(za, zb, w, zs);
         const int nxc = (xb - xa + tx - 1) / tx, wx = (xb - xa + nxc - 1) / nxc;  // even x chunks
         for (int x = xa; x < xb; x += wx)
             for (auto& z : zs) {
@@ -568,7 +577,9 @@ struct PlanT final : public pysit_plan {
     void add_tasks3d(int xa, int xb, int ya, int yb, int za, int zb, int kind) {
         if (xb <= xa || yb <= ya || zb <= za) return;
         std::vector<std::pair<int, int>> zs;
-        split(za, zb, wave3d_seg((int)sizeof(T), kind), zs);
+        int w = wave3d_seg((int)sizeof(T), kind);
+        if (kind == 0 && tz > 0) w = std::min(w, tz);
+        split(za, zb, w, zs);
         const int rows = wave3d_rows_per_block();
         const int nxc = (xb - xa + tx - 1) / tx, wx = (xb - xa + nxc - 1) / nxc;
         for (int x = xa; x < xb; x += wx)
@@ -600,15 +611,18 @@ struct PlanT final : public pysit_plan {
         ntask3d[1] = (int)(tasks3d.size() / 6) - ntask3d[0];
     }
 
-    // ints of the task table for a task length tx_try (the current table is kept)
+    // ints of the task table for a task length tx_try and z extent tz_try (the current table is kept)
     static constexpr int kMinTileX = 8;
-    size_t task_ints(int tx_try) {
+    static constexpr int kMinTileZ = 16;
+    size_t task_ints(int tx_try, int tz_try) {
         if (dim == 1) return 0;
-        const int keep = tx;
+        const int keep = tx, keepz = tz;
         tx = tx_try;
+        tz = tz_try;
         size_t n;
         if (dim == 2) { build_tasks2d(); n = tasks2d.size(); } else { build_tasks3d(); n = tasks3d.size(); }
         tx = keep;
+        tz = keepz;
         if (dim == 2) build_tasks2d(); else build_tasks3d();
         return n;
     }
@@ -740,7 +754,7 @@ struct PlanT final : public pysit_plan {
         off.err = take(sizeof(int));
         off.ctr = take(2 * sizeof(unsigned long long));
         off.shsteps = take(std::max<size_t>(shot_steps.size(), 1) * sizeof(int));
-        task_cap = std::max<size_t>(task_ints(kMinTileX), std::max(tasks2d.size(), tasks3d.size()));
+        task_cap = std::max<size_t>(task_ints(kMinTileX, kMinTileZ), std::max(tasks2d.size(), tasks3d.size()));
         off.tasks = take(std::max<size_t>(task_cap, 1) * sizeof(int));
         off.partial = take(kRedBlocks * sizeof(double));
         off.rnorm = take(sizeof(double));
@@ -1332,26 +1346,37 @@ struct PlanT final : public pysit_plan {
     }
 
     int autotune(const int* cand, int ncand, int n, int* chosen, double* ms_out, cudaStream_t s) override {
+        int cz = tz, chosen_z = 0;
+        return autotune2(cand, ncand, &cz, 1, n, chosen, &chosen_z, ms_out, s);
+    }
+
+    // Every (x length, z extent) pair is timed twice, the second pass in reverse order; each
+    // keeps its faster time and the fastest pair stays.  ms_out[ix * ncz + iz].
+    int autotune2(const int* cx, int ncx, const int* cz, int ncz, int n, int* chosen_x, int* chosen_z,
+                  double* ms_out, cudaStream_t s) override {
         PGB_REQUIRE(ws, "no workspace bound");
         PGB_REQUIRE(model_set, "pysit_plan_set_model must be called first");
         PGB_REQUIRE(dim >= 2, "autotuning applies to the 2D and 3D task sweeps");
-        PGB_REQUIRE(cand && ncand >= 1 && chosen, "need at least one candidate and an output");
+        PGB_REQUIRE(cx && ncx >= 1 && cz && ncz >= 1 && chosen_x && chosen_z, "need candidates and outputs");
         PGB_REQUIRE(n >= 1, "nsteps must be >= 1");
-        for (int c = 0; c < ncand; ++c)
-            PGB_REQUIRE(cand[c] >= kMinTileX && cand[c] <= 4096, "candidate task length %d outside [%d, 4096]",
-                        cand[c], kMinTileX);
+        for (int c = 0; c < ncx; ++c)
+            PGB_REQUIRE(cx[c] >= kMinTileX && cx[c] <= 4096, "candidate task length %d outside [%d, 4096]", cx[c],
+                        kMinTileX);
+        for (int c = 0; c < ncz; ++c)
+            PGB_REQUIRE(cz[c] == 0 || cz[c] >= kMinTileZ, "candidate z extent %d below %d (0: full width)", cz[c],
+                        kMinTileZ);
         cudaEvent_t e0, e1;
         PGB_CHECK_CUDA(cudaEventCreate(&e0));
         PGB_CHECK_CUDA(cudaEventCreate(&e1));
-        int best = cand[0];
+        const int nc = ncx * ncz;
+        int best = 0;
         float best_ms = 1e30f;
         int rc = PYSIT_OK;
-        // two passes over the candidates, the second in reverse order; each keeps its faster time
-        std::vector<float> t(ncand, 1e30f);
+        std::vector<float> t(nc, 1e30f);
         for (int pass = 0; pass < 2 && rc == PYSIT_OK; ++pass)
-            for (int i = 0; i < ncand && rc == PYSIT_OK; ++i) {
-                const int c = pass == 0 ? i : ncand - 1 - i;
-                if ((rc = use_tile(cand[c], s))) break;
+            for (int i = 0; i < nc && rc == PYSIT_OK; ++i) {
+                const int c = pass == 0 ? i : nc - 1 - i;
+                if ((rc = use_tile(cx[c / ncz], cz[c % ncz], s))) break;
                 // the sweeps a gradient runs: forward (in recompute mode when dWaveOp is kept) and adjoint
                 const int fmode = store_all ? kRecomp : kFwd;
                 if ((rc = step_loop(fmode, 2, s))) break;  // warm-up
@@ -1363,15 +1388,22 @@ struct PlanT final : public pysit_plan {
                 cudaEventElapsedTime(&ms, e0, e1);
                 t[c] = std::min(t[c], ms);
             }
-        for (int c = 0; c < ncand && rc == PYSIT_OK; ++c) {
+        for (int c = 0; c < nc && rc == PYSIT_OK; ++c) {
             if (ms_out) ms_out[c] = t[c];
-            if (t[c] < best_ms) { best_ms = t[c]; best = cand[c]; }
+            if (t[c] < best_ms) { best_ms = t[c]; best = c; }
         }
-        if (rc == PYSIT_OK) rc = use_tile(best, s);
+        if (rc == PYSIT_OK) rc = use_tile(cx[best / ncz], cz[best % ncz], s);
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         if (rc) return rc;
-        *chosen = best;
+        *chosen_x = cx[best / ncz];
+        *chosen_z = cz[best % ncz];
+        return PYSIT_OK;
+    }
+
+    int tiles(int* tile_x, int* tile_z) const override {
+        if (tile_x) *tile_x = tx;
+        if (tile_z) *tile_z = tz;
         return PYSIT_OK;
     }
 
@@ -1382,10 +1414,11 @@ struct PlanT final : public pysit_plan {
         return PYSIT_OK;
     }
 
-    // rebuild and upload the task table for task length t; captured graphs hold the
-    // old table's counts, so they are dropped
-    int use_tile(int t, cudaStream_t s) {
+    // rebuild and upload the task table for task length t and z extent z; captured graphs
+    // hold the old table's counts, so they are dropped
+    int use_tile(int t, int z, cudaStream_t s) {
         tx = t;
+        tz = z > 0 ? z / 4 * 4 : 0;
         std::vector<int>& tab = dim == 3 ? (build_tasks3d(), tasks3d) : (build_tasks2d(), tasks2d);
         PGB_REQUIRE(tab.size() <= task_cap, "task table of %zu ints exceeds its buffer (%zu)", tab.size(), task_cap);
         PGB_CHECK_CUDA(cudaMemcpyAsync(ws + off.tasks, tab.data(), tab.size() * sizeof(int), cudaMemcpyHostToDevice, s));
@@ -1827,8 +1860,14 @@ struct LanesPlan final : public pysit_plan {
         return rc;
     }
     int autotune(const int* cand, int ncand, int n, int* chosen, double* ms, cudaStream_t s) override {
-        int rc = kids[0]->autotune(cand, ncand, n, chosen, ms, s);
-        for (int c = 1; c < lanes() && rc == PYSIT_OK; ++c) rc = kids[c]->use_tile(*chosen, s);
+        int cz = 0, chosen_z = 0;
+        kids[0]->tiles(nullptr, &cz);
+        return autotune2(cand, ncand, &cz, 1, n, chosen, &chosen_z, ms, s);
+    }
+    int autotune2(const int* cx, int ncx, const int* cz, int ncz, int n, int* chosen_x, int* chosen_z, double* ms,
+                  cudaStream_t s) override {
+        int rc = kids[0]->autotune2(cx, ncx, cz, ncz, n, chosen_x, chosen_z, ms, s);
+        for (int c = 1; c < lanes() && rc == PYSIT_OK; ++c) rc = kids[c]->use_tile(*chosen_x, *chosen_z, s);
         for (auto& kv : graphs)
             if (kv.second.first) cudaGraphExecDestroy(kv.second.first);
         graphs.clear();
@@ -1836,6 +1875,7 @@ struct LanesPlan final : public pysit_plan {
         return rc;
     }
     int tuning(int* tile, double* share) const override { return kids[0]->tuning(tile, share); }
+    int tiles(int* tile_x, int* tile_z) const override { return kids[0]->tiles(tile_x, tile_z); }
 };
 
 }  // namespace
@@ -1969,6 +2009,17 @@ extern "C" int pysit_plan_autotune(pysit_plan* p, const int* candidates, int nca
     PGB_REQUIRE(p, "NULL plan");
     return p->autotune(candidates, ncand, nsteps, chosen, ms, (cudaStream_t)stream);
 } PGB_API_CATCH("pysit_plan_autotune")
+
+extern "C" int pysit_plan_autotune_tiles(pysit_plan* p, const int* cand_x, int ncx, const int* cand_z, int ncz,
+                                         int nsteps, int* chosen_x, int* chosen_z, double* ms, void* stream) try {
+    PGB_REQUIRE(p, "NULL plan");
+    return p->autotune2(cand_x, ncx, cand_z, ncz, nsteps, chosen_x, chosen_z, ms, (cudaStream_t)stream);
+} PGB_API_CATCH("pysit_plan_autotune_tiles")
+
+extern "C" int pysit_plan_get_tiles(const pysit_plan* p, int* tile_x, int* tile_z) try {
+    PGB_REQUIRE(p, "NULL plan");
+    return p->tiles(tile_x, tile_z);
+} PGB_API_CATCH("pysit_plan_get_tiles")
 
 // ---- plan groups ------------------------------------------------------------------------
 struct pysit_group {

@@ -167,7 +167,20 @@ __device__ __forceinline__ T inject_rhs(const Inject<T>& inj, const int* bx, int
     int e0 = __ldg(rp + c), e1 = __ldg(rp + c + 1);
     const T* amp = inj.amp + shot * inj.amp_sstride;
     T acc = T(0);
-    for (int e = e0; e < e1; ++e) acc += __ldg(inj.w + e) * __ldg(amp + __ldg(inj.pt + e));
+    int e = e0;
+    // taps in groups of 8: the point indices and weights first, then the amplitudes, so that
+    // a group's dependent loads are in flight together (the sum keeps the taps' order)
+    for (; e + 8 <= e1; e += 8) {
+        int pt[8];
+        T w[8], a[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) { pt[q] = __ldg(inj.pt + e + q); w[q] = __ldg(inj.w + e + q); }
+#pragma unroll
+        for (int q = 0; q < 8; ++q) a[q] = __ldg(amp + pt[q]);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) acc += w[q] * a[q];
+    }
+    for (; e < e1; ++e) acc += __ldg(inj.w + e) * __ldg(amp + __ldg(inj.pt + e));
     return acc;
 }
 
@@ -181,7 +194,20 @@ __device__ __forceinline__ void record_block(const WaveParams<T>& p, int rb) {
     int e0 = __ldg(p.rec.rowptr + id), e1 = __ldg(p.rec.rowptr + id + 1);
     const T* u = p.u_cur + (long long)shot * p.fstride;
     T acc = T(0);
-    for (int e = e0; e < e1; ++e) acc += __ldg(p.rec.w + e) * u[__ldg(p.rec.off + e)];
+    int e = e0;
+    // taps in groups of 8: offsets and weights first, then the wavefield values, so that a
+    // group's dependent loads are in flight together (the sum keeps the taps' order)
+    for (; e + 8 <= e1; e += 8) {
+        long long off[8];
+        T w[8], v[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) { off[q] = __ldg(p.rec.off + e + q); w[q] = __ldg(p.rec.w + e + q); }
+#pragma unroll
+        for (int q = 0; q < 8; ++q) v[q] = __ldg(u + off[q]);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) acc += w[q] * v[q];
+    }
+    for (; e < e1; ++e) acc += __ldg(p.rec.w + e) * __ldg(u + __ldg(p.rec.off + e));
     p.rec.traces[shot * p.rec.tr_sstride + r] = acc;
 }
 

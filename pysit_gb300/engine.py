@@ -28,13 +28,21 @@ __all__ = ["WavePlan", "PlanGroup", "padded_cells", "default_checkpoint_every"]
 _DESC_AXIS = {1: [2], 2: [0, 2], 3: [0, 1, 2]}  # mesh axis -> (x, y, z) slot of the descriptor
 
 # tunings chosen by WavePlan.autotune (task length along x, 2D shell block shares per step
-# mode), per (dim, order, padded grid, dtype, psi form, shots per launch, schedule, forward
+# mode, z extent of the interior tasks), per (dim, order, padded grid, dtype, psi form, shots per launch, schedule, forward
 # only, lanes); later plans of the same configuration start from them.  With the environment
 # variable PYSIT_CUDA_TUNE_CACHE naming a JSON file, the table is read from that file on first
 # use and written back after every new tuning, so later processes on the machine start from it.
 _TUNED = {}
 _TUNE_FILES_READ = set()
 TILE_CANDIDATES = {2: (8, 16, 32, 64), 3: (8, 16, 32, 64)}
+# z extents of the interior tasks tried, as fractions of the kernels' full width (32 lanes x
+# the 16-byte lane vector: 128 cells in FP32, 64 in FP64); 0 stands for the full width
+TILE_Z_FRACTIONS = (1.0, 0.75, 0.5)
+
+
+def tile_z_candidates(dtype_bytes):
+    full = 32 * (16 // dtype_bytes)
+    return [0] + [max(16, int(full * f) // 4 * 4) for f in TILE_Z_FRACTIONS[1:]]
 
 
 def _tune_cache_file():
@@ -51,15 +59,16 @@ def _read_tunings(path):
     out = {}
     for row in rows if isinstance(rows, list) else []:
         try:
-            key, tile, share = row
-            out[ast.literal_eval(key)] = (int(tile), tuple(float(v) for v in share))
+            key, tile, share = row[:3]
+            tile_z = int(row[3]) if len(row) > 3 else 0
+            out[ast.literal_eval(key)] = (int(tile), tuple(float(v) for v in share), tile_z)
         except (ValueError, SyntaxError, TypeError):
             continue
     return out
 
 
 def _write_tunings(path, table):
-    rows = [[repr(k), v[0], list(v[1])] for k, v in table.items()]
+    rows = [[repr(k), v[0], list(v[1]), v[2] if len(v) > 2 else 0] for k, v in table.items()]
     tmp = f"{path}.{os.getpid()}.tmp"
     with open(tmp, "w") as f:
         json.dump(rows, f)
@@ -256,7 +265,9 @@ class WavePlan:
         d.tile_x = tuned[0] if tuned else 0
         for k in range(3):
             d.shell_share[k] = tuned[1][k] if tuned else 0.0
+        d.tile_z = tuned[2] if tuned and len(tuned) > 2 else 0
         self.tile_x = d.tile_x
+        self.tile_z = d.tile_z
 
         h = C.c_void_p()
         _native.check(lib.pysit_plan_create(C.byref(d), C.byref(h)))
@@ -441,25 +452,33 @@ class WavePlan:
                                                         C.c_void_p(_native.stream_handle())))
         return self.hess, self.rnorm2
 
-    def autotune(self, candidates=None, nsteps=48):
-        """Time the task lengths along x in `candidates` (forward + adjoint steps on this plan's
-        buffers), keep the fastest for this plan and for later plans of the same configuration.
-        Returns {"chosen": rows, "ms": {candidate: milliseconds}}.  1D plans have no tiles."""
+    def autotune(self, candidates=None, nsteps=48, z_candidates=None):
+        """Time every pair of a task length along x in `candidates` and a z extent of the
+        interior tasks in `z_candidates` (0: the full width; forward + adjoint steps on this
+        plan's buffers), keep the fastest for this plan and for later plans of the same
+        configuration.  Returns {"chosen": rows, "chosen_z": cells, "ms": {(x, z): milliseconds}}.
+        1D plans have no tiles."""
         if self.dim == 1:
-            return {"chosen": 0, "ms": {}}
+            return {"chosen": 0, "chosen_z": 0, "ms": {}}
+        torch = _native.require_cuda()
         cand = list(candidates or TILE_CANDIDATES[self.dim])
+        zc = list(z_candidates if z_candidates is not None
+                  else tile_z_candidates(8 if self.tdtype == torch.float64 else 4))
         self.set_model()
-        arr = (C.c_int * len(cand))(*cand)
-        ms = (C.c_double * len(cand))()
-        chosen = C.c_int()
-        _native.check(_native.load().pysit_plan_autotune(self._h, arr, len(cand), int(nsteps), C.byref(chosen), ms,
-                                                         C.c_void_p(_native.stream_handle())))
-        self.tile_x = int(chosen.value)
+        ax = (C.c_int * len(cand))(*cand)
+        az = (C.c_int * len(zc))(*zc)
+        ms = (C.c_double * (len(cand) * len(zc)))()
+        cx, cz = C.c_int(), C.c_int()
+        _native.check(_native.load().pysit_plan_autotune_tiles(
+            self._h, ax, len(cand), az, len(zc), int(nsteps), C.byref(cx), C.byref(cz), ms,
+            C.c_void_p(_native.stream_handle())))
+        self.tile_x, self.tile_z = int(cx.value), int(cz.value)
         tile, share = C.c_int(), (C.c_double * 3)()
         _native.check(_native.load().pysit_plan_get_tuning(self._h, C.byref(tile), share))
         self.shell_share = [float(v) for v in share]
-        _tuning_put(self._tune_key, (self.tile_x, tuple(self.shell_share)))
-        return {"chosen": self.tile_x, "ms": dict(zip(cand, list(ms))), "shell_share": self.shell_share}
+        _tuning_put(self._tune_key, (self.tile_x, tuple(self.shell_share), self.tile_z))
+        times = {(x, z): ms[i * len(zc) + j] for i, x in enumerate(cand) for j, z in enumerate(zc)}
+        return {"chosen": self.tile_x, "chosen_z": self.tile_z, "ms": times, "shell_share": self.shell_share}
 
     def step_loop(self, mode, nsteps):
         """Enqueue `nsteps` launches of one step kernel (0 forward, 1 recompute, 2 adjoint) on the

@@ -201,15 +201,22 @@ def test_status_word_clear_after_stable_run_and_flags_instability():
 
 @pytest.mark.parametrize("name", ["o8", "3d"])
 def test_autotuned_tiles_keep_the_gradient(name, golden):
-    """The autotuner rebuilds the task table with the fastest x-length; the gradient is unchanged."""
+    """The autotuner rebuilds the task table with the fastest (x length, interior z extent) pair;
+    the gradient is unchanged, also with interior tasks 16 cells deep (several z-segments)."""
     from pysit_gb300.engine import WavePlan
     g = golden(name)
     m, shots, solver, C, C0 = _setup(name, g)
     solver.model_parameters = solver.ModelParameters(m, {"C": C0})
     plan = WavePlan(solver, shots)
     plan.load_observed()
-    res = plan.autotune(candidates=(8, 16, 48), nsteps=4)
-    assert res["chosen"] in (8, 16, 48) and len(res["ms"]) == 3 and all(v > 0 for v in res["ms"].values())
+    res = plan.autotune(candidates=(8, 16, 48), nsteps=4, z_candidates=(0, 16))
+    assert res["chosen"] in (8, 16, 48) and res["chosen_z"] in (0, 16)
+    assert len(res["ms"]) == 6 and all(v > 0 for v in res["ms"].values())
+    grad, rn = plan.gradient()
+    assert plan.status() == 0
+    assert _rel(grad.cpu().numpy(), g["grad"]) < 1e-9
+    res = plan.autotune(candidates=(16,), nsteps=2, z_candidates=(16,))
+    assert (res["chosen"], res["chosen_z"]) == (16, 16)
     grad, rn = plan.gradient()
     assert plan.status() == 0
     assert _rel(grad.cpu().numpy(), g["grad"]) < 1e-9

@@ -1,6 +1,8 @@
 """Host-side mirror of the reference API (geometry, acquisition, factory, model
 arithmetic) against the reference's own outputs (golden fixtures, and the live
 reference where it is importable)."""
+import json
+
 import numpy as np
 import pytest
 
@@ -301,7 +303,7 @@ def test_tuning_cache_file_round_trip(monkeypatch, tmp_path):
     unreadable file is ignored; without the variable nothing is written."""
     from pysit_gb300 import engine
     key = (2, 8, (1232, 464), str(np.float32), 0, np.int64(22), "store", False, 1)
-    value = (16, (0.25, 0.3, 0.35))
+    value = (16, (0.25, 0.3, 0.35), 96)
     path = tmp_path / "tunings.json"
     monkeypatch.setattr(engine, "_TUNED", {})
     monkeypatch.setattr(engine, "_TUNE_FILES_READ", set())
@@ -316,6 +318,11 @@ def test_tuning_cache_file_round_trip(monkeypatch, tmp_path):
     monkeypatch.setattr(engine, "_TUNE_FILES_READ", set())
     assert engine._tuning_get(key) == value
     assert engine._tuning_get(key[:-1] + (2,)) is None
+    # a file written before z extents were tuned: rows of three entries read as the full width
+    path.write_text(json.dumps([[repr(engine._plain_key(key)), 16, [0.25, 0.3, 0.35]]]))
+    monkeypatch.setattr(engine, "_TUNED", {})
+    monkeypatch.setattr(engine, "_TUNE_FILES_READ", set())
+    assert engine._tuning_get(key) == (16, (0.25, 0.3, 0.35), 0)
     path.write_text("not json")
     monkeypatch.setattr(engine, "_TUNED", {})
     monkeypatch.setattr(engine, "_TUNE_FILES_READ", set())
