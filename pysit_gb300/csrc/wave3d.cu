@@ -42,22 +42,24 @@ __device__ __forceinline__ void record3(const WaveParams<T>& p, long long id) {
     p.rec.traces[shot * p.rec.tr_sstride + r] = acc;
 }
 
+// derivative taps around v (a cell's address) along a 32-bit stride s (a field of one
+// shot has fewer than 2^31 elements): first derivative sum_m a_m (v_+m - v_-m) ...
 template <typename T, int R>
-__device__ __forceinline__ T dd1(const T* __restrict__ v, long long o, long long s) {
+__device__ __forceinline__ T dd1(const T* __restrict__ v, int s) {
     T a = T(0);
 #pragma unroll
-    for (int m = 1; m <= R; ++m) a += T(d1w(R, m)) * (v[o + m * s] - v[o - m * s]);
+    for (int m = 1; m <= R; ++m) a += T(d1w(R, m)) * (v[m * s] - v[-m * s]);
     return a;
 }
-// second derivative in difference form: sum_m w_m ((v_+m - v_0) + (v_-m - v_0)),
+// ... and second derivative in difference form: sum_m w_m ((v_+m - v_0) + (v_-m - v_0)),
 // equal to the central stencil (the weights sum to zero) with far less FP32
 // cancellation than w_0 v_0 + sum_m w_m (v_+m + v_-m)
 template <typename T, int R>
-__device__ __forceinline__ T dd2(const T* __restrict__ v, long long o, long long s) {
-    const T c = v[o];
+__device__ __forceinline__ T dd2(const T* __restrict__ v, int s) {
+    const T c = v[0];
     T a = T(0);
 #pragma unroll
-    for (int m = 1; m <= R; ++m) a += T(d2w(R, m)) * ((v[o + m * s] - c) + (v[o - m * s] - c));
+    for (int m = 1; m <= R; ++m) a += T(d2w(R, m)) * ((v[m * s] - c) + (v[-m * s] - c));
     return a;
 }
 
@@ -66,38 +68,39 @@ __device__ __forceinline__ T dd2(const T* __restrict__ v, long long o, long long
 template <typename T, int R, int MODE>
 __device__ __forceinline__ void cell3d(const WaveParams<T>& p, const int shot, const int i, const int j,
                                        const int k) {
-    const long long sh = (long long)shot * p.fstride;
-    const long long ys = p.ldz, xs = (long long)p.rows_y * p.ldz;
-    const long long o = ((long long)(i + p.hx) * p.rows_y + (j + p.hy)) * p.ldz + kOZ + k;
-    const T* __restrict__ u = p.u_cur + sh;
+    // every operand is addressed from the cell's own offset (64-bit once) with 32-bit taps
+    const long long base = (long long)shot * p.fstride +
+                           ((long long)(i + p.hx) * p.rows_y + (j + p.hy)) * p.ldz + kOZ + k;
+    const long long o = base - (long long)shot * p.fstride;  // the cell in the shared C^2 field
+    const int ys = p.ldz, xs = p.rows_y * p.ldz;
+    const T* __restrict__ u = p.u_cur + base;
     const bool ok = i > 0 && i < p.nx - 1 && j > 0 && j < p.ny - 1 && k > 0 && k < p.nz - 1;
     const bool px = i < p.pxl || i >= p.nx - p.pxr;
     const bool py = j < p.pyl || j >= p.ny - p.pyr;
     const bool pz = k < p.pzl || k >= p.nz - p.pzr;
     const bool psireg = (int)px + (int)py + (int)pz >= 2;
     const T sx = __ldg(p.sgx + i), sy = __ldg(p.sgy + j), sz = __ldg(p.sgz + k);
-    const T uc = u[o], uo = p.u_prev[sh + o], c2 = __ldg(p.c2 + o);
-    T F = dd2<T, R>(u, o, xs) * p.idx2 + dd2<T, R>(u, o, ys) * p.idy2 + dd2<T, R>(u, o, 1) * p.idz2;
+    const T uc = u[0], uo = p.u_prev[base], c2 = __ldg(p.c2 + o);
+    T F = dd2<T, R>(u, xs) * p.idx2 + dd2<T, R>(u, ys) * p.idy2 + dd2<T, R>(u, 1) * p.idz2;
     // Phi derivatives: state is zero outside the padding, skip the reads where no tap can reach it
     const bool nearx = i - R < p.pxl || i + R >= p.nx - p.pxr;
     const bool neary = j - R < p.pyl || j + R >= p.ny - p.pyr;
     const bool nearz = k - R < p.pzl || k + R >= p.nz - p.pzr;
-    if (nearx || py || pz) F += dd1<T, R>(p.phx_in + sh, o, xs) * p.idx;
-    if (neary || px || pz) F += dd1<T, R>(p.phy_in + sh, o, ys) * p.idy;
-    if (nearz || px || py) F += dd1<T, R>(p.phz_in + sh, o, 1) * p.idz;
+    if (nearx || py || pz) F += dd1<T, R>(p.phx_in + base, xs) * p.idx;
+    if (neary || px || pz) F += dd1<T, R>(p.phy_in + base, ys) * p.idy;
+    if (nearz || px || py) F += dd1<T, R>(p.phz_in + base, 1) * p.idz;
     const int* bx = p.inj.box + shot * 6;
     if (p.inj.on) F += inject_rhs3(p.inj, bx, shot, i, j, k);
-    const T ps = psireg ? p.psi_in[sh + o] : T(0);
+    const T ps = psireg ? p.psi_in[base] : T(0);
     T unew;
     const bool pmlc = sx != T(0) || sy != T(0) || sz != T(0);
     if (pmlc) {
-        const T dudx = dd1<T, R>(u, o, xs) * p.idx, dudy = dd1<T, R>(u, o, ys) * p.idy,
-                dudz = dd1<T, R>(u, o, 1) * p.idz;
+        const T dudx = dd1<T, R>(u, xs) * p.idx, dudy = dd1<T, R>(u, ys) * p.idy, dudz = dd1<T, R>(u, 1) * p.idz;
         T dpsx = T(0), dpsy = T(0), dpsz = T(0);
-        if (sy != T(0) && sz != T(0)) dpsx = dd1<T, R>(p.psi_in + sh, o, xs) * p.idx;
-        if (sz != T(0) && sx != T(0)) dpsy = dd1<T, R>(p.psi_in + sh, o, ys) * p.idy;
-        if (sx != T(0) && sy != T(0)) dpsz = dd1<T, R>(p.psi_in + sh, o, 1) * p.idz;
-        const T phx = p.phx_in[sh + o], phy = p.phy_in[sh + o], phz = p.phz_in[sh + o];
+        if (sy != T(0) && sz != T(0)) dpsx = dd1<T, R>(p.psi_in + base, xs) * p.idx;
+        if (sz != T(0) && sx != T(0)) dpsy = dd1<T, R>(p.psi_in + base, ys) * p.idy;
+        if (sx != T(0) && sy != T(0)) dpsz = dd1<T, R>(p.psi_in + base, 1) * p.idz;
+        const T phx = p.phx_in[base], phy = p.phy_in[base], phz = p.phz_in[base];
         T nx_ = phx - p.dt * sx * phx + p.dt * (sy + sz - sx) * dudx + p.dt * (sy * sz * dpsx);
         T ny_ = phy - p.dt * sy * phy + p.dt * (sz + sx - sy) * dudy + p.dt * (sz * sx * dpsy);
         T nz_ = phz - p.dt * sz * phz + p.dt * (sx + sy - sz) * dudz + p.dt * (sx * sy * dpsz);
@@ -109,23 +112,23 @@ __device__ __forceinline__ void cell3d(const WaveParams<T>& p, const int shot, c
                        (sx * sy + sy * sz + sz * sx) * uc;
         unew = fac1 * fac2;
         if (!ok) { nx_ = ny_ = nz_ = unew = T(0); }
-        p.phx_out[sh + o] = nx_;
-        p.phy_out[sh + o] = ny_;
-        p.phz_out[sh + o] = nz_;
+        p.phx_out[base] = nx_;
+        p.phy_out[base] = ny_;
+        p.phz_out[base] = nz_;
     } else {
         unew = p.dt2 * c2 * F - (uo - T(2) * uc);
         if (!ok) unew = T(0);
     }
-    if (psireg) p.psi_out[sh + o] = ok ? ps + p.dt * uc : T(0);
-    p.u_prev[sh + o] = unew;
+    if (psireg) p.psi_out[base] = ok ? ps + p.dt * uc : T(0);
+    p.u_prev[base] = unew;
     if (MODE == kRecomp && p.dw_out) {
         T d = p.psi_c2 ? c2 * (F - (sx * sy * sz) * ps) : c2 * F - (sx * sy * sz) * ps;
         const T mx = __ldg(p.mgx + i), my = __ldg(p.mgy + j), mz = __ldg(p.mgz + k);
         d += ((mx + my + mz) - (sx + sy + sz)) * (unew - uo) * p.i2dt +
              ((mx * my + my * mz + mz * mx) - (sx * sy + sy * sz + sz * sx)) * uc + (mx * my * mz) * ps;
-        __stcs(p.dw_out + sh + o, ok ? d : T(0));
+        __stcs(p.dw_out + base, ok ? d : T(0));
     }
-    if (MODE == kAdj && p.image) p.ic[sh + o] += uc * __ldcs(p.dw_in + sh + o);
+    if (MODE == kAdj && p.image) p.ic[base] += uc * __ldcs(p.dw_in + base);
     if ((MODE == kFwd || (MODE == kRecomp && p.nan_check)) && p.err && !isfinite(unew))
         atomicOr(p.err, PGB_ERR_NONFINITE);
 }
@@ -369,12 +372,12 @@ __global__ void __launch_bounds__(256) wave1d_kernel(const WaveParams<T> p, int 
     const bool ok = k > 0 && k < p.nz - 1;
     const T sz = __ldg(p.sgz + k);
     const T uc = u[o], uo = p.u_prev[sh + o], c2 = __ldg(p.c2 + o);
-    T F = dd2<T, R>(u, o, 1) * p.idz2 + dd1<T, R>(p.phz_in + sh, o, 1) * p.idz;
+    T F = dd2<T, R>(u + o, 1) * p.idz2 + dd1<T, R>(p.phz_in + sh + o, 1) * p.idz;
     const int* bx = p.inj.box + shot * 6;
     if (p.inj.on) F += inject_rhs3(p.inj, bx, shot, 0, 0, k);
     T unew;
     if (sz != T(0)) {
-        const T dudz = dd1<T, R>(u, o, 1) * p.idz;
+        const T dudz = dd1<T, R>(u + o, 1) * p.idz;
         const T phz = p.phz_in[sh + o];
         T nz_ = phz - p.dt * sz * (phz + dudz);
         const T fac1 = T(2) * p.dt2 / (T(2) + p.dt * sz);
