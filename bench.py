@@ -45,10 +45,10 @@ sys.path.insert(0, ROOT)
 
 METRIC = "FWI gradient shots/s, batched adjoint vs plain, 1\u00d7GB300 at \u22641e-3 rel err; Gcell/s"
 # DRAM bytes (read + write) per shot of a launch of each 2D step (interior + PML-shell kernels),
-# from ncu captures of the same kernels at 22 shots per launch and task length 16
+# from one ncu capture of the three step modes at 22 shots per launch
 # (profiles/wave2d_steps_cfg2_22shots_dram.md); a launch's traffic is this times its shots (the
-# kernels' traffic grows in proportion to the shots).  None where no capture backs a number.
-TRAFFIC_PER_SHOT = {"forward": None, "recompute": 192.0e6 / 22, "adjoint": 326.5e6 / 22}
+# kernels' traffic grows in proportion to the shots).
+TRAFFIC_PER_SHOT = {"forward": 174.3e6 / 22, "recompute": 198.5e6 / 22, "adjoint": 335.5e6 / 22}
 
 
 def max_over_ranks(values, device):
@@ -437,7 +437,10 @@ def main():
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / nrep
         nb = w * ((4 + extra[name]) * n_int + (8 + extra[name]) * n_pml) * plan.shots_per_launch
+        # the same bytes with C^2 counted once per launch: the shots of a launch share one field
+        nd = nb - w * n_all * (plan.shots_per_launch - 1)
         modes[name] = {"launch_ms": ms, "bytes_per_launch": nb, "achieved_gbs": nb / (ms * 1e-3) / 1e9,
+                       "distinct_bytes_per_launch": nd, "distinct_gbs": nd / (ms * 1e-3) / 1e9,
                        "kernel_launches_per_step": plan.launches() // nrep}
     if plan.status():
         raise RuntimeError("device status flags set during the kernel timing")
@@ -487,12 +490,17 @@ def main():
                          "frac": dom["achieved_gbs"] / peak,
                          "traffic": (TRAFFIC_PER_SHOT[dom_name] * shots_per_launch
                                      if TRAFFIC_PER_SHOT.get(dom_name) else None),
-                         "traffic_note": "ncu capture at 22 shots per launch, task length 16, scaled by shots",
+                         "traffic_note": "ncu capture at 22 shots per launch, scaled by shots",
+                         "frac_distinct": dom["distinct_gbs"] / peak,
+                         "frac_distinct_note": "the same launch time against the bytes with C^2 read once per "
+                                               "launch (it is shared by the launch's shots)",
                          "peak_kind": peak_kind,
                          "kernel": f"2D {dom_name} step (interior + PML-shell kernels)",
                          "bytes_per_launch": dom["bytes_per_launch"], "launch_ms": dom["launch_ms"],
                          "modes": {k: {"launch_ms": v["launch_ms"], "achieved_gbs": v["achieved_gbs"],
-                                       "frac": v["achieved_gbs"] / peak} for k, v in modes.items()},
+                                       "frac": v["achieved_gbs"] / peak,
+                                       "frac_distinct": v["distinct_gbs"] / peak,
+                                       "traffic": TRAFFIC_PER_SHOT[k] * shots_per_launch} for k, v in modes.items()},
                          "forward_graph": {"launch_ms": fwd_launch_ms, "achieved_gbs": achieved,
                                            "gcell_per_s": fwd_gcells}},
             "gpu_launches": launches, "misfit_rnorm2": rn, "clocks": clocks,
