@@ -356,6 +356,7 @@ struct PlanT final : public pysit_plan {
     int rec_box_max = 0;              // largest receiver injection box (cells) over the shots
     bool rec_in_shell = false;        // 2D: every receiver box lies in cells of PML-shell tasks only
     std::vector<int> rec_rows;        // [nshots*nrec+1]
+    int rec_lanes = 1;                // recorder threads per (shot, receiver)
     std::vector<long long> rec_off;   // internal offsets
     std::vector<double> rec_ws;       // sampling weights
     std::vector<double> src_amp;      // [nshots][nsteps][nsrc]
@@ -572,7 +573,8 @@ struct PlanT final : public pysit_plan {
 
     // 3D block tasks: the interior box (R cells clear of the padding, off the outer
     // ring, z-bounds multiples of 4) and the six slabs of the shell around it; x in
-    // chunks of about tx rows, y in groups of one row per warp, z in segments.
+    // chunks of about tx rows, z in segments, y in groups of the rows one block
+    // covers (a shell warp takes several rows of a narrow z segment).
     // Consecutive tasks are neighbouring y-groups (their halo rows meet in L2).
     void add_tasks3d(int xa, int xb, int ya, int yb, int za, int zb, int kind) {
         if (xb <= xa || yb <= ya || zb <= za) return;
@@ -580,11 +582,11 @@ struct PlanT final : public pysit_plan {
         int w = wave3d_seg((int)sizeof(T), kind);
         if (kind == 0 && tz > 0) w = std::min(w, tz);
         split(za, zb, w, zs);
-        const int rows = wave3d_rows_per_block();
         const int nxc = (xb - xa + tx - 1) / tx, wx = (xb - xa + nxc - 1) / nxc;
         for (int x = xa; x < xb; x += wx)
             for (auto& z : zs)
-                for (int y = ya; y < yb; y += rows) {
+                for (int y = ya, rows = wave3d_task_rows((int)sizeof(T), kind, z.second - z.first); y < yb;
+                     y += rows) {
                     int t[6] = {x, std::min(xb, x + wx), y, std::min(yb, y + rows), z.first, z.second};
                     tasks3d.insert(tasks3d.end(), t, t + 6);
                 }
@@ -697,6 +699,10 @@ struct PlanT final : public pysit_plan {
                 cnt[(size_t)s * nrec + d.rec_tap_point[e] + 1]++;
             }
         for (size_t r = 0; r < (size_t)nshots * nrec; ++r) rec_rows[r + 1] = (int)(rec_rows[r] + cnt[r + 1]);
+        // threads per receiver: about 8 taps a thread, at most a warp
+        const double mean_taps = nshots * nrec > 0 ? (double)total / ((double)nshots * nrec) : 0.0;
+        rec_lanes = 1;
+        while (rec_lanes < 32 && rec_lanes * 8 < mean_taps) rec_lanes *= 2;
         rec_off.assign(total, 0);
         rec_ws.assign(total, 0.0);
         std::vector<int> fill(rec_rows.begin(), rec_rows.end() - 1);
@@ -1437,7 +1443,8 @@ struct PlanT final : public pysit_plan {
         p.rec.traces = tr_k;
         p.rec.tr_sstride = (long long)nsteps * nrec;
         p.rec.nrec = nrec;
-        p.rec.blocks = nrec > 0 ? ceil_div((long long)gn * nrec, bz) : 0;
+        p.rec.lanes = rec_lanes;
+        p.rec.blocks = nrec > 0 ? ceil_div((long long)gn * nrec * rec_lanes, bz) : 0;
     }
 
     void enqueue_forward(void* traces_out, cudaStream_t s) {

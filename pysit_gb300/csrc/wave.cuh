@@ -101,6 +101,7 @@ struct Record {
     long long tr_sstride;    // stride between shots in the trace array
     int nrec;
     int blocks;              // number of recorder blocks appended to the grid
+    int lanes;               // threads per (shot, receiver): a power of two up to 32
 };
 
 template <typename T>
@@ -184,31 +185,42 @@ __device__ __forceinline__ T inject_rhs(const Inject<T>& inj, const int* bx, int
     return acc;
 }
 
-// trace recorder block: one thread per (shot, receiver), taps summed in order
+// trace recorder block: p.rec.lanes threads per (shot, receiver).  Lane l sums taps
+// l, l + lanes, ... in order; a fixed butterfly over the lanes adds the partial sums,
+// so the result does not depend on scheduling.  Every thread of the block takes part
+// (the butterfly shuffles over whole warps).
 template <typename T>
 __device__ __forceinline__ void record_block(const WaveParams<T>& p, int rb) {
-    int id = rb * blockDim.x + threadIdx.x;
-    int total = p.nshot * p.rec.nrec;
-    if (id >= total) return;
-    int shot = id / p.rec.nrec, r = id - shot * p.rec.nrec;
-    int e0 = __ldg(p.rec.rowptr + id), e1 = __ldg(p.rec.rowptr + id + 1);
-    const T* u = p.u_cur + (long long)shot * p.fstride;
+    const int G = p.rec.lanes;
+    const long long t = (long long)rb * blockDim.x + threadIdx.x;
+    const long long id = t / G;
+    const int l = (int)(t & (G - 1));
+    const long long total = (long long)p.nshot * p.rec.nrec;
     T acc = T(0);
-    int e = e0;
-    // taps in groups of 8: offsets and weights first, then the wavefield values, so that a
-    // group's dependent loads are in flight together (the sum keeps the taps' order)
-    for (; e + 8 <= e1; e += 8) {
-        long long off[8];
-        T w[8], v[8];
+    if (id < total) {
+        const int shot = (int)(id / p.rec.nrec);
+        const int e1 = __ldg(p.rec.rowptr + id + 1);
+        const T* u = p.u_cur + (long long)shot * p.fstride;
+        int e = __ldg(p.rec.rowptr + id) + l;
+        // a lane's taps in groups of 4: offsets and weights first, then the wavefield
+        // values, so that a group's dependent loads are in flight together
+        for (; e + 3 * G < e1; e += 4 * G) {
+            long long off[4];
+            T w[4], v[4];
 #pragma unroll
-        for (int q = 0; q < 8; ++q) { off[q] = __ldg(p.rec.off + e + q); w[q] = __ldg(p.rec.w + e + q); }
+            for (int q = 0; q < 4; ++q) { off[q] = __ldg(p.rec.off + e + q * G); w[q] = __ldg(p.rec.w + e + q * G); }
 #pragma unroll
-        for (int q = 0; q < 8; ++q) v[q] = __ldg(u + off[q]);
+            for (int q = 0; q < 4; ++q) v[q] = __ldg(u + off[q]);
 #pragma unroll
-        for (int q = 0; q < 8; ++q) acc += w[q] * v[q];
+            for (int q = 0; q < 4; ++q) acc += w[q] * v[q];
+        }
+        for (; e < e1; e += G) acc += __ldg(p.rec.w + e) * __ldg(u + __ldg(p.rec.off + e));
     }
-    for (; e < e1; ++e) acc += __ldg(p.rec.w + e) * __ldg(u + __ldg(p.rec.off + e));
-    p.rec.traces[shot * p.rec.tr_sstride + r] = acc;
+    for (int m = G >> 1; m > 0; m >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, m);
+    if (id < total && l == 0) {
+        const int shot = (int)(id / p.rec.nrec), r = (int)(id - (long long)shot * p.rec.nrec);
+        p.rec.traces[shot * p.rec.tr_sstride + r] = acc;
+    }
 }
 
 // persistent-warp 2D sweep fed by shared-memory row rings, one task kind per
@@ -223,12 +235,12 @@ int wave2d_warp_seg(int dtype_bytes, int order, int pml);
 // resident task blocks of the whole GPU for one (dtype, order, mode, kind)
 int wave2d_warp_blocks(int dtype_bytes, int order, int mode, int kind);
 void wave2d_warp_prepare();
-// 3D block tasks (x0, x1, y0, y1, zs, ze): one block of wave3d_rows_per_block()
-// warps (one y-row each) per task and shot; KIND 0 interior, 1 PML shell
+// 3D block tasks (x0, x1, y0, y1, zs, ze): one block per task and shot; KIND 0
+// interior (one y-row per warp), 1 PML shell (32 / vectors-of-z rows per warp)
 template <typename T, int R, int MODE, int KIND>
 void launch_wave3d_tasks(const WaveParams<T>& p, const int* tasks, int ntasks, cudaStream_t s);
-int wave3d_rows_per_block();
 int wave3d_seg(int dtype_bytes, int kind);  // widest z-range of a task of each kind
+int wave3d_task_rows(int dtype_bytes, int kind, int zcells);  // y-rows of a task of zcells z-cells
 template <typename T, int R, int MODE>
 void launch_wave1d(const WaveParams<T>& p, int bz, cudaStream_t s);
 

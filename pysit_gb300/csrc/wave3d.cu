@@ -5,7 +5,8 @@
 //
 // 3D: a table of block tasks covers the padded grid once (interior: R cells
 // clear of the padding and off the outer ring; PML shell: the rest).  Each kind
-// is its own kernel; both sweep along x with the neighbour planes in L1.
+// is its own kernel; both sweep along x with the neighbour planes in L1, V cells
+// (one 16-byte vector) per lane.
 // 1D: one thread per cell.
 //
 // 3D auxiliary state: Phi_x/y/z is non-zero only inside the padding; psi
@@ -63,76 +64,6 @@ __device__ __forceinline__ T dd2(const T* __restrict__ v, int s) {
     return a;
 }
 
-// One cell of the reference's 3D step (_3D.h:107-235) with the batched fusions:
-// the general path, PML included.  Cells of the outer ring get zero.
-template <typename T, int R, int MODE>
-__device__ __forceinline__ void cell3d(const WaveParams<T>& p, const int shot, const int i, const int j,
-                                       const int k) {
-    // every operand is addressed from the cell's own offset (64-bit once) with 32-bit taps
-    const long long base = (long long)shot * p.fstride +
-                           ((long long)(i + p.hx) * p.rows_y + (j + p.hy)) * p.ldz + kOZ + k;
-    const long long o = base - (long long)shot * p.fstride;  // the cell in the shared C^2 field
-    const int ys = p.ldz, xs = p.rows_y * p.ldz;
-    const T* __restrict__ u = p.u_cur + base;
-    const bool ok = i > 0 && i < p.nx - 1 && j > 0 && j < p.ny - 1 && k > 0 && k < p.nz - 1;
-    const bool px = i < p.pxl || i >= p.nx - p.pxr;
-    const bool py = j < p.pyl || j >= p.ny - p.pyr;
-    const bool pz = k < p.pzl || k >= p.nz - p.pzr;
-    const bool psireg = (int)px + (int)py + (int)pz >= 2;
-    const T sx = __ldg(p.sgx + i), sy = __ldg(p.sgy + j), sz = __ldg(p.sgz + k);
-    const T uc = u[0], uo = p.u_prev[base], c2 = __ldg(p.c2 + o);
-    T F = dd2<T, R>(u, xs) * p.idx2 + dd2<T, R>(u, ys) * p.idy2 + dd2<T, R>(u, 1) * p.idz2;
-    // Phi derivatives: state is zero outside the padding, skip the reads where no tap can reach it
-    const bool nearx = i - R < p.pxl || i + R >= p.nx - p.pxr;
-    const bool neary = j - R < p.pyl || j + R >= p.ny - p.pyr;
-    const bool nearz = k - R < p.pzl || k + R >= p.nz - p.pzr;
-    if (nearx || py || pz) F += dd1<T, R>(p.phx_in + base, xs) * p.idx;
-    if (neary || px || pz) F += dd1<T, R>(p.phy_in + base, ys) * p.idy;
-    if (nearz || px || py) F += dd1<T, R>(p.phz_in + base, 1) * p.idz;
-    const int* bx = p.inj.box + shot * 6;
-    if (p.inj.on) F += inject_rhs3(p.inj, bx, shot, i, j, k);
-    const T ps = psireg ? p.psi_in[base] : T(0);
-    T unew;
-    const bool pmlc = sx != T(0) || sy != T(0) || sz != T(0);
-    if (pmlc) {
-        const T dudx = dd1<T, R>(u, xs) * p.idx, dudy = dd1<T, R>(u, ys) * p.idy, dudz = dd1<T, R>(u, 1) * p.idz;
-        T dpsx = T(0), dpsy = T(0), dpsz = T(0);
-        if (sy != T(0) && sz != T(0)) dpsx = dd1<T, R>(p.psi_in + base, xs) * p.idx;
-        if (sz != T(0) && sx != T(0)) dpsy = dd1<T, R>(p.psi_in + base, ys) * p.idy;
-        if (sx != T(0) && sy != T(0)) dpsz = dd1<T, R>(p.psi_in + base, 1) * p.idz;
-        const T phx = p.phx_in[base], phy = p.phy_in[base], phz = p.phz_in[base];
-        T nx_ = phx - p.dt * sx * phx + p.dt * (sy + sz - sx) * dudx + p.dt * (sy * sz * dpsx);
-        T ny_ = phy - p.dt * sy * phy + p.dt * (sz + sx - sy) * dudy + p.dt * (sz * sx * dpsy);
-        T nz_ = phz - p.dt * sz * phz + p.dt * (sx + sy - sz) * dudz + p.dt * (sx * sy * dpsz);
-        const T fac1 = T(2) * p.dt2 / (T(2) + p.dt * (sx + sy + sz));
-        // the reference multiplies sigma_x sigma_y sigma_z psi by C^2 (_3D.h:219); the
-        // consistent form (psi_c2 = 0) leaves it out, as the matrix operator does
-        const T src = p.psi_c2 ? c2 * (F - (sx * sy * sz) * ps) : c2 * F - (sx * sy * sz) * ps;
-        const T fac2 = src - (uo - T(2) * uc) * p.idt2 + (sx + sy + sz) * uo * p.i2dt -
-                       (sx * sy + sy * sz + sz * sx) * uc;
-        unew = fac1 * fac2;
-        if (!ok) { nx_ = ny_ = nz_ = unew = T(0); }
-        p.phx_out[base] = nx_;
-        p.phy_out[base] = ny_;
-        p.phz_out[base] = nz_;
-    } else {
-        unew = p.dt2 * c2 * F - (uo - T(2) * uc);
-        if (!ok) unew = T(0);
-    }
-    if (psireg) p.psi_out[base] = ok ? ps + p.dt * uc : T(0);
-    p.u_prev[base] = unew;
-    if (MODE == kRecomp && p.dw_out) {
-        T d = p.psi_c2 ? c2 * (F - (sx * sy * sz) * ps) : c2 * F - (sx * sy * sz) * ps;
-        const T mx = __ldg(p.mgx + i), my = __ldg(p.mgy + j), mz = __ldg(p.mgz + k);
-        d += ((mx + my + mz) - (sx + sy + sz)) * (unew - uo) * p.i2dt +
-             ((mx * my + my * mz + mz * mx) - (sx * sy + sy * sz + sz * sx)) * uc + (mx * my * mz) * ps;
-        __stcs(p.dw_out + base, ok ? d : T(0));
-    }
-    if (MODE == kAdj && p.image) p.ic[base] += uc * __ldcs(p.dw_in + base);
-    if ((MODE == kFwd || (MODE == kRecomp && p.nan_check)) && p.err && !isfinite(unew))
-        atomicOr(p.err, PGB_ERR_NONFINITE);
-}
-
 // ---- task sweeps ---------------------------------------------------------------
 // A task (x0, x1, y0, y1, zs, ze) is handled by one block: warp w owns y-row
 // y0 + w and sweeps x0..x1-1 over the z-range [zs, ze).  The block's rows of the
@@ -172,28 +103,6 @@ __device__ __forceinline__ void prefetch_row(const WaveParams<T>& p, long long s
             pf_l1(p.phy_in + sh + o - m * ys);
             pf_l1(p.phy_in + sh + o + m * ys);
         }
-    }
-}
-
-// PML shell: one cell per lane, the general per-cell update
-#ifndef PGB_3D_SHELL_MINB
-#define PGB_3D_SHELL_MINB 4  // resident shell blocks per SM the register budget aims at (64 registers)
-#endif
-template <typename T, int R, int MODE>
-__global__ void __launch_bounds__(kW3 * 32, PGB_3D_SHELL_MINB) wave3d_shell_kernel(const WaveParams<T> p, const int* __restrict__ tasks,
-                                                               int ntasks) {
-    const int shot = blockIdx.x / ntasks;
-    const int* tk = tasks + 6 * (blockIdx.x - shot * ntasks);
-    const int j = __ldg(tk + 2) + (threadIdx.x >> 5);
-    const int k = __ldg(tk + 4) + (threadIdx.x & 31);
-    if (j >= __ldg(tk + 3) || k >= __ldg(tk + 5)) return;
-    const int x1 = __ldg(tk + 1);
-    const long long sh = (long long)shot * p.fstride;
-    const long long xs = (long long)p.rows_y * p.ldz;
-    const long long o0 = ((long long)(p.hx) * p.rows_y + (j + p.hy)) * p.ldz + kOZ + k;  // row x = 0
-    for (int i = __ldg(tk); i < x1; ++i) {
-        prefetch_row<T, R, MODE, true>(p, sh, o0 + (long long)min(i + PGB_3D_AHEAD, x1 - 1) * xs);
-        cell3d<T, R, MODE>(p, shot, i, j, k);
     }
 }
 
@@ -355,6 +264,323 @@ __global__ void __launch_bounds__(kW3 * 32, (sizeof(T) == 4 ? PGB_3D_INT_MINB : 
     if (MODE != kAdj && bad && p.err) atomicOr(p.err, PGB_ERR_NONFINITE);
 }
 
+// a lane's V cells as an array (the components of a vector load)
+template <typename T>
+__device__ __forceinline__ T vc(const typename Vec3<T>::type& a, int v) {
+    return reinterpret_cast<const T*>(&a)[v];
+}
+
+// store the first n of a lane's V cells: one vector store when all belong to the task
+template <typename T, bool STREAM>
+__device__ __forceinline__ void st_lane(T* q, const T* a, int n) {
+    using VT = typename Vec3<T>::type;
+    constexpr int V = Vec3<T>::N;
+    if (n == V) {
+        if constexpr (STREAM) __stcs(reinterpret_cast<VT*>(q), *reinterpret_cast<const VT*>(a));
+        else *reinterpret_cast<VT*>(q) = *reinterpret_cast<const VT*>(a);
+    } else {
+#pragma unroll
+        for (int v = 0; v < V; ++v)
+            if (v < n) {
+                if constexpr (STREAM) __stcs(q + v, a[v]);
+                else q[v] = a[v];
+            }
+    }
+}
+
+// first derivative sum_m a_m (v_+m - v_-m) of each of a lane's cells along x or y
+// from the 2R tap vectors t (t[R - m] at -m, t[R + m - 1] at +m), scaled by h
+template <typename T, int R>
+__device__ __forceinline__ void dd1_taps(const typename Vec3<T>::type (&t)[2 * R], T h, T* out) {
+#pragma unroll
+    for (int v = 0; v < Vec3<T>::N; ++v) {
+        T a = T(0);
+#pragma unroll
+        for (int m = 1; m <= R; ++m) a += T(d1w(R, m)) * (vc<T>(t[R + m - 1], v) - vc<T>(t[R - m], v));
+        out[v] = a * h;
+    }
+}
+template <typename T, int R>
+__device__ __forceinline__ void load_taps(const T* q, int s, typename Vec3<T>::type (&t)[2 * R]) {
+#pragma unroll
+    for (int m = 1; m <= R; ++m) {
+        t[R - m] = ldv(q - m * s);
+        t[R + m - 1] = ldv(q + m * s);
+    }
+}
+// the centre window along z: the lane's V cells with HZ cells on either side
+template <typename T, int NB>
+__device__ __forceinline__ void load_window(const T* q, T* w) {
+    constexpr int V = Vec3<T>::N;
+#pragma unroll
+    for (int b = 0; b <= 2 * NB; ++b) {
+        const typename Vec3<T>::type a = ldv(q + (b - NB) * V);
+#pragma unroll
+        for (int v = 0; v < V; ++v) w[b * V + v] = vc<T>(a, v);
+    }
+}
+
+// PML shell: V cells per lane along z (16-byte vectors), each with the general
+// update of the reference's 3D step (_3D.h:107-235) and the batched fusions.  A
+// task's z-range [zs, ze) (zs a multiple of 4, at most 32 vectors) takes nzv
+// lanes of a y-row and a warp 32 / nzv rows; cells of a vector at or past ze are
+// read (zero padding) but not written.  Operand groups no cell of the lane needs
+// are skipped: Phi taps that can only meet zero state, psi away from the bands
+// where two axes are in the padding, the PML terms where no sigma is set.  Cells
+// of the outer ring get zero.
+#ifndef PGB_3D_SHELL_WARPS
+#define PGB_3D_SHELL_WARPS 8  // warps of a shell block
+#endif
+#ifndef PGB_3D_SHELL_MINB
+#define PGB_3D_SHELL_MINB (16 / PGB_3D_SHELL_WARPS)  // resident shell blocks per SM (FP32): 128 registers
+#endif
+constexpr int kW3S = PGB_3D_SHELL_WARPS;
+template <typename T, int R, int MODE>
+__global__ void __launch_bounds__(kW3S * 32, (sizeof(T) == 4 ? PGB_3D_SHELL_MINB : 1))
+    wave3d_shell_kernel(const WaveParams<T> p, const int* __restrict__ tasks, int ntasks) {
+    using VT = typename Vec3<T>::type;
+    constexpr int V = Vec3<T>::N;
+    constexpr int AL = 16 / (int)sizeof(T);
+    constexpr int HZ = (R + AL - 1) / AL * AL;
+    constexpr int NB = HZ / V;
+    constexpr int NW = (2 * NB + 1) * V;
+    constexpr int C0 = NB * V;
+    const int shot = blockIdx.x / ntasks;
+    const int* tk = tasks + 6 * (blockIdx.x - shot * ntasks);
+    const int zs = __ldg(tk + 4), ze = __ldg(tk + 5);
+    const int nzv = (ze - zs + V - 1) / V, rpw = 32 / nzv;
+    const int lane = threadIdx.x & 31, r = lane / nzv;
+    const int j = __ldg(tk + 2) + (threadIdx.x >> 5) * rpw + r;
+    if (r >= rpw || j >= __ldg(tk + 3)) return;
+    const int zl = zs + (lane - r * nzv) * V;
+    const int nv = min(V, ze - zl);  // cells of the lane's vector inside the task
+    const int x0 = __ldg(tk), x1 = __ldg(tk + 1);
+    const long long sh = (long long)shot * p.fstride;
+    const int ys = p.ldz, xs = p.rows_y * p.ldz;  // a field of one shot has fewer than 2^31 elements
+    // what the x sweep does not change: y and z sigmas and masks
+    const T sy = __ldg(p.sgy + j);
+    const T my = MODE == kRecomp ? __ldg(p.mgy + j) : T(0);
+    const bool py = j < p.pyl || j >= p.ny - p.pyr;
+    const bool neary = j - R < p.pyl || j + R >= p.ny - p.pyr;
+    T sz[V], mz[V];
+    bool okz[V], pz[V];
+    bool any_sz = false, any_pz = false, any_nearz = false;
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+        const int k = zl + v;
+        const bool in = v < nv;
+        sz[v] = in ? __ldg(p.sgz + k) : T(0);
+        mz[v] = in && MODE == kRecomp ? __ldg(p.mgz + k) : T(0);
+        okz[v] = in && j > 0 && j < p.ny - 1 && k > 0 && k < p.nz - 1;
+        pz[v] = in && (k < p.pzl || k >= p.nz - p.pzr);
+        any_sz |= sz[v] != T(0);
+        any_pz |= pz[v];
+        any_nearz |= in && (k - R < p.pzl || k + R >= p.nz - p.pzr);
+    }
+    const int* bx = p.inj.box + shot * 6;
+    const bool inj_col = p.inj.on && j >= bx[2] && j < bx[3] && zl + V > bx[4] && zl < bx[5];
+    bool bad = false;
+    long long o = ((long long)(x0 + p.hx) * p.rows_y + (j + p.hy)) * p.ldz + kOZ + zl;
+    for (int i = x0; i < x1; ++i, o += xs) {
+        prefetch_row<T, R, MODE, true>(p, sh, o + (long long)(min(i + PGB_3D_AHEAD, x1 - 1) - i) * xs);
+        const T sx = __ldg(p.sgx + i);
+        const bool px = i < p.pxl || i >= p.nx - p.pxr;
+        const bool nearx = i - R < p.pxl || i + R >= p.nx - p.pxr;
+        const bool okx = i > 0 && i < p.nx - 1;
+        const T* u = p.u_cur + sh + o;
+        // u: Laplacian in difference form per axis and the first derivatives
+        T w[NW];
+        load_window<T, NB>(u, w);
+        T uc[V], F[V], dux[V], duy[V], duz[V];
+        {
+            VT t[2 * R];
+            load_taps<T, R>(u, xs, t);
+#pragma unroll
+            for (int v = 0; v < V; ++v) {
+                uc[v] = w[C0 + v];
+                T a2 = T(0), a1 = T(0);
+#pragma unroll
+                for (int m = 1; m <= R; ++m) {
+                    const T up = vc<T>(t[R + m - 1], v), um = vc<T>(t[R - m], v);
+                    a2 += T(d2w(R, m)) * ((up - uc[v]) + (um - uc[v]));
+                    a1 += T(d1w(R, m)) * (up - um);
+                }
+                F[v] = a2 * p.idx2;
+                dux[v] = a1 * p.idx;
+            }
+            load_taps<T, R>(u, ys, t);
+#pragma unroll
+            for (int v = 0; v < V; ++v) {
+                T a2 = T(0), a1 = T(0);
+#pragma unroll
+                for (int m = 1; m <= R; ++m) {
+                    const T up = vc<T>(t[R + m - 1], v), um = vc<T>(t[R - m], v);
+                    a2 += T(d2w(R, m)) * ((up - uc[v]) + (um - uc[v]));
+                    a1 += T(d1w(R, m)) * (up - um);
+                }
+                F[v] += a2 * p.idy2;
+                duy[v] = a1 * p.idy;
+            }
+        }
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+            T a2 = T(0), a1 = T(0);
+#pragma unroll
+            for (int m = 1; m <= R; ++m) {
+                const T up = w[C0 + v + m], um = w[C0 + v - m];
+                a2 += T(d2w(R, m)) * ((up - uc[v]) + (um - uc[v]));
+                a1 += T(d1w(R, m)) * (up - um);
+            }
+            F[v] += a2 * p.idz2;
+            duz[v] = a1 * p.idz;
+        }
+        // Phi derivatives: the state is zero outside the padding; a tap group no cell can
+        // see non-zero is skipped (one that some cells need adds exact zeros to the others)
+        if (nearx || py || any_pz) {
+            VT t[2 * R];
+            T d[V];
+            load_taps<T, R>(p.phx_in + sh + o, xs, t);
+            dd1_taps<T, R>(t, p.idx, d);
+#pragma unroll
+            for (int v = 0; v < V; ++v) F[v] += d[v];
+        }
+        if (neary || px || any_pz) {
+            VT t[2 * R];
+            T d[V];
+            load_taps<T, R>(p.phy_in + sh + o, ys, t);
+            dd1_taps<T, R>(t, p.idy, d);
+#pragma unroll
+            for (int v = 0; v < V; ++v) F[v] += d[v];
+        }
+        if (any_nearz || px || py) {
+            load_window<T, NB>(p.phz_in + sh + o, w);
+#pragma unroll
+            for (int v = 0; v < V; ++v) {
+                T a = T(0);
+#pragma unroll
+                for (int m = 1; m <= R; ++m) a += T(d1w(R, m)) * (w[C0 + v + m] - w[C0 + v - m]);
+                F[v] += a * p.idz;
+            }
+        }
+        if (inj_col) {
+#pragma unroll
+            for (int v = 0; v < V; ++v) F[v] += inject_rhs3(p.inj, bx, shot, i, j, zl + v);
+        }
+        bool psireg[V];
+        bool any_ps = false;
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+            psireg[v] = (int)px + (int)py + (int)pz[v] >= 2;
+            any_ps |= psireg[v];
+        }
+        T ps[V];
+        if (any_ps) {
+            const VT a = ldv(p.psi_in + sh + o);
+#pragma unroll
+            for (int v = 0; v < V; ++v) ps[v] = psireg[v] ? vc<T>(a, v) : T(0);
+        } else {
+#pragma unroll
+            for (int v = 0; v < V; ++v) ps[v] = T(0);
+        }
+        const VT uo_v = ldv_plain(p.u_prev + sh + o);
+        const VT c2_v = ldv(p.c2 + o);
+        alignas(16) T un[V];
+        if (sx != T(0) || sy != T(0) || any_sz) {
+            // psi derivatives where two sigmas meet (zero elsewhere, as the products they enter)
+            T dpx[V], dpy[V], dpz[V];
+#pragma unroll
+            for (int v = 0; v < V; ++v) dpx[v] = dpy[v] = dpz[v] = T(0);
+            if (sy != T(0) && any_sz) {
+                VT t[2 * R];
+                load_taps<T, R>(p.psi_in + sh + o, xs, t);
+                dd1_taps<T, R>(t, p.idx, dpx);
+            }
+            if (sx != T(0) && any_sz) {
+                VT t[2 * R];
+                load_taps<T, R>(p.psi_in + sh + o, ys, t);
+                dd1_taps<T, R>(t, p.idy, dpy);
+            }
+            if (sx != T(0) && sy != T(0)) {
+                load_window<T, NB>(p.psi_in + sh + o, w);
+#pragma unroll
+                for (int v = 0; v < V; ++v) {
+                    T a = T(0);
+#pragma unroll
+                    for (int m = 1; m <= R; ++m) a += T(d1w(R, m)) * (w[C0 + v + m] - w[C0 + v - m]);
+                    dpz[v] = a * p.idz;
+                }
+            }
+            const VT phx_v = ldv(p.phx_in + sh + o), phy_v = ldv(p.phy_in + sh + o), phz_v = ldv(p.phz_in + sh + o);
+            alignas(16) T nxo[V], nyo[V], nzo[V];
+#pragma unroll
+            for (int v = 0; v < V; ++v) {
+                const T szv = sz[v], uo = vc<T>(uo_v, v), c2 = vc<T>(c2_v, v);
+                const T phx = vc<T>(phx_v, v), phy = vc<T>(phy_v, v), phz = vc<T>(phz_v, v);
+                const bool pml = sx != T(0) || sy != T(0) || szv != T(0);
+                const bool ok = okx && okz[v];
+                const T psx = sy != T(0) && szv != T(0) ? dpx[v] : T(0);
+                const T psy = szv != T(0) && sx != T(0) ? dpy[v] : T(0);
+                const T psz = sx != T(0) && sy != T(0) ? dpz[v] : T(0);
+                const T nx_ = phx - p.dt * sx * phx + p.dt * (sy + szv - sx) * dux[v] + p.dt * (sy * szv * psx);
+                const T ny_ = phy - p.dt * sy * phy + p.dt * (szv + sx - sy) * duy[v] + p.dt * (szv * sx * psy);
+                const T nz_ = phz - p.dt * szv * phz + p.dt * (sx + sy - szv) * duz[v] + p.dt * (sx * sy * psz);
+                const T fac1 = T(2) * p.dt2 / (T(2) + p.dt * (sx + sy + szv));
+                // the reference multiplies sigma_x sigma_y sigma_z psi by C^2 (_3D.h:219); the
+                // consistent form (psi_c2 = 0) leaves it out, as the matrix operator does
+                const T src = p.psi_c2 ? c2 * (F[v] - (sx * sy * szv) * ps[v]) : c2 * F[v] - (sx * sy * szv) * ps[v];
+                const T fac2 = src - (uo - T(2) * uc[v]) * p.idt2 + (sx + sy + szv) * uo * p.i2dt -
+                               (sx * sy + sy * szv + szv * sx) * uc[v];
+                const T upml = fac1 * fac2, uplain = p.dt2 * c2 * F[v] - (uo - T(2) * uc[v]);
+                un[v] = ok ? (pml ? upml : uplain) : T(0);
+                // cells outside the padding keep their zero state
+                nxo[v] = ok && pml ? nx_ : T(0);
+                nyo[v] = ok && pml ? ny_ : T(0);
+                nzo[v] = ok && pml ? nz_ : T(0);
+            }
+            st_lane<T, false>(p.phx_out + sh + o, nxo, nv);
+            st_lane<T, false>(p.phy_out + sh + o, nyo, nv);
+            st_lane<T, false>(p.phz_out + sh + o, nzo, nv);
+        } else {
+#pragma unroll
+            for (int v = 0; v < V; ++v)
+                un[v] = okx && okz[v] ? p.dt2 * vc<T>(c2_v, v) * F[v] - (vc<T>(uo_v, v) - T(2) * uc[v]) : T(0);
+        }
+        if (any_ps) {
+            alignas(16) T pso[V];
+#pragma unroll
+            for (int v = 0; v < V; ++v) pso[v] = psireg[v] && okx && okz[v] ? ps[v] + p.dt * uc[v] : T(0);
+            st_lane<T, false>(p.psi_out + sh + o, pso, nv);
+        }
+        st_lane<T, false>(p.u_prev + sh + o, un, nv);
+        if (MODE == kRecomp && p.dw_out) {
+            const T mx = __ldg(p.mgx + i);
+            alignas(16) T dwo[V];
+#pragma unroll
+            for (int v = 0; v < V; ++v) {
+                const T szv = sz[v], mzv = mz[v], c2 = vc<T>(c2_v, v), sxyz = sx * sy * szv;
+                T d = p.psi_c2 ? c2 * (F[v] - sxyz * ps[v]) : c2 * F[v] - sxyz * ps[v];
+                d += ((mx + my + mzv) - (sx + sy + szv)) * (un[v] - vc<T>(uo_v, v)) * p.i2dt +
+                     ((mx * my + my * mzv + mzv * mx) - (sx * sy + sy * szv + szv * sx)) * uc[v] + (mx * my * mzv) * ps[v];
+                dwo[v] = okx && okz[v] ? d : T(0);
+            }
+            st_lane<T, true>(p.dw_out + sh + o, dwo, nv);
+        }
+        if (MODE == kAdj && p.image) {
+            const VT dw_v = __ldcs(reinterpret_cast<const VT*>(p.dw_in + sh + o));
+            const VT ic_v = ldv_plain(p.ic + sh + o);
+            alignas(16) T ico[V];
+#pragma unroll
+            for (int v = 0; v < V; ++v) ico[v] = vc<T>(ic_v, v) + uc[v] * vc<T>(dw_v, v);
+            st_lane<T, false>(p.ic + sh + o, ico, nv);
+        }
+        if (MODE == kFwd || (MODE == kRecomp && p.nan_check)) {
+#pragma unroll
+            for (int v = 0; v < V; ++v) bad |= v < nv && !isfinite(un[v]);
+        }
+    }
+    if (MODE != kAdj && bad && p.err) atomicOr(p.err, PGB_ERR_NONFINITE);
+}
+
 // 1D: one axis (z), Phi_z only (_1D.h:117-129).
 template <typename T, int R, int MODE>
 __global__ void __launch_bounds__(256) wave1d_kernel(const WaveParams<T> p, int ntile) {
@@ -407,11 +633,17 @@ void launch_wave3d_tasks(const WaveParams<T>& p, const int* tasks, int ntasks, c
     if (KIND == 0)
         wave3d_interior_kernel<T, R, MODE><<<grid, kW3 * 32, 0, s>>>(p, tasks, ntasks);
     else
-        wave3d_shell_kernel<T, R, MODE><<<grid, kW3 * 32, 0, s>>>(p, tasks, ntasks);
+        wave3d_shell_kernel<T, R, MODE><<<grid, kW3S * 32, 0, s>>>(p, tasks, ntasks);
 }
 
-int wave3d_rows_per_block() { return kW3; }
-int wave3d_seg(int dtype_bytes, int kind) { return kind == 0 ? 32 * (16 / dtype_bytes) : 32; }
+int wave3d_seg(int dtype_bytes, int kind) {
+    (void)kind;
+    return 32 * (16 / dtype_bytes);
+}
+int wave3d_task_rows(int dtype_bytes, int kind, int zcells) {
+    const int V = 16 / dtype_bytes;
+    return kind == 0 ? kW3 : kW3S * (32 / ((zcells + V - 1) / V));
+}
 
 template <typename T, int R, int MODE>
 void launch_wave1d(const WaveParams<T>& p, int bz, cudaStream_t s) {
