@@ -71,7 +71,10 @@ __device__ __forceinline__ T dd2(const T* __restrict__ v, int s) {
 // about once; the x- and y-neighbours are constant offsets from the centre row.
 constexpr int kW3 = 8;  // warps (y-rows) per block
 #ifndef PGB_3D_AHEAD
-#define PGB_3D_AHEAD 2     // rows ahead whose operands are prefetched into L1
+#define PGB_3D_AHEAD 1     // interior: rows ahead whose operands are prefetched into L1 (0: none)
+#endif
+#ifndef PGB_3D_SHELL_AHEAD
+#define PGB_3D_SHELL_AHEAD 1  // the same for the PML shell
 #endif
 
 // L1 prefetch of the line holding q (the addresses used are rows the task reads)
@@ -184,7 +187,8 @@ __global__ void __launch_bounds__(kW3 * 32, (sizeof(T) == 4 ? PGB_3D_INT_MINB : 
     bool bad = false;
     long long o = ((long long)(x0 + p.hx) * p.rows_y + (j + p.hy)) * p.ldz + kOZ + zl;
     for (int i = x0; i < x1; ++i, o += xs) {
-        prefetch_row<T, R, MODE, false>(p, sh, o + (long long)(min(i + PGB_3D_AHEAD, x1 - 1) - i) * xs);
+        if (PGB_3D_AHEAD > 0)
+            prefetch_row<T, R, MODE, false>(p, sh, o + (long long)(min(i + PGB_3D_AHEAD, x1 - 1) - i) * xs);
         const T* u = p.u_cur + sh + o;
         T w[NW];
 #pragma unroll
@@ -382,7 +386,8 @@ __global__ void __launch_bounds__(kW3S * 32, (sizeof(T) == 4 ? PGB_3D_SHELL_MINB
     bool bad = false;
     long long o = ((long long)(x0 + p.hx) * p.rows_y + (j + p.hy)) * p.ldz + kOZ + zl;
     for (int i = x0; i < x1; ++i, o += xs) {
-        prefetch_row<T, R, MODE, true>(p, sh, o + (long long)(min(i + PGB_3D_AHEAD, x1 - 1) - i) * xs);
+        if (PGB_3D_SHELL_AHEAD > 0)
+            prefetch_row<T, R, MODE, true>(p, sh, o + (long long)(min(i + PGB_3D_SHELL_AHEAD, x1 - 1) - i) * xs);
         const T sx = __ldg(p.sgx + i);
         const bool px = i < p.pxl || i >= p.nx - p.pxr;
         const bool nearx = i - R < p.pxl || i + R >= p.nx - p.pxr;
