@@ -330,7 +330,7 @@ struct PlanT final : public pysit_plan {
     unsigned wait_polls = 0;     // tries of a step kernel's bulk-copy wait (0: the kernels' default)
     int wait_fault = 0;          // test aid: the 2D step kernels' waits run out (pysit_plan_desc.wait_fault)
     std::vector<int> shot_steps; // record length of each shot in steps (empty: all nsteps)
-    size_t task_cap = 0;         // ints the task buffer holds (enough for the shortest x-chunk)
+    size_t task_cap = 0;         // ints the task buffer holds (enough for any tile the tuner may set)
     double dx, dy, dz, dt;
     int pad_lo[3], pad_hi[3];
     int pl[3], pr[3];  // PML-state widths (kernel profile lengths)
@@ -534,6 +534,27 @@ struct PlanT final : public pysit_plan {
         int width = ((b - a + n - 1) / n + 3) / 4 * 4;
         for (int z = a; z < b; z += width) out.push_back({z, std::min(b, z + width)});
     }
+    // 3D z segments of at most w cells (w a multiple of 4 and of V): the even split, or
+    // full w-wide segments and a remainder, whichever leaves fewer lanes idle.  A warp
+    // takes 32 / nv rows of a segment of nv vectors, so a narrow remainder fills a warp
+    // with several rows.
+    void split3d(int a, int b, int w, std::vector<std::pair<int, int>>& out) const {
+        constexpr int V = V16<T>::N;
+        auto eff = [&](const std::vector<std::pair<int, int>>& seg) {
+            double used = 0, slots = 0;
+            for (auto& z : seg) {
+                const int nv = (z.second - z.first + V - 1) / V;
+                used += nv;
+                slots += 32.0 / (32 / nv);  // lane slots one row of the segment takes
+            }
+            return slots > 0 ? used / slots : 0.0;
+        };
+        std::vector<std::pair<int, int>> even, full;
+        split(a, b, w, even);
+        for (int z = a; z < b; z += w) full.push_back({z, std::min(b, z + w)});
+        const auto& pick = eff(full) > eff(even) + 1e-9 ? full : even;
+        out.insert(out.end(), pick.begin(), pick.end());
+    }
     void add_tasks(int xa, int xb, int za, int zb, int kind) {
         if (xb <= xa || zb <= za) return;
         std::vector<std::pair<int, int>> zs;
@@ -581,7 +602,7 @@ struct PlanT final : public pysit_plan {
         std::vector<std::pair<int, int>> zs;
         int w = wave3d_seg((int)sizeof(T), kind);
         if (kind == 0 && tz > 0) w = std::min(w, tz);
-        split(za, zb, w, zs);
+        split3d(za, zb, w, zs);
         const int nxc = (xb - xa + tx - 1) / tx, wx = (xb - xa + nxc - 1) / nxc;
         for (int x = xa; x < xb; x += wx)
             for (auto& z : zs)
@@ -760,7 +781,11 @@ struct PlanT final : public pysit_plan {
         off.err = take(sizeof(int));
         off.ctr = take(2 * sizeof(unsigned long long));
         off.shsteps = take(std::max<size_t>(shot_steps.size(), 1) * sizeof(int));
-        task_cap = std::max<size_t>(task_ints(kMinTileX, kMinTileZ), std::max(tasks2d.size(), tasks3d.size()));
+        // the largest table any tuning can ask for: the shortest x-chunk, and every z extent
+        // (in 3D a narrower segment can give more tasks: its warps take several rows, but
+        // not always enough to make up for the extra segments)
+        task_cap = std::max<size_t>(task_ints(kMinTileX, 0), std::max(tasks2d.size(), tasks3d.size()));
+        for (int z = kMinTileZ; z <= 32 * V16<T>::N; z += 4) task_cap = std::max(task_cap, task_ints(kMinTileX, z));
         off.tasks = take(std::max<size_t>(task_cap, 1) * sizeof(int));
         off.partial = take(kRedBlocks * sizeof(double));
         off.rnorm = take(sizeof(double));

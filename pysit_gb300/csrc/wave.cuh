@@ -235,8 +235,8 @@ int wave2d_warp_seg(int dtype_bytes, int order, int pml);
 // resident task blocks of the whole GPU for one (dtype, order, mode, kind)
 int wave2d_warp_blocks(int dtype_bytes, int order, int mode, int kind);
 void wave2d_warp_prepare();
-// 3D block tasks (x0, x1, y0, y1, zs, ze): one block per task and shot; KIND 0
-// interior (one y-row per warp), 1 PML shell (32 / vectors-of-z rows per warp)
+// 3D block tasks (x0, x1, y0, y1, zs, ze): one block per task and shot (KIND 0
+// interior, 1 PML shell); a warp takes 32 / (vectors of the z-range) y-rows
 template <typename T, int R, int MODE, int KIND>
 void launch_wave3d_tasks(const WaveParams<T>& p, const int* tasks, int ntasks, cudaStream_t s);
 int wave3d_seg(int dtype_bytes, int kind);  // widest z-range of a task of each kind

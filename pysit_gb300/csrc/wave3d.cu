@@ -151,7 +151,8 @@ __device__ __forceinline__ typename Vec3<T>::type ldv_plain(const T* q) {
 
 // Interior: 16-byte vectors (V cells per lane), arithmetic on cell pairs, no PML
 // state (every tap is off the padding), no masks (off the outer ring).  Task
-// z-bounds are multiples of 4 cells, so every vector load is aligned.
+// z-bounds are multiples of 4 cells, so every vector load is aligned; a task whose
+// z-range is at most 16 vectors gives a warp several y-rows (wave3d_task_rows).
 #ifndef PGB_3D_INT_MINB
 #define PGB_3D_INT_MINB 2  // resident interior blocks per SM the register budget aims at (FP32)
 #endif
@@ -169,9 +170,12 @@ __global__ void __launch_bounds__(kW3 * 32, (sizeof(T) == 4 ? PGB_3D_INT_MINB : 
     constexpr int C0 = NB * V;
     const int shot = blockIdx.x / ntasks;
     const int* tk = tasks + 6 * (blockIdx.x - shot * ntasks);
-    const int j = __ldg(tk + 2) + (threadIdx.x >> 5);
-    const int zl = __ldg(tk + 4) + (threadIdx.x & 31) * V;
-    if (j >= __ldg(tk + 3) || zl >= __ldg(tk + 5)) return;
+    // the task's z-range takes nzv lanes of a y-row and a warp 32 / nzv rows
+    const int zs = __ldg(tk + 4), nzv = (__ldg(tk + 5) - zs) / V, rpw = 32 / nzv;
+    const int lane = threadIdx.x & 31, r = lane / nzv;
+    const int j = __ldg(tk + 2) + (threadIdx.x >> 5) * rpw + r;
+    if (r >= rpw || j >= __ldg(tk + 3)) return;
+    const int zl = zs + (lane - r * nzv) * V;
     const int x0 = __ldg(tk), x1 = __ldg(tk + 1);
     const long long sh = (long long)shot * p.fstride;
     const long long ys = p.ldz, xs = (long long)p.rows_y * p.ldz;
@@ -647,7 +651,7 @@ int wave3d_seg(int dtype_bytes, int kind) {
 }
 int wave3d_task_rows(int dtype_bytes, int kind, int zcells) {
     const int V = 16 / dtype_bytes;
-    return kind == 0 ? kW3 : kW3S * (32 / ((zcells + V - 1) / V));
+    return (kind == 0 ? kW3 : kW3S) * (32 / ((zcells + V - 1) / V));
 }
 
 template <typename T, int R, int MODE>
