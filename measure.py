@@ -261,10 +261,12 @@ def run_gradient3d(scale=1.0, nshots=8, nsteps=3000, autotune=True):
 
 
 def run_steps(workload="cfg2", scale=1.0, nshots=None, nsteps=64, shots_per_launch=None, reps=32,
-              schedule="checkpoint"):
+              schedule="checkpoint", tile=None):
     """Per-launch times of the three step kernels (forward, recompute, adjoint) of a workload's
     first shot group, each timed alone with CUDA events (pysit_plan_step_loop), with the
-    algorithmic bytes of the step and Gcell/s (a benchmarking aid for profiling)."""
+    algorithmic bytes of the step and Gcell/s (a benchmarking aid for profiling).  `tile` sets
+    the x task length (default: the plan's own); the timed loops run inside the NVTX range
+    `steps`, so that a profiler can pick out their launches."""
     import torch
 
     from pysit_gb300.engine import WavePlan
@@ -278,6 +280,8 @@ def run_steps(workload="cfg2", scale=1.0, nshots=None, nsteps=64, shots_per_laun
     solver.model_parameters = solver.ModelParameters(m, {"C": C0})
     # (with the kept schedule the recompute-mode launches also record traces, as its forward sweep does)
     plan = WavePlan(solver, shots, shots_per_launch=shots_per_launch or len(shots), gradient_schedule=schedule)
+    if tile:
+        plan.autotune(candidates=[int(tile)], nsteps=4, z_candidates=[0])
     plan.forward()
     torch.cuda.synchronize()
     n_all = int(np.prod(m.shape(include_bc=True, as_grid=True)))
@@ -286,14 +290,17 @@ def run_steps(workload="cfg2", scale=1.0, nshots=None, nsteps=64, shots_per_laun
     w = 4 if solver.precision == "single" else 8
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     out = {"workload": workload, "scale": scale, "grid": [int(v) for v in m.shape(include_bc=True, as_grid=True)],
-           "shots_per_launch": plan.shots_per_launch, "schedule": plan.gradient_schedule, "modes": {}}
+           "shots_per_launch": plan.shots_per_launch, "schedule": plan.gradient_schedule,
+           "tile_x": plan.tile_x or "plan default", "modes": {}}
     for mode, name, extra in ((0, "forward", 0), (1, "recompute", 1), (2, "adjoint", 3)):
         plan.step_loop(mode, 4)
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push("steps")
         e0.record()
         plan.step_loop(mode, reps)
         e1.record()
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
         ms = e0.elapsed_time(e1) / reps
         nb = w * ((4 + extra) * n_int + (4 + pml_extra[0] + extra) * n_pml) * plan.shots_per_launch
         out["modes"][name] = {"launch_ms": ms, "gbs": nb / (ms * 1e-3) / 1e9,
@@ -343,6 +350,7 @@ def _main(argv=None):
     ap.add_argument("--shots", type=int, default=None, help="default 256 (cfg4), 128 (cfg5)")
     ap.add_argument("--nsteps", type=int, default=4000)
     ap.add_argument("--scale", type=float, default=1.0)
+    ap.add_argument("--tile", type=int, default=None, help="steps2d / steps3d: x task length (default: the plan's)")
     ap.add_argument("--plain", action="store_true", help="per-shot FP64 objective instead of the batched FP32 one")
     ap.add_argument("--precision", default="single", choices=["single", "double"],
                     help="cfg5 / gn: precision of the batched objective")
@@ -372,7 +380,7 @@ def _main(argv=None):
     if a.workload in ("steps2d", "steps3d"):
         out = run_steps("cfg2" if a.workload == "steps2d" else "cfg3", scale=a.scale, nshots=a.shots,
                         nsteps=a.nsteps, shots_per_launch=a.shots_per_launch,
-                        schedule="store" if a.schedule == "store" else "checkpoint")
+                        schedule="store" if a.schedule == "store" else "checkpoint", tile=a.tile)
         print(json.dumps(out))
         return
     if a.workload == "hessian":
