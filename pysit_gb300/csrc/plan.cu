@@ -32,6 +32,10 @@
 
 #include "wave.cuh"
 
+#ifndef PGB_REC_BLOCKS_PER_SM
+#define PGB_REC_BLOCKS_PER_SM 1  // 2D recorder blocks per SM (leading blocks of the interior kernel)
+#endif
+
 namespace pgb {
 namespace {
 
@@ -357,6 +361,7 @@ struct PlanT final : public pysit_plan {
     bool rec_in_shell = false;        // 2D: every receiver box lies in cells of PML-shell tasks only
     std::vector<int> rec_rows;        // [nshots*nrec+1]
     int rec_lanes = 1;                // recorder threads per (shot, receiver)
+    mutable int rec_cap = 0;          // 2D: recorder blocks at most (a share of the block slots; 0: not yet known)
     std::vector<long long> rec_off;   // internal offsets
     std::vector<double> rec_ws;       // sampling weights
     std::vector<double> src_amp;      // [nshots][nsteps][nsrc]
@@ -1469,7 +1474,20 @@ struct PlanT final : public pysit_plan {
         p.rec.tr_sstride = (long long)nsteps * nrec;
         p.rec.nrec = nrec;
         p.rec.lanes = rec_lanes;
-        p.rec.blocks = nrec > 0 ? ceil_div((long long)gn * nrec * rec_lanes, bz) : 0;
+        // 2D: the recorder blocks lead the interior kernel's grid and hold one of its block
+        // slots each while they run, so a few of them stride over the receivers and the step's
+        // own blocks take the other slots from the start
+        if (rec_cap == 0) {
+            int dev = 0, sms = 0;
+            if (cudaGetDevice(&dev) != cudaSuccess ||
+                cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+                cudaGetLastError();
+                sms = 1;
+            }
+            rec_cap = std::max(1, sms * PGB_REC_BLOCKS_PER_SM);
+        }
+        const long long need = nrec > 0 ? ceil_div((long long)gn * nrec * rec_lanes, bz) : 0;
+        p.rec.blocks = (int)(dim == 2 ? std::min<long long>(need, (long long)rec_cap) : need);
     }
 
     void enqueue_forward(void* traces_out, cudaStream_t s) {

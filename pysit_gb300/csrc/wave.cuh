@@ -185,41 +185,47 @@ __device__ __forceinline__ T inject_rhs(const Inject<T>& inj, const int* bx, int
     return acc;
 }
 
-// trace recorder block: p.rec.lanes threads per (shot, receiver).  Lane l sums taps
-// l, l + lanes, ... in order; a fixed butterfly over the lanes adds the partial sums,
-// so the result does not depend on scheduling.  Every thread of the block takes part
-// (the butterfly shuffles over whole warps).
+// trace recorder block: p.rec.lanes threads per (shot, receiver), the p.rec.blocks
+// recorder blocks striding over the receivers.  Lane l sums taps l, l + lanes, ... in
+// order, up to 8 of them with their loads in flight together; a fixed butterfly over the
+// lanes adds the partial sums, so the result does not depend on scheduling.  Every thread
+// of the block takes part (the butterfly shuffles over whole warps).
 template <typename T>
 __device__ __forceinline__ void record_block(const WaveParams<T>& p, int rb) {
+    constexpr int kTaps = 8;
     const int G = p.rec.lanes;
     const long long t = (long long)rb * blockDim.x + threadIdx.x;
-    const long long id = t / G;
     const int l = (int)(t & (G - 1));
     const long long total = (long long)p.nshot * p.rec.nrec;
-    T acc = T(0);
-    if (id < total) {
-        const int shot = (int)(id / p.rec.nrec);
-        const int e1 = __ldg(p.rec.rowptr + id + 1);
-        const T* u = p.u_cur + (long long)shot * p.fstride;
-        int e = __ldg(p.rec.rowptr + id) + l;
-        // a lane's taps in groups of 4: offsets and weights first, then the wavefield
-        // values, so that a group's dependent loads are in flight together
-        for (; e + 3 * G < e1; e += 4 * G) {
-            long long off[4];
-            T w[4], v[4];
+    const long long pass = (long long)p.rec.blocks * blockDim.x / G;  // receivers per pass
+    for (long long base = 0; base < total; base += pass) {           // the same count on every lane
+        const long long id = base + t / G;
+        T acc = T(0);
+        if (id < total) {
+            const int shot = (int)(id / p.rec.nrec);
+            const int e1 = __ldg(p.rec.rowptr + id + 1);
+            const T* u = p.u_cur + (long long)shot * p.fstride;
+            for (int e = __ldg(p.rec.rowptr + id) + l; e < e1; e += kTaps * G) {
+                long long off[kTaps];
+                T w[kTaps], v[kTaps];
 #pragma unroll
-            for (int q = 0; q < 4; ++q) { off[q] = __ldg(p.rec.off + e + q * G); w[q] = __ldg(p.rec.w + e + q * G); }
+                for (int q = 0; q < kTaps; ++q) {
+                    const bool in = e + q * G < e1;
+                    off[q] = in ? __ldg(p.rec.off + e + q * G) : 0;
+                    w[q] = in ? __ldg(p.rec.w + e + q * G) : T(0);
+                }
 #pragma unroll
-            for (int q = 0; q < 4; ++q) v[q] = __ldg(u + off[q]);
+                for (int q = 0; q < kTaps; ++q) v[q] = e + q * G < e1 ? __ldg(u + off[q]) : T(0);
 #pragma unroll
-            for (int q = 0; q < 4; ++q) acc += w[q] * v[q];
+                for (int q = 0; q < kTaps; ++q)
+                    if (e + q * G < e1) acc += w[q] * v[q];
+            }
         }
-        for (; e < e1; e += G) acc += __ldg(p.rec.w + e) * __ldg(u + __ldg(p.rec.off + e));
-    }
-    for (int m = G >> 1; m > 0; m >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, m);
-    if (id < total && l == 0) {
-        const int shot = (int)(id / p.rec.nrec), r = (int)(id - (long long)shot * p.rec.nrec);
-        p.rec.traces[shot * p.rec.tr_sstride + r] = acc;
+        for (int m = G >> 1; m > 0; m >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, m);
+        if (id < total && l == 0) {
+            const int shot = (int)(id / p.rec.nrec), r = (int)(id - (long long)shot * p.rec.nrec);
+            p.rec.traces[shot * p.rec.tr_sstride + r] = acc;
+        }
     }
 }
 
