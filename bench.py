@@ -17,8 +17,8 @@ shots per launch as fit, no recompute sweep; the same gradient to the last bit),
          alone with CUDA events): algorithmic bytes per launch / mean launch
          time, against the measured HBM copy peak; all three under "modes"
   plain_fp64  the plain path: PySIT's per-shot, per-step loop in FP64 over the
-         per-step CUDA kernels, one shot on a bounded sample of steps
-         (extrapolated), and the batched/plain speed-up
+         per-step CUDA kernels, one whole shot-gradient (the path runs shot after
+         shot), and the batched/plain speed-up
   cpu_baseline  the CPU oracle port of the same pipeline on the host cores, on
          a bounded sample of steps, extrapolated to a full gradient
   kept_schedule  (checkpointed runs at N=1) the same gradient with dWaveOp kept
@@ -219,11 +219,13 @@ def accuracy_vs_fp64(obs_host, ts_obs, scale, nshots, nsteps, nshots_check=8):
                                "reference": "FP64 batched gradient of the same shots and observed data"}}
 
 
-def plain_fp64_baseline(scale=1.0, nsteps_full=4000, nsample=1024, order=8):
+def plain_fp64_baseline(scale=1.0, nsteps_full=4000, nsample=None, order=8):
     """The plain path on the GPU: PySIT's per-shot, per-step control flow
     (TemporalLeastSquares.compute_gradient, temporal_least_squares.py:141-198) in FP64 over the
-    per-step CUDA kernels, one shot of the same grid timed over `nsample` steps and extrapolated
-    to the full step count (its cost per step does not depend on the number of steps)."""
+    per-step CUDA kernels: one whole shot-gradient of the same grid (all `nsteps_full` steps,
+    unless `nsample` asks for fewer, which are then scaled to the full count: the cost per step
+    does not depend on the number of steps); the path runs shot after shot, so shots/s is the
+    inverse of that time."""
     import torch
     import pysit_gb300 as api
     from pysit_gb300 import workloads
@@ -240,10 +242,11 @@ def plain_fp64_baseline(scale=1.0, nsteps_full=4000, nsample=1024, order=8):
         return time.perf_counter() - t0, solver.nsteps
 
     run(32)  # warm-up (kernels, allocator)
-    t, ns = run(nsample)
+    t, ns = run(nsample or nsteps_full)
     per_shot = t / ns * nsteps_full
-    return {"value": 1.0 / per_shot, "unit": "shots/s", "dtype": "f64",
-            "sample": f"1 shot x {ns} steps of the same grid, extrapolated to {nsteps_full} steps; wall {t:.2f}s"}
+    what = (f"1 shot-gradient of the same grid, all {ns} steps" if ns >= nsteps_full else
+            f"1 shot x {ns} steps of the same grid, scaled to {nsteps_full} steps")
+    return {"value": 1.0 / per_shot, "unit": "shots/s", "dtype": "f64", "sample": f"{what}; wall {t:.2f}s"}
 
 
 # ---------------------------------------------------------------------------
