@@ -294,6 +294,14 @@ int pysit_plan_autotune_tiles(pysit_plan* plan, const int* cand_x, int ncx, cons
                               int nsteps, int* chosen_x, int* chosen_z, double* ms, void* stream);
 /* The plan's current task length along x and z extent of its interior tasks (0: full width). */
 int pysit_plan_get_tiles(const pysit_plan* plan, int* tile_x, int* tile_z);
+/* A host copy of the plan's current task table, no counterpart in the reference (diagnostics
+ * and tests; needs no device).  2D: rows of 5 ints (x0, x1, zs, ze, kind: 0 interior, 1 PML
+ * shell), the warp tasks of one shot; 3D: rows of 6 ints (x0, x1, y0, y1, zs, ze), one block of
+ * 8 warps each, a warp taking 32 / ceil((ze - zs) / V) y-rows (V = 4 FP32, 2 FP64 cells a lane);
+ * 1D: none.  The interior tasks come first, *n_interior of them.  *n_ints receives the table's
+ * size in ints; at most cap ints are written to out (which may be NULL). */
+int pysit_plan_task_table(const pysit_plan* plan, int32_t* out, uint64_t cap, uint64_t* n_ints,
+                          int32_t* n_interior);
 /* The plan's current tuning: task length along x and the three 2D shell block shares
  * (pysit_plan_desc.shell_share).  Either output may be NULL. */
 int pysit_plan_get_tuning(const pysit_plan* plan, int* tile_x, double* shell_share);

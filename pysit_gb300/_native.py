@@ -99,6 +99,8 @@ _PROTOS = {
     "pysit_plan_autotune_tiles": (_i, [_vp, C.POINTER(_i), _i, C.POINTER(_i), _i, _i, C.POINTER(_i), C.POINTER(_i),
                                        C.POINTER(C.c_double), _vp]),
     "pysit_plan_get_tiles": (_i, [_vp, C.POINTER(_i), C.POINTER(_i)]),
+    "pysit_plan_task_table": (_i, [_vp, C.POINTER(C.c_int32), C.c_uint64, C.POINTER(C.c_uint64),
+                                   C.POINTER(C.c_int32)]),
     "pysit_group_create": (_i, [C.POINTER(_vp), _i, C.POINTER(_vp)]),
     "pysit_group_destroy": (_i, [_vp]),
     "pysit_group_gradient": (_i, [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp), _vp]),

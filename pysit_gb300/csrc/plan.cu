@@ -311,6 +311,8 @@ struct pysit_plan {
     virtual int autotune2(const int* cx, int ncx, const int* cz, int ncz, int nsteps, int* chosen_x,
                           int* chosen_z, double* ms, cudaStream_t s) = 0;
     virtual int tiles(int* tile_x, int* tile_z) const = 0;
+    // host copy of the current task table (interior tasks first)
+    virtual int task_table(int32_t* out, uint64_t cap, uint64_t* n_ints, int32_t* n_interior) const = 0;
     // enqueue misfit + gradient on s without graph handling (for a group's capture)
     virtual int enqueue_grad_raw(const void* dobs, double* grad, double* rnorm2, cudaStream_t s) = 0;
     // linearised modelling / Gauss-Newton Hessian application for a model perturbation
@@ -1443,6 +1445,15 @@ struct PlanT final : public pysit_plan {
         return PYSIT_OK;
     }
 
+    int task_table(int32_t* out, uint64_t cap, uint64_t* n_ints, int32_t* n_interior) const override {
+        static const std::vector<int> none;
+        const std::vector<int>& tab = dim == 3 ? tasks3d : dim == 2 ? tasks2d : none;
+        if (n_ints) *n_ints = tab.size();
+        if (n_interior) *n_interior = dim == 3 ? ntask3d[0] : dim == 2 ? ntask2d[0] : 0;
+        if (out) std::copy_n(tab.begin(), std::min<size_t>((size_t)cap, tab.size()), out);
+        return PYSIT_OK;
+    }
+
     int tuning(int* tile, double* share) const override {
         if (tile) *tile = tx;
         if (share)
@@ -1926,6 +1937,9 @@ struct LanesPlan final : public pysit_plan {
     }
     int tuning(int* tile, double* share) const override { return kids[0]->tuning(tile, share); }
     int tiles(int* tile_x, int* tile_z) const override { return kids[0]->tiles(tile_x, tile_z); }
+    int task_table(int32_t* out, uint64_t cap, uint64_t* n_ints, int32_t* n_interior) const override {
+        return kids[0]->task_table(out, cap, n_ints, n_interior);
+    }
 };
 
 }  // namespace
@@ -2070,6 +2084,12 @@ extern "C" int pysit_plan_get_tiles(const pysit_plan* p, int* tile_x, int* tile_
     PGB_REQUIRE(p, "NULL plan");
     return p->tiles(tile_x, tile_z);
 } PGB_API_CATCH("pysit_plan_get_tiles")
+
+extern "C" int pysit_plan_task_table(const pysit_plan* p, int32_t* out, uint64_t cap, uint64_t* n_ints,
+                                     int32_t* n_interior) try {
+    PGB_REQUIRE(p, "NULL plan");
+    return p->task_table(out, cap, n_ints, n_interior);
+} PGB_API_CATCH("pysit_plan_task_table")
 
 // ---- plan groups ------------------------------------------------------------------------
 struct pysit_group {
