@@ -47,8 +47,8 @@ def test_autograd_forward_without_grad_gives_the_misfit(golden):
 # The tolerance is loose on purpose: the gradient is the reference's discrete adjoint (the
 # adjoint-state sweep of temporal_modeling.py:228-387 with its imaging condition), which is not the
 # exact derivative of the discrete misfit (the PML and the time-stepping are not differentiated
-# exactly), so it differs from the centred finite difference by about a percent.  Exactness against
-# the reference itself is held by the golden-gradient tests (1e-10 and tighter).
+# exactly), so it differs from the centred finite difference by about a percent.  Agreement with
+# the reference itself is held by the golden-gradient tests (FP64 gradient within 1e-9).
 @pytest.mark.parametrize("precision,tol", [("double", 2e-2), ("single", 3e-2)])
 def test_directional_derivative_matches_finite_difference(precision, tol):
     import torch
