@@ -44,6 +44,10 @@ DEEP_SPECS = {
                  f=25.0, model="layered", nsrc=2, nrec=20, sdepth=2000.0, rdepth=1800.0),
     "deep3d": dict(dim=3, n=(15, 13, 161), L=(140.0, 120.0, 1600.0), pml=(5, 5.0), order=8, T=0.14, cfl=0.25,
                    f=30.0, model="layered", nsrc=(1, 1), nrec=(3, 3), sdepth=800.0, rdepth=700.0),
+    # many receivers (12 shots x 501, about 47 taps each): more receiver threads than the 2D trace
+    # recorder's blocks hold at once, so the recorder strides over the receivers in several passes
+    "manyrec": dict(dim=2, n=(501, 47), L=(5000.0, 460.0), pml=(9, 170.0), order=8, T=0.3, cfl=0.3,
+                    f=20.0, model="random", nsrc=12, nrec="max", sdepth=50.0, rdepth=30.0),
 }
 
 

@@ -49,6 +49,11 @@ def deep3d():
     return _oracle("deep3d")
 
 
+@pytest.fixture(scope="module")
+def manyrec():
+    return _oracle("manyrec")
+
+
 def _gpu(name, precision, schedule, dobs):
     import torch
     from pysit_gb300.engine import WavePlan
@@ -89,3 +94,11 @@ def test_deep_2d_grid_matches_the_oracle(deep2d):
 def test_deep_3d_grid_matches_the_oracle(deep3d):
     assert deep3d["nz"] - 2 * (5 + 4) > 128
     _check(deep3d, "deep3d")
+
+
+def test_many_receivers_match_the_oracle(manyrec):
+    # 12 x 501 receivers at 8 recorder threads each exceed the 128-thread recorder blocks of one
+    # block per SM (152 on a GB300) several times over
+    nshots, _, nrec = manyrec["traces"].shape
+    assert nshots * nrec * 8 > 2 * 152 * 128
+    _check(manyrec, "manyrec")
