@@ -471,6 +471,10 @@ struct PlanT final : public pysit_plan {
         ldz = ((kOZ + nz + kTailZ) + 31) / 32 * 32;
         fstride = (long long)(nx + 2 * hx) * rows_y * ldz;
         fstride = (fstride + 63) / 64 * 64;
+        // the 3D shell kernel addresses its taps with 32-bit offsets of up to R x-planes
+        PGB_REQUIRE(dim < 3 || (long long)kHalo * rows_y * ldz < (1LL << 31),
+                    "3D x-plane of %lld elements is too large (R planes must stay below 2^31 elements)",
+                    (long long)rows_y * ldz);
         field_bytes = (size_t)fstride * G * sizeof(T);
         nseg = (nsteps + S - 1) / S;
         nslots = store_all ? (nsteps + p_img - 1) / p_img : S;

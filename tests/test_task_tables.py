@@ -140,3 +140,11 @@ def test_task_table_of_a_1d_plan_is_empty(lib):
     keep = []
     tab, nint = _table(lib, _desc(keep, 1, (1, 1, 120), ((0, 0), (0, 0), (10, 10)), 4, _native.PYSIT_F64))
     assert tab.size == 0 and nint == 0
+
+
+def test_3d_plan_refuses_x_planes_beyond_32_bit_tap_offsets(lib):
+    keep = []
+    d = _desc(keep, 3, (12, 24000, 24000), ((2, 2), (2, 2), (2, 2)), 4, _native.PYSIT_F32)
+    h = C.c_void_p()
+    assert lib.pysit_plan_create(C.byref(d), C.byref(h)) == _native.PYSIT_EINVAL
+    assert b"x-plane" in lib.pysit_cuda_last_error()
